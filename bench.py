@@ -1,0 +1,406 @@
+"""Benchmark of the co-kriging hot path on one workload.
+
+Workload (one "step"): the precision configuration -- one series, 4000
+surface points on 8 folded surfaces, 1500 orientations (N = 8498), cubic
+kernel, linear drift, a 256^3 regular grid (16.8M points): kriging-matrix
+build, solve, isovalues, evaluation with fused segmentation, series
+combination.  ``value`` is grid points/s of the mixed form (FP64 build, FP32
+LU + FP64 FGMRES, FP32 evaluation with FP64 isovalues) with inputs resident in
+HBM; the plain FP64 form is timed on the same inputs in the same run.
+``e2e`` runs the same step through ``gempy_gb300.compute_model`` from host
+(numpy) inputs with the host<->device copies inside the timed region.
+
+``--impl reference`` times the CPU restatement of the reference's algorithm
+(the FP64 oracle; the reference's own engine is not available) on a bounded
+sample of the same workload, with all host threads.
+
+Multi-GPU: the path runs as independent replicas (one per rank), no
+collective on the data path; ``value`` sums all ranks' points over the slowest
+rank's time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "grid points/s + kriging solves/s: mixed/learned vs FP64 GPU at 1e-6 field error"
+WORKLOAD = ("precision: 1 series, 4000 surface points on 8 folded surfaces, 1500 orientations "
+            "(N=8498), cubic, linear drift, 256^3 regular grid")
+
+# algorithmic work per unit (fixed constants: F_C = 20 per surface-point kernel,
+# F_G = 30 per orientation kernel, 2N for the drift/weights, x2 with gradients)
+F_C, F_G, F_K = 20, 30, 40
+
+
+def eval_flops_per_point(n_p, n_k, n_o, N, gradient=False):
+    f = (n_p + n_k) * F_C + n_o * F_G + 2 * N
+    return 2 * f if gradient else f
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        d["_source"] = "measured"
+        return d
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0, "_source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi sampling during the timed region (read only)."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{index}.csv") \
+            if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else f"/tmp/gk_clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    rows.append((float(parts[1]), float(parts[2]), float(parts[3]), parts[5:9]))
+                except ValueError:
+                    continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = np.array([r[0] for r in rows])
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i, v in enumerate(r[3]) if v.lower() == "active"})
+        load = sm[sm > 0.5 * sm.max()] if len(sm) else sm
+        return {"sm_mhz": float(np.median(load)), "sm_max_mhz": float(rows[0][1]), "reasons": reasons,
+                "samples": len(rows), "power_w_max": float(max(r[2] for r in rows))}
+
+
+def count_kernels(fn):
+    """Kernel launches of one call of fn (profiler trace outside the timed region)."""
+    import torch
+    from torch.profiler import ProfilerActivity, profile
+    with profile(activities=[ProfilerActivity.CUDA]) as prof:
+        fn()
+        torch.cuda.synchronize()
+    n, ours = 0, 0
+    for e in prof.events():
+        if getattr(e, "device_type", None) is not None and str(e.device_type).endswith("CUDA"):
+            n += 1
+            name = e.name
+            if any(k in name for k in ("gk::", "build_kernel", "panel_kernel", "eval_kernel", "trsv", "gemm_update",
+                                       "laswp", "trsm", "gemv", "dots_", "combine", "pack_kernel", "alpha_",
+                                       "equil", "convert", "scale", "from_f32", "sub_basis", "add_basis",
+                                       "perm_from", "gather", "corners", "mark_count", "scan_blocks", "scatter")):
+                ours += 1
+    return ours, n
+
+
+def reference_arm(args):
+    """CPU restatement timed on the host cores (bounded sample per step)."""
+    import torch  # noqa: F401  (rank handling below uses env only)
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from gempy_gb300 import synthetic
+    from oracle import kriging, segmentation
+    from tests._models import oracle_series_list
+    m = synthetic.precision()
+    (s,) = oracle_series_list(m)
+    grid = m.interpolation_input.grid.dense_grid
+    n_total = grid.n_points
+    rng = np.random.default_rng(0)
+    sample = int(os.environ.get("GK_REF_SAMPLE", "8192"))
+    idx = np.sort(rng.choice(n_total, sample, replace=False))
+    xs = grid.values[idx]
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+
+    def step():
+        t0 = time.perf_counter()
+        K, b = kriging.build_system(s)
+        w = kriging.solve(K, b)
+        iso = kriging.isovalues(s, w)
+        t1 = time.perf_counter()
+        z = kriging.evaluate(s, w, xs)
+        segmentation.segment(z, iso, m.interpolation_input.unit_values, m.options.sigmoid_slope)
+        t2 = time.perf_counter()
+        return t1 - t0, (t2 - t1) / sample
+
+    for _ in range(max(0, min(args.warmup, 1))):
+        step()
+    ts, te = [], []
+    for _ in range(max(1, min(args.steps, 2))):
+        a, b = step()
+        ts.append(a)
+        te.append(b)
+    t_solve, t_pt = float(np.mean(ts)), float(np.mean(te))
+    t_step = t_solve + t_pt * n_total
+    v = n_total / t_step
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "grid points/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "grid_points": n_total},
+            "solves_per_s": 1.0 / t_solve,
+            "cpu_baseline": {"value": v, "unit": "grid points/s", "cores": cores, "kind": "port",
+                             "sample": f"FP64 numpy/scipy oracle: full build+LU (N={s.size}) per step + "
+                                       f"{sample}-point subsample of the 256^3 grid, extrapolated to "
+                                       f"{n_total} points"},
+            "e2e": {"value": v, "unit": "grid points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--plain-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--grid", type=int, default=256)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+
+    import gempy_gb300 as gg
+    from gempy_gb300 import kernels as K
+    from gempy_gb300 import synthetic
+
+    m = synthetic.precision(resolution=(args.grid,) * 3)
+    ii, opts, dd = m.interpolation_input, m.options, m.data_descriptor
+    grid = ii.grid.dense_grid
+    n_pts = grid.n_points
+    ko = opts.kernel_options
+    sp, ori = ii.surface_points, ii.orientations
+    pps = dd.tensors_structure.number_of_points_per_surface
+    ds = K.DeviceSeries(ori.dip_positions, ori.dip_gradients, ori.nugget_effect_grad, sp.sp_coords,
+                        sp.nugget_effect_scalar, pps, range=ko.range, c_o=ko.c_o, uni_degree=ko.uni_degree,
+                        kernel=ko.kernel_function, i_res=ko.i_res, gi_res=ko.gi_res)
+    N = ds.N
+    uv = ii.unit_values
+    pts = K.Points.regular(grid)
+    ref_pts = K.Points(xyz=ds.ref_points)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    out_buf = {"field": torch.empty(n_pts, dtype=torch.float64, device="cuda"),
+               "values": torch.empty(n_pts, dtype=torch.float64, device="cuda")}
+    ev_times = []
+
+    def step(mixed, record=None):
+        K64, b = K.build(ds, K.GK_F64)
+        if mixed:
+            w, info = K.solve_mixed(ds, tol=1e-11, K=K64, b=b)
+        else:
+            f = K.lu_factor(K64, K.GK_F64, overwrite=True)
+            w = K.lu_solve(f, b)
+            info = f.info
+        del K64
+        model = K.prepare(ds, w)
+        iso_t, _, _, _ = K.evaluate(ds, model, ref_pts, K.GK_F64)
+        iso = iso_t.cpu().numpy()
+        order = np.argsort(-iso, kind="stable")
+        seg = K.make_segment(iso[order], uv, opts.sigmoid_slope)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fld, _, vals, _ = K.evaluate(ds, model, pts, K.GK_F32 if mixed else K.GK_F64, seg=seg, out=out_buf)
+        e1.record(stream)
+        cv, ci, _ = K.combine(fld[None], vals[None], [4], [iso.min()], [iso.max()], want_masks=False)
+        if record is not None:
+            record.append((e0, e1))
+        return w, info, iso, fld, ci
+
+    def timed(mixed, steps, warmup):
+        for _ in range(warmup):
+            step(mixed)
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        evs, per = [], []
+        for _ in range(steps):
+            flush.fill_(1.0)                                  # L2 flush between steps (256 MB)
+            s0 = torch.cuda.Event(enable_timing=True)
+            s1 = torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            step(mixed, evs)
+            s1.record(stream)
+            torch.cuda.synchronize()
+            per.append(s0.elapsed_time(s1))
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        ms = float(np.sum(per))
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        ev_ms = float(np.mean([a.elapsed_time(b) for a, b in evs]))
+        return ms / steps, ev_ms
+
+    # ---- mixed form, timed
+    with ClockSampler(local) as clk:
+        ms_mixed, ev_mixed = timed(True, args.steps, args.warmup)
+    clocks = clk.summary()
+    # ---- plain FP64 form, same inputs
+    ms_plain, ev_plain = timed(False, args.plain_steps, 1)
+
+    # ---- accuracy of the mixed form vs the plain FP64 form on the full grid
+    w_m, info_m, iso_m, fld_m, ids_m = step(True)
+    fld_m = fld_m.clone()
+    ids_m = ids_m.clone()
+    w_p, _, iso_p, fld_p, ids_p = step(False)
+    zp = fld_p
+    err_field = float((fld_m - zp).abs().max() / zp.abs().max())
+    err_w = float((w_m - w_p).abs().max() / w_p.abs().max())
+    band = max(10.0 / opts.sigmoid_slope, 4 * err_field * float(zp.abs().max()))
+    iso_t = torch.as_tensor(iso_p, device="cuda")
+    outside = ((zp[:, None] - iso_t[None, :]).abs() > band).all(dim=1)
+    mism = int(((ids_m != ids_p) & outside).sum())
+    info_mixed = K.read_info(info_m)
+
+    # ---- end to end through compute_model with host inputs (H2D + D2H inside)
+    cfg = gg.EngineConfig(dtype="float32")
+    e2e_ii = ii
+    opts_e2e = opts
+    for _ in range(1):
+        gg.compute_model(e2e_ii, opts_e2e, dd, config=cfg)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, 3))
+    for _ in range(e2e_steps):
+        sol = gg.compute_model(e2e_ii, opts_e2e, dd, config=cfg)
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    h2d = sum(a.nbytes for a in (sp.sp_coords, sp.nugget_effect_scalar, ori.dip_positions, ori.dip_gradients,
+                                 ori.nugget_effect_grad)) + 8 * len(pps)
+    d2h = sum(np.asarray(a).nbytes for a in (sol.raw_arrays.lith_block, sol.raw_arrays.scalar_field_matrix,
+                                             sol.raw_arrays.mask_matrix_squeezed, sol.raw_arrays.block_matrix))
+
+    # ---- roofline of the dominant kernel (the FP32 evaluation)
+    pk = peaks()
+    n_k = len(pps)
+    fl_pt = eval_flops_per_point(sp.sp_coords.shape[0], n_k, ori.dip_positions.shape[0], N)
+    achieved_tf = fl_pt * n_pts / (ev_mixed * 1e-3) / 1e12
+    sm_mhz = pk.get("sm_max_mhz", 2070.0)
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    n_ours, n_all = count_kernels(lambda: step(True))
+
+    ms_step = ms_mixed
+    line = {
+        "metric": METRIC,
+        "value": world * n_pts / (ms_step * 1e-3),
+        "unit": "grid points/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_step,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 (FP64 residual, update, isovalues)",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "grid_points": n_pts, "N": N,
+                   "l2": "flushed between steps (256 MB write); K (FP64, 578 MB) is larger than L2",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "solves_per_s": 1e3 / (ms_step - ev_mixed) if ms_step > ev_mixed else None,
+        "plain_fp64": {"ms_per_step": ms_plain, "grid_points_per_s": n_pts / (ms_plain * 1e-3),
+                       "eval_ms": ev_plain, "solve_build_ms": ms_plain - ev_plain,
+                       "solves_per_s": 1e3 / (ms_plain - ev_plain)},
+        "speedup_vs_plain_fp64": {"grid_points_per_s": ms_plain / ms_step,
+                                  "eval_kernel": ev_plain / ev_mixed,
+                                  "solve_build": (ms_plain - ev_plain) / (ms_step - ev_mixed)},
+        "errors_vs_fp64": {"field_rel_max": err_field, "weights_rel_max": err_w,
+                           "ids_mismatch_outside_band": mism, "band": band,
+                           "solver_residual": float(info_mixed["residual"]),
+                           "solver_iterations": int(info_mixed["iterations"])},
+        "clocks": clocks,
+        "e2e": {"value": n_pts / e2e_s, "unit": "grid points/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * e2e_s},
+        "gpu_launches": n_ours * args.steps,
+        "gpu_launches_per_step": n_ours,
+        "roofline": {"kernel": "gk::eval_kernel<float,2,false> (field + fused segmentation)",
+                     "bound": "fp32", "achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved_tf / fp32_peak, "traffic": None,
+                     "peak_source": f"nominal FP32 SIMT: 152 SMs x 128 lanes x 2 x {sm_mhz:.0f} MHz "
+                                    f"(max SM clock from MEASURED_PEAKS.json, {pk['_source']})",
+                     "work": f"{fl_pt} algorithmic flops/point x {n_pts} points per launch",
+                     "eval_ms": ev_mixed},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(m)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def cpu_baseline(m, sample=4096):
+    from oracle import kriging, segmentation
+    from tests._models import oracle_series_list
+    (s,) = oracle_series_list(m)
+    grid = m.interpolation_input.grid.dense_grid
+    n_total = grid.n_points
+    rng = np.random.default_rng(0)
+    idx = np.sort(rng.choice(n_total, sample, replace=False))
+    xs = grid.values[idx]
+    t0 = time.perf_counter()
+    K, b = kriging.build_system(s)
+    w = kriging.solve(K, b)
+    iso = kriging.isovalues(s, w)
+    t1 = time.perf_counter()
+    z = kriging.evaluate(s, w, xs)
+    segmentation.segment(z, iso, m.interpolation_input.unit_values, m.options.sigmoid_slope)
+    t2 = time.perf_counter()
+    t_step = (t1 - t0) + (t2 - t1) / sample * n_total
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    return {"value": n_total / t_step, "unit": "grid points/s", "cores": cores, "kind": "port",
+            "sample": f"FP64 numpy/scipy oracle (BLAS threads = all {cores} cores): full build+LU "
+                      f"(N={s.size}) + {sample}-point subsample of the grid, extrapolated to {n_total} points",
+            "solve_s": t1 - t0, "eval_s_per_point": (t2 - t1) / sample}
+
+
+if __name__ == "__main__":
+    main()

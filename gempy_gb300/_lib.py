@@ -1,0 +1,120 @@
+"""ctypes binding of ``libgempy_gb300.so`` (declared in ``include/gempy_gb300.h``).
+
+The library is built in-tree by ``gempy_gb300/build.py`` (or
+``__graft_entry__.build()``).  Loading fails loudly when it is missing or when
+no CUDA device is usable: this package has no CPU path.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgempy_gb300.so")
+
+GK_OK, GK_ERR_ARG, GK_ERR_SIZE, GK_ERR_CUDA = 0, 1, 2, 3
+GK_ERR_SINGULAR, GK_ERR_NOT_CONVERGED, GK_ERR_NONFINITE, GK_ERR_TIMEOUT = 4, 5, 6, 7
+STATUS_NAMES = {0: "OK", 1: "ERR_ARG", 2: "ERR_SIZE", 3: "ERR_CUDA", 4: "ERR_SINGULAR",
+                5: "ERR_NOT_CONVERGED", 6: "ERR_NONFINITE", 7: "ERR_TIMEOUT"}
+GK_F64, GK_F32 = 0, 1
+GK_KERNEL_CUBIC, GK_KERNEL_EXPONENTIAL = 0, 1
+GK_MAX_SURFACES = 32
+
+c_int32_p = ctypes.POINTER(ctypes.c_int32)
+c_double_p = ctypes.POINTER(ctypes.c_double)
+
+
+class GkInfo(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("where", ctypes.c_int32), ("iterations", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("residual", ctypes.c_double)]
+
+
+class GkSystem(ctypes.Structure):
+    _fields_ = [("n_ori", ctypes.c_int32), ("n_sp", ctypes.c_int32), ("n_iface", ctypes.c_int32),
+                ("uni_degree", ctypes.c_int32), ("kernel", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("range", ctypes.c_double), ("c_o", ctypes.c_double), ("i_res", ctypes.c_double),
+                ("gi_res", ctypes.c_double),
+                ("dip_positions", ctypes.c_void_p), ("dip_gradients", ctypes.c_void_p),
+                ("nugget_grad", ctypes.c_void_p), ("sp_coords", ctypes.c_void_p),
+                ("nugget_sp", ctypes.c_void_p), ("ref_index", ctypes.c_void_p),
+                ("rest_index", ctypes.c_void_p)]
+
+
+class GkPoints(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("dims", ctypes.c_int32 * 3), ("n", ctypes.c_int64),
+                ("origin", ctypes.c_double * 3), ("spacing", ctypes.c_double * 3),
+                ("xyz", ctypes.c_void_p)]
+
+
+class GkSegment(ctypes.Structure):
+    _fields_ = [("n_surf", ctypes.c_int32), ("reserved", ctypes.c_int32), ("slope", ctypes.c_double),
+                ("isovalues", ctypes.c_double * GK_MAX_SURFACES),
+                ("unit_values", ctypes.c_double * (GK_MAX_SURFACES + 1))]
+
+
+# (name, restype, argtypes) of every exported symbol; tests check the header
+# declares exactly these.
+SIGNATURES = [
+    ("gk_system_size", ctypes.c_int64, [ctypes.POINTER(GkSystem)]),
+    ("gk_build", ctypes.c_int, [ctypes.POINTER(GkSystem), ctypes.c_int, ctypes.c_void_p, ctypes.c_int64,
+                                ctypes.c_void_p, ctypes.c_void_p]),
+    ("gk_lu_workspace_bytes", ctypes.c_size_t, [ctypes.c_int, ctypes.c_int64]),
+    ("gk_lu_factor", ctypes.c_int, [ctypes.c_int, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
+                                    ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
+                                    ctypes.c_void_p]),
+    ("gk_lu_solve", ctypes.c_int, [ctypes.c_int, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
+                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                   ctypes.c_void_p, ctypes.c_void_p]),
+    ("gk_solve_mixed_workspace_bytes", ctypes.c_size_t, [ctypes.c_int64]),
+    ("gk_solve_mixed", ctypes.c_int, [ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                      ctypes.c_void_p, ctypes.c_double, ctypes.c_int32, ctypes.c_void_p,
+                                      ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]),
+    ("gk_eval_model_bytes", ctypes.c_size_t, [ctypes.POINTER(GkSystem)]),
+    ("gk_eval_prepare", ctypes.c_int, [ctypes.POINTER(GkSystem), ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_void_p]),
+    ("gk_eval", ctypes.c_int, [ctypes.POINTER(GkSystem), ctypes.c_void_p, ctypes.POINTER(GkPoints),
+                               ctypes.c_int, ctypes.POINTER(GkSegment), ctypes.c_void_p, ctypes.c_void_p,
+                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    ("gk_combine_series", ctypes.c_int, [ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+                                         c_int32_p, c_double_p, c_double_p, ctypes.c_void_p,
+                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    ("gk_octree_corners", ctypes.c_int, [ctypes.c_int64, ctypes.c_void_p, c_double_p, ctypes.c_void_p,
+                                         ctypes.c_void_p]),
+    ("gk_octree_workspace_bytes", ctypes.c_size_t, [ctypes.c_int64]),
+    ("gk_octree_refine", ctypes.c_int, [ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                        c_double_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_size_t, ctypes.c_void_p]),
+    ("gk_version", ctypes.c_char_p, []),
+]
+
+_lib = None
+
+
+class GkError(RuntimeError):
+    def __init__(self, func, status, where=None):
+        self.status = status
+        msg = f"{func} failed: {STATUS_NAMES.get(status, status)}"
+        if where is not None:
+            msg += f" (at {where})"
+        super().__init__(msg)
+
+
+def load():
+    """Load the library once; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(
+            f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'` "
+            "(gempy_gb300 has no CPU fallback)")
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, res, args in SIGNATURES:
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(func, status):
+    if status != GK_OK:
+        raise GkError(func, status)

@@ -1,0 +1,167 @@
+// Shared device helpers of the co-kriging kernels: covariance functions,
+// status reporting and a bounded grid barrier for cooperative launches.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/gempy_gb300.h"
+
+#define GK_CUDA_TRY(expr)                                   \
+    do {                                                    \
+        cudaError_t _e = (expr);                            \
+        if (_e != cudaSuccess) return GK_ERR_CUDA;          \
+    } while (0)
+
+#define GK_LAUNCH_CHECK()                                   \
+    do {                                                    \
+        if (cudaPeekAtLastError() != cudaSuccess) {         \
+            (void)cudaGetLastError();                       \
+            return GK_ERR_CUDA;                             \
+        }                                                   \
+    } while (0)
+
+namespace gk {
+
+constexpr int kSMs = 152;  // GB300: 2 dies x 76 SMs (queried at run time too)
+
+// Regulariser of h_u h_v / r^2 in the gradient-gradient block.
+constexpr double kGradEps = 1e-5;
+
+// Iteration cap of every inter-CTA spin wait: ~seconds at worst, then the
+// kernel records GK_ERR_TIMEOUT and returns instead of hanging the GPU.
+constexpr long long kSpinLimit = 20LL * 1000 * 1000;
+
+__host__ __device__ inline int drift_count(int degree) {
+    return degree == 1 ? 3 : (degree == 2 ? 9 : 0);
+}
+
+// Radial covariance with unit sill and its radial derivatives:
+//   C(r), C'(r)/r, C''(r), (C'/r)'(r)/r.
+// Cubic: C = 1 - 7 s^2 + 35/4 s^3 - 7/2 s^5 + 3/4 s^7 for s = r/a < 1, else 0.
+// Exponential: squared exponential exp(-r^2 / (2 a^2)).
+template <typename T>
+struct Cov {
+    int kind;
+    T a, ia, ia2, ia4;  // a, 1/a, 1/a^2, 1/a^4
+
+    __host__ __device__ static Cov make(int kind, double a) {
+        Cov c;
+        c.kind = kind;
+        c.a = (T)a;
+        c.ia = (T)(1.0 / a);
+        c.ia2 = (T)(1.0 / (a * a));
+        c.ia4 = (T)(1.0 / (a * a * a * a));
+        return c;
+    }
+
+    __device__ __forceinline__ T C(T r) const {
+        if (kind == GK_KERNEL_CUBIC) {
+            T s = r * ia;
+            if (s >= (T)1) return (T)0;
+            T s2 = s * s;
+            return (T)1 + s2 * ((T)-7 + s * ((T)8.75 + s2 * ((T)-3.5 + (T)0.75 * s2)));
+        }
+        return gexp(-(T)0.5 * r * r * ia2);
+    }
+    __device__ __forceinline__ T d1_r(T r) const {
+        if (kind == GK_KERNEL_CUBIC) {
+            T s = r * ia;
+            if (s >= (T)1) return (T)0;
+            T s2 = s * s;
+            return ia2 * ((T)-14 + s * ((T)26.25 + s2 * ((T)-17.5 + (T)5.25 * s2)));
+        }
+        return -ia2 * gexp(-(T)0.5 * r * r * ia2);
+    }
+    __device__ __forceinline__ T d2(T r) const {
+        if (kind == GK_KERNEL_CUBIC) {
+            T s = r * ia;
+            if (s >= (T)1) return (T)0;
+            T s2 = s * s;
+            return ia2 * ((T)-14 + s * ((T)52.5 + s2 * ((T)-70 + (T)31.5 * s2)));
+        }
+        T e = gexp(-(T)0.5 * r * r * ia2);
+        return (r * r * ia4 - ia2) * e;
+    }
+    // (C'/r)'/r; finite at r = 0 is enough (it multiplies terms O(r^2)).
+    __device__ __forceinline__ T d3_r(T r) const {
+        if (kind == GK_KERNEL_CUBIC) {
+            T s = r * ia;
+            if (s >= (T)1 || s <= (T)0) return (T)0;
+            T s2 = s * s;
+            return ia4 * ((T)26.25 / s + s * ((T)-52.5 + (T)26.25 * s2));
+        }
+        return ia4 * gexp(-(T)0.5 * r * r * ia2);
+    }
+    __device__ __forceinline__ static T gexp(T x);
+};
+
+template <>
+__device__ __forceinline__ double Cov<double>::gexp(double x) { return exp(x); }
+template <>
+__device__ __forceinline__ float Cov<float>::gexp(float x) { return expf(x); }
+
+template <typename T>
+__device__ __forceinline__ T gsqrt(T x);
+template <>
+__device__ __forceinline__ double gsqrt<double>(double x) { return sqrt(x); }
+template <>
+__device__ __forceinline__ float gsqrt<float>(float x) { return sqrtf(x); }
+
+// Records the first failure into a device info word.
+__device__ inline void report(gk_info* info, int status, int where) {
+    if (info == nullptr) return;
+    if (atomicCAS(&info->status, 0, status) == 0) info->where = where;
+}
+
+// Sense-free grid barrier for cooperative launches.  ``bar[0]`` counts
+// arrivals, ``bar[1]`` is the generation.  Every wait is bounded: on timeout
+// the barrier sets ``*abort`` and reports GK_ERR_TIMEOUT; callers test
+// ``*abort`` after each barrier and return.
+struct GridBarrier {
+    unsigned int* bar;      // 2 words, zero before the launch
+    volatile int* abort;    // 1 word, zero before the launch
+    gk_info* info;
+
+    __device__ bool sync(unsigned int nblocks) {
+        __syncthreads();
+        __shared__ int s_ok;
+        if (threadIdx.x == 0) {
+            s_ok = 1;
+            unsigned int gen = atomicAdd(&bar[1], 0u);
+            __threadfence();
+            unsigned int arrived = atomicAdd(&bar[0], 1u);
+            if (arrived == nblocks - 1) {
+                atomicExch(&bar[0], 0u);
+                __threadfence();
+                atomicAdd(&bar[1], 1u);
+            } else {
+                long long spins = 0;
+                while (true) {
+                    unsigned int g;
+                    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(g) : "l"(bar + 1) : "memory");
+                    if (g != gen) break;
+                    if (*abort) { s_ok = 0; break; }
+                    if (++spins > kSpinLimit) {
+                        *abort = 1;
+                        report(info, GK_ERR_TIMEOUT, -1);
+                        s_ok = 0;
+                        break;
+                    }
+                }
+            }
+            __threadfence();
+        }
+        __syncthreads();
+        return s_ok != 0;
+    }
+};
+
+inline int device_sm_count() {
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return kSMs;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return kSMs;
+    return n > 0 ? n : kSMs;
+}
+
+}  // namespace gk

@@ -1,0 +1,520 @@
+// Scalar-field / gradient evaluation with fused sigmoid segmentation, and the
+// series combination.  Replaces the engine's grid evaluation and
+// segmentation reached from gempy/API/compute_API.py:68-73 (outputs read back
+// as exported_fields.scalar_field, values_block / ids_block).
+//
+// Contraction.  With the solved weights folded into packed "records"
+//   orientation o : (x_o, c_o gi_res w_o)          -> Z += C'/r(|x-x_o|) (w_o . (x_o - x))
+//   surface point p: (x_p, c_o gi_res alpha_p)     -> Z += alpha_p C(|x - x_p|)
+// every grid point needs one radial kernel per record; records are streamed
+// through shared memory in tiles by the TMA engine (1-D cp.async.bulk with an
+// mbarrier, two stages), so a CTA's 256 threads x PPT points reuse each tile.
+// Grid coordinates of regular grids are generated in the kernel.  In FP32 mode
+// the per-tile partial sums are FP32 and are added into FP64 accumulators once
+// per tile; the drift, the segmentation thresholds and the outputs are FP64.
+#include <cstring>
+
+#include "gk_common.cuh"
+
+namespace gk {
+
+static size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+struct ModelLayout {
+    size_t ori64, sp64, mu64, ori32, sp32, alpha, total;
+};
+
+static ModelLayout model_layout(int n_ori, int n_sp) {
+    ModelLayout L;
+    size_t o = 0;
+    L.ori64 = o; o += al256((size_t)n_ori * 8 * sizeof(double));
+    L.sp64 = o;  o += al256((size_t)n_sp * 4 * sizeof(double));
+    L.mu64 = o;  o += al256(16 * sizeof(double));
+    L.ori32 = o; o += al256((size_t)n_ori * 8 * sizeof(float));
+    L.sp32 = o;  o += al256((size_t)n_sp * 4 * sizeof(float));
+    L.alpha = o; o += al256((size_t)n_sp * sizeof(double));
+    L.total = o;
+    return L;
+}
+
+// alpha[rest_t] += gi w_t   (rest points are unique per interface row)
+__global__ void alpha_rest_kernel(const int32_t* __restrict__ rest, int n_iface, const double* __restrict__ wi,
+                                  double gi, double* alpha) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n_iface) atomicAdd(alpha + rest[t], gi * wi[t]);
+}
+
+// alpha[ref] -= gi sum_{t in run} w_t, one thread per run of equal ref_index
+__global__ void alpha_ref_kernel(const int32_t* __restrict__ ref, int n_iface, const double* __restrict__ wi, double gi,
+                                 double* alpha) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_iface) return;
+    if (t > 0 && ref[t - 1] == ref[t]) return;
+    double s = 0.0;
+    int u = t;
+    for (; u < n_iface && ref[u] == ref[t]; ++u) s += wi[u];
+    atomicAdd(alpha + ref[t], -gi * s);
+}
+
+__global__ void pack_kernel(int n_ori, int n_sp, int n_iface, int n_drift, double scale, double gi,
+                            const double* __restrict__ dip, const double* __restrict__ sp,
+                            const double* __restrict__ w, const double* __restrict__ alpha, double* ori64,
+                            double* sp64, double* mu64, float* ori32, float* sp32) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n_ori) {
+        double rec[8] = {dip[3 * i], dip[3 * i + 1], dip[3 * i + 2], scale * w[i], scale * w[n_ori + i],
+                         scale * w[2 * n_ori + i], 0.0, 0.0};
+        for (int k = 0; k < 8; ++k) { ori64[8 * i + k] = rec[k]; ori32[8 * i + k] = (float)rec[k]; }
+    }
+    if (i < n_sp) {
+        double rec[4] = {sp[3 * i], sp[3 * i + 1], sp[3 * i + 2], scale * alpha[i]};
+        for (int k = 0; k < 4; ++k) { sp64[4 * i + k] = rec[k]; sp32[4 * i + k] = (float)rec[k]; }
+    }
+    if (i < 16) mu64[i] = i < n_drift ? gi * w[3 * n_ori + n_iface + i] : 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// TMA (bulk copy) + mbarrier helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+constexpr long long kMbarSpin = 4LL * 1000 * 1000;
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    for (long long i = 0; i < kMbarSpin; ++i)
+        if (mbar_try(bar, parity)) return true;
+    return false;
+}
+
+struct EvalParams {
+    int kind;
+    int dims[3];
+    int64_t n;
+    double origin[3], spacing[3];
+    const double* xyz;
+    int n_ori, n_sp, n_drift, degree, kernel;
+    double range;
+    const void* ori;   // packed records in T
+    const void* sp;
+    const double* mu;
+    int tiles_ori, tiles_sp, rec_ori, rec_sp;  // records per tile
+    int stage_bytes;
+    int has_seg;
+    gk_segment seg;
+    double* field;
+    double* grad;
+    double* values;
+    int32_t* ids;
+    int* err;          // device error word (timeouts), may be NULL
+};
+
+template <typename T> __device__ __forceinline__ T fast_r(T r2);
+template <> __device__ __forceinline__ float fast_r<float>(float r2) { return r2 > 0.f ? r2 * rsqrtf(r2) : 0.f; }
+template <> __device__ __forceinline__ double fast_r<double>(double r2) { return sqrt(r2); }
+
+template <typename T> __device__ __forceinline__ T sigm(double t);
+template <> __device__ __forceinline__ double sigm<double>(double t) {
+    if (t >= 0.0) return 1.0 / (1.0 + exp(-t));
+    double e = exp(t);
+    return e / (1.0 + e);
+}
+template <> __device__ __forceinline__ float sigm<float>(double t) {
+    float tf = (float)t;
+    if (tf >= 0.f) return 1.f / (1.f + expf(-tf));
+    float e = expf(tf);
+    return e / (1.f + e);
+}
+
+template <typename T, int PPT, bool GRAD>
+__global__ void __launch_bounds__(256) eval_kernel(const EvalParams P) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ int s_fail;
+    const int tid = threadIdx.x;
+    unsigned char* stage[2] = {smem, smem + P.stage_bytes};
+    if (tid == 0) {
+        mbar_init(&mbar[0], 1);
+        mbar_init(&mbar[1], 1);
+        mbar_fence_init();
+        s_fail = 0;
+    }
+    __syncthreads();
+
+    const Cov<T> cv = Cov<T>::make(P.kernel, P.range);
+    const int64_t chunk_pts = (int64_t)blockDim.x * PPT;
+    const int64_t n_chunks = (P.n + chunk_pts - 1) / chunk_pts;
+    const int n_tiles = P.tiles_ori + P.tiles_sp;
+    const int64_t my_chunks = n_chunks > blockIdx.x ? (n_chunks - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    const int64_t n_items = my_chunks * n_tiles;
+
+    auto tile_src = [&](int t, uint32_t& bytes) -> const void* {
+        if (t < P.tiles_ori) {
+            int r0 = t * P.rec_ori;
+            int nr = min(P.rec_ori, P.n_ori - r0);
+            bytes = (uint32_t)(nr * 8 * sizeof(T));
+            return (const T*)P.ori + (size_t)r0 * 8;
+        }
+        int ts = t - P.tiles_ori;
+        int r0 = ts * P.rec_sp;
+        int nr = min(P.rec_sp, P.n_sp - r0);
+        bytes = (uint32_t)(nr * 4 * sizeof(T));
+        return (const T*)P.sp + (size_t)r0 * 4;
+    };
+    auto issue = [&](int64_t item) {
+        if (tid != 0) return;
+        int s = (int)(item & 1);
+        int t = (int)(item % n_tiles);
+        uint32_t bytes;
+        const void* src = tile_src(t, bytes);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(&mbar[s], bytes);
+        bulk_g2s(stage[s], src, bytes, &mbar[s]);
+    };
+    if (n_items > 0) issue(0);
+    if (n_items > 1) issue(1);
+
+    int64_t item = 0;
+    for (int64_t lc = 0; lc < my_chunks; ++lc) {
+        const int64_t chunk = blockIdx.x + lc * gridDim.x;
+        T x[PPT][3];
+        double xd[PPT][3];
+        int64_t pid[PPT];
+#pragma unroll
+        for (int p = 0; p < PPT; ++p) {
+            pid[p] = chunk * chunk_pts + tid + (int64_t)p * blockDim.x;
+            int64_t q = pid[p] < P.n ? pid[p] : P.n - 1;
+            if (P.kind == 0) {
+                int64_t nyz = (int64_t)P.dims[1] * P.dims[2];
+                int64_t ix = q / nyz, rem = q - ix * nyz;
+                int64_t iy = rem / P.dims[2], iz = rem - iy * P.dims[2];
+                xd[p][0] = P.origin[0] + (double)ix * P.spacing[0];
+                xd[p][1] = P.origin[1] + (double)iy * P.spacing[1];
+                xd[p][2] = P.origin[2] + (double)iz * P.spacing[2];
+            } else {
+                xd[p][0] = P.xyz[3 * q];
+                xd[p][1] = P.xyz[3 * q + 1];
+                xd[p][2] = P.xyz[3 * q + 2];
+            }
+            for (int k = 0; k < 3; ++k) x[p][k] = (T)xd[p][k];
+        }
+        double Z[PPT], G[PPT][3];
+#pragma unroll
+        for (int p = 0; p < PPT; ++p) { Z[p] = 0.0; G[p][0] = G[p][1] = G[p][2] = 0.0; }
+
+        for (int t = 0; t < n_tiles; ++t, ++item) {
+            const int s = (int)(item & 1);
+            const uint32_t parity = (uint32_t)((item >> 1) & 1);
+            if (!mbar_wait(&mbar[s], parity)) {
+                if (P.err) atomicExch(P.err, GK_ERR_TIMEOUT);
+                s_fail = 1;
+            }
+            __syncthreads();
+            if (s_fail) goto drain;
+            {
+                T zt[PPT], gt[PPT][3];
+#pragma unroll
+                for (int p = 0; p < PPT; ++p) { zt[p] = (T)0; gt[p][0] = gt[p][1] = gt[p][2] = (T)0; }
+                if (t < P.tiles_ori) {
+                    const T* rec = reinterpret_cast<const T*>(stage[s]);
+                    const int nr = min(P.rec_ori, P.n_ori - t * P.rec_ori);
+                    for (int q = 0; q < nr; ++q) {
+                        const T ox = rec[8 * q], oy = rec[8 * q + 1], oz = rec[8 * q + 2];
+                        const T wx = rec[8 * q + 3], wy = rec[8 * q + 4], wz = rec[8 * q + 5];
+#pragma unroll
+                        for (int p = 0; p < PPT; ++p) {
+                            const T hx = ox - x[p][0], hy = oy - x[p][1], hz = oz - x[p][2];
+                            const T r = fast_r<T>(hx * hx + hy * hy + hz * hz);
+                            const T k1 = cv.d1_r(r);
+                            const T wh = wx * hx + wy * hy + wz * hz;
+                            zt[p] += k1 * wh;
+                            if (GRAD) {
+                                const T k3 = cv.d3_r(r) * wh;
+                                gt[p][0] -= k3 * hx + k1 * wx;
+                                gt[p][1] -= k3 * hy + k1 * wy;
+                                gt[p][2] -= k3 * hz + k1 * wz;
+                            }
+                        }
+                    }
+                } else {
+                    const T* rec = reinterpret_cast<const T*>(stage[s]);
+                    const int ts = t - P.tiles_ori;
+                    const int nr = min(P.rec_sp, P.n_sp - ts * P.rec_sp);
+                    for (int q = 0; q < nr; ++q) {
+                        const T px = rec[4 * q], py = rec[4 * q + 1], pz = rec[4 * q + 2], al = rec[4 * q + 3];
+#pragma unroll
+                        for (int p = 0; p < PPT; ++p) {
+                            const T hx = x[p][0] - px, hy = x[p][1] - py, hz = x[p][2] - pz;
+                            const T r = fast_r<T>(hx * hx + hy * hy + hz * hz);
+                            zt[p] += al * cv.C(r);
+                            if (GRAD) {
+                                const T k1 = al * cv.d1_r(r);
+                                gt[p][0] += k1 * hx;
+                                gt[p][1] += k1 * hy;
+                                gt[p][2] += k1 * hz;
+                            }
+                        }
+                    }
+                }
+#pragma unroll
+                for (int p = 0; p < PPT; ++p) {
+                    Z[p] += (double)zt[p];
+                    if (GRAD) { G[p][0] += (double)gt[p][0]; G[p][1] += (double)gt[p][1]; G[p][2] += (double)gt[p][2]; }
+                }
+            }
+            __syncthreads();  // stage s fully consumed
+            if (item + 2 < n_items) issue(item + 2);
+        }
+        // epilogue: drift, outputs, segmentation
+#pragma unroll
+        for (int p = 0; p < PPT; ++p) {
+            if (pid[p] >= P.n) continue;
+            const double* mu = P.mu;
+            const double X = xd[p][0], Y = xd[p][1], Zc = xd[p][2];
+            double z = Z[p];
+            if (P.n_drift >= 3) z += mu[0] * X + mu[1] * Y + mu[2] * Zc;
+            if (P.n_drift >= 9)
+                z += mu[3] * X * X + mu[4] * Y * Y + mu[5] * Zc * Zc + mu[6] * X * Y + mu[7] * X * Zc + mu[8] * Y * Zc;
+            if (P.field) P.field[pid[p]] = z;
+            if (GRAD && P.grad) {
+                double gx = G[p][0], gy = G[p][1], gz = G[p][2];
+                if (P.n_drift >= 3) { gx += mu[0]; gy += mu[1]; gz += mu[2]; }
+                if (P.n_drift >= 9) {
+                    gx += 2.0 * mu[3] * X + mu[6] * Y + mu[7] * Zc;
+                    gy += 2.0 * mu[4] * Y + mu[6] * X + mu[8] * Zc;
+                    gz += 2.0 * mu[5] * Zc + mu[7] * X + mu[8] * Y;
+                }
+                P.grad[3 * pid[p]] = gx;
+                P.grad[3 * pid[p] + 1] = gy;
+                P.grad[3 * pid[p] + 2] = gz;
+            }
+            if (P.has_seg) {
+                double v = P.seg.unit_values[0];
+                for (int k = 0; k < P.seg.n_surf; ++k)
+                    v += (P.seg.unit_values[k + 1] - P.seg.unit_values[k]) *
+                         (double)sigm<T>(P.seg.slope * (P.seg.isovalues[k] - z));
+                if (P.values) P.values[pid[p]] = v;
+                if (P.ids) P.ids[pid[p]] = (int32_t)rint(v);
+            }
+        }
+    }
+    return;
+drain:
+    // a stage wait gave up: wait (bounded) for copies still in flight, then leave
+    if (tid == 0) {
+        for (int64_t it = item; it < n_items && it < item + 2; ++it) mbar_wait(&mbar[it & 1], (uint32_t)((it >> 1) & 1));
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// series combination
+// ---------------------------------------------------------------------------
+struct CombineParams {
+    int n_series;
+    int64_t n;
+    const double* fields;
+    const double* values;
+    int relations[GK_MAX_SURFACES];
+    double min_iso[GK_MAX_SURFACES];
+    double max_iso[GK_MAX_SURFACES];
+    double* out_values;
+    int32_t* out_ids;
+    uint8_t* masks;
+};
+
+__global__ void combine_kernel(const CombineParams P) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    bool taken = false;
+    double v = 0.0;
+    for (int s = 0; s < P.n_series; ++s) {
+        bool raw;
+        const int rel = P.relations[s];
+        if (rel == 4 || s == P.n_series - 1) raw = true;                              // BASEMENT / last
+        else if (rel == 1) raw = P.fields[(int64_t)s * P.n + i] >= P.min_iso[s];      // ERODE
+        else raw = P.fields[(int64_t)(s + 1) * P.n + i] >= P.max_iso[s + 1];          // ONLAP
+        bool m = raw && !taken;
+        taken = taken || m;
+        if (m) v += P.values[(int64_t)s * P.n + i];
+        if (P.masks) P.masks[(int64_t)s * P.n + i] = m ? 1 : 0;
+    }
+    if (P.out_values) P.out_values[i] = v;
+    if (P.out_ids) P.out_ids[i] = (int32_t)rint(v);
+}
+
+}  // namespace gk
+
+using namespace gk;
+
+gk_status gk_check_system(const gk_system* s);
+
+extern "C" size_t gk_eval_model_bytes(const gk_system* s) {
+    if (s == nullptr) return 0;
+    return model_layout(s->n_ori, s->n_sp).total;
+}
+
+extern "C" gk_status gk_eval_prepare(const gk_system* s, const double* w, void* model, gk_stream stream) {
+    gk_status st = gk_check_system(s);
+    if (st != GK_OK) return st;
+    if (w == nullptr || model == nullptr) return GK_ERR_ARG;
+    cudaStream_t cs = (cudaStream_t)stream;
+    ModelLayout L = model_layout(s->n_ori, s->n_sp);
+    char* m = (char*)model;
+    double* alpha = (double*)(m + L.alpha);
+    const int n_drift = drift_count(s->uni_degree);
+    const int ng = 3 * s->n_ori;
+    GK_CUDA_TRY(cudaMemsetAsync(alpha, 0, (size_t)s->n_sp * sizeof(double), cs));
+    if (s->n_iface > 0) {
+        unsigned b = (unsigned)((s->n_iface + 255) / 256);
+        alpha_rest_kernel<<<b, 256, 0, cs>>>(s->rest_index, s->n_iface, w + ng, s->gi_res, alpha);
+        GK_LAUNCH_CHECK();
+        alpha_ref_kernel<<<b, 256, 0, cs>>>(s->ref_index, s->n_iface, w + ng, s->gi_res, alpha);
+        GK_LAUNCH_CHECK();
+    }
+    int nmax = s->n_ori > s->n_sp ? s->n_ori : s->n_sp;
+    if (nmax < 16) nmax = 16;
+    pack_kernel<<<(unsigned)((nmax + 255) / 256), 256, 0, cs>>>(
+        s->n_ori, s->n_sp, s->n_iface, n_drift, s->c_o * s->gi_res, s->gi_res, s->dip_positions, s->sp_coords, w,
+        alpha, (double*)(m + L.ori64), (double*)(m + L.sp64), (double*)(m + L.mu64), (float*)(m + L.ori32),
+        (float*)(m + L.sp32));
+    GK_LAUNCH_CHECK();
+    return GK_OK;
+}
+
+template <typename T, int PPT, bool GRAD>
+static gk_status launch_eval(EvalParams& P, cudaStream_t st) {
+    const int stage_bytes = 32 * 1024;
+    P.stage_bytes = stage_bytes;
+    P.rec_ori = stage_bytes / (8 * sizeof(T));
+    P.rec_sp = stage_bytes / (4 * sizeof(T));
+    P.tiles_ori = (P.n_ori + P.rec_ori - 1) / P.rec_ori;
+    P.tiles_sp = (P.n_sp + P.rec_sp - 1) / P.rec_sp;
+    auto k = eval_kernel<T, PPT, GRAD>;
+    size_t smem = 2 * (size_t)stage_bytes;
+    GK_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int occ = 0;
+    GK_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, 256, smem));
+    if (occ < 1) occ = 1;
+    const int64_t chunk_pts = 256LL * PPT;
+    int64_t n_chunks = (P.n + chunk_pts - 1) / chunk_pts;
+    int64_t grid = (int64_t)occ * device_sm_count();
+    if (grid > n_chunks) grid = n_chunks;
+    if (grid < 1) grid = 1;
+    if (P.tiles_ori + P.tiles_sp == 0) {
+        // no covariance records: a zero-length record set still needs the drift epilogue
+        P.tiles_sp = 0;
+    }
+    k<<<(unsigned)grid, 256, smem, st>>>(P);
+    GK_LAUNCH_CHECK();
+    return GK_OK;
+}
+
+extern "C" gk_status gk_eval(const gk_system* s, const void* model, const gk_points* pts, gk_prec prec,
+                             const gk_segment* seg, double* field, double* grad, double* values, int32_t* ids,
+                             gk_stream stream) {
+    gk_status st = gk_check_system(s);
+    if (st != GK_OK) return st;
+    if (model == nullptr || pts == nullptr) return GK_ERR_ARG;
+    if (pts->n < 0) return GK_ERR_ARG;
+    if (pts->n == 0) return GK_OK;
+    if (pts->kind == 0) {
+        if (pts->dims[0] <= 0 || pts->dims[1] <= 0 || pts->dims[2] <= 0) return GK_ERR_ARG;
+        if ((int64_t)pts->dims[0] * pts->dims[1] * pts->dims[2] != pts->n) return GK_ERR_ARG;
+    } else if (pts->kind != 1 || pts->xyz == nullptr) {
+        return GK_ERR_ARG;
+    }
+    if (seg != nullptr && (seg->n_surf < 0 || seg->n_surf > GK_MAX_SURFACES)) return GK_ERR_SIZE;
+    if ((values || ids) && seg == nullptr) return GK_ERR_ARG;
+    if (s->n_ori + s->n_sp == 0) return GK_ERR_ARG;
+    ModelLayout L = model_layout(s->n_ori, s->n_sp);
+    const char* m = (const char*)model;
+    EvalParams P;
+    memset(&P, 0, sizeof(P));
+    P.kind = pts->kind;
+    for (int k = 0; k < 3; ++k) {
+        P.dims[k] = pts->dims[k];
+        P.origin[k] = pts->origin[k];
+        P.spacing[k] = pts->spacing[k];
+    }
+    P.n = pts->n;
+    P.xyz = pts->xyz;
+    P.n_ori = s->n_ori;
+    P.n_sp = s->n_sp;
+    P.n_drift = drift_count(s->uni_degree);
+    P.degree = s->uni_degree;
+    P.kernel = s->kernel;
+    P.range = s->range;
+    P.mu = (const double*)(m + L.mu64);
+    P.has_seg = seg != nullptr;
+    if (seg) P.seg = *seg;
+    P.field = field;
+    P.grad = grad;
+    P.values = values;
+    P.ids = ids;
+    P.err = nullptr;
+    cudaStream_t cs = (cudaStream_t)stream;
+    if (prec == GK_F64) {
+        P.ori = m + L.ori64;
+        P.sp = m + L.sp64;
+        return grad ? launch_eval<double, 1, true>(P, cs) : launch_eval<double, 1, false>(P, cs);
+    }
+    if (prec == GK_F32) {
+        P.ori = m + L.ori32;
+        P.sp = m + L.sp32;
+        return grad ? launch_eval<float, 2, true>(P, cs) : launch_eval<float, 2, false>(P, cs);
+    }
+    return GK_ERR_ARG;
+}
+
+extern "C" gk_status gk_combine_series(int32_t n_series, int64_t n, const double* fields, const double* values,
+                                       const int32_t* relations, const double* min_iso, const double* max_iso,
+                                       double* out_values, int32_t* out_ids, uint8_t* masks, gk_stream stream) {
+    if (n_series < 1 || n_series > GK_MAX_SURFACES || n < 0) return GK_ERR_ARG;
+    if (fields == nullptr || values == nullptr || relations == nullptr || min_iso == nullptr || max_iso == nullptr)
+        return GK_ERR_ARG;
+    if (n == 0) return GK_OK;
+    CombineParams P;
+    memset(&P, 0, sizeof(P));
+    P.n_series = n_series;
+    P.n = n;
+    P.fields = fields;
+    P.values = values;
+    for (int s = 0; s < n_series; ++s) {
+        if (relations[s] != 1 && relations[s] != 2 && relations[s] != 4) return GK_ERR_ARG;
+        P.relations[s] = relations[s];
+        P.min_iso[s] = min_iso[s];
+        P.max_iso[s] = max_iso[s];
+    }
+    P.out_values = out_values;
+    P.out_ids = out_ids;
+    P.masks = masks;
+    combine_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(P);
+    GK_LAUNCH_CHECK();
+    return GK_OK;
+}

@@ -1,0 +1,159 @@
+// Octree refinement: voxel corners, marking and ordered compaction of the
+// children of marked voxels.  Replaces the engine's octree step over the
+// reference's octree grid (gempy/core/data/grid.py:128-151,
+// grid_modules/regular_grid.py:36-43).  A voxel is refined when the ids at
+// its 8 corners are not all equal; children are listed 8 per refined voxel
+// (x slowest, z fastest) in parent order, which matches the point order of
+// the reference's approved anticline scalar field
+// (test/test_model_types/test_example_models_I.py:19-23).
+#include "gk_common.cuh"
+
+namespace gk {
+
+__device__ __forceinline__ void corner_sign(int c, double& sx, double& sy, double& sz) {
+    sx = (c & 4) ? 1.0 : -1.0;
+    sy = (c & 2) ? 1.0 : -1.0;
+    sz = (c & 1) ? 1.0 : -1.0;
+}
+
+__global__ void corners_kernel(int64_t n, const double* __restrict__ c, double hx, double hy, double hz,
+                               double* __restrict__ out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 8 * n) return;
+    int64_t v = i >> 3;
+    int k = (int)(i & 7);
+    double sx, sy, sz;
+    corner_sign(k, sx, sy, sz);
+    out[3 * i] = c[3 * v] + sx * hx;
+    out[3 * i + 1] = c[3 * v + 1] + sy * hy;
+    out[3 * i + 2] = c[3 * v + 2] + sz * hz;
+}
+
+constexpr int kScanBlock = 256;
+
+// per-block count of marked voxels
+__global__ void mark_count_kernel(int64_t n, const int32_t* __restrict__ ids, int refine_all,
+                                  int64_t* __restrict__ block_counts) {
+    __shared__ int cnt;
+    if (threadIdx.x == 0) cnt = 0;
+    __syncthreads();
+    int64_t v = (int64_t)blockIdx.x * kScanBlock + threadIdx.x;
+    int m = 0;
+    if (v < n) {
+        if (refine_all) m = 1;
+        else {
+            const int32_t* c = ids + 8 * v;
+            int32_t a = c[0];
+            for (int k = 1; k < 8; ++k) m |= (c[k] != a);
+        }
+    }
+    int w = __syncthreads_count(m);
+    if (threadIdx.x == 0) block_counts[blockIdx.x] = w;
+    (void)cnt;
+}
+
+// exclusive scan of block counts in one CTA (sequential over chunks of 1024)
+__global__ void scan_blocks_kernel(int64_t nb, int64_t* __restrict__ counts, int64_t* __restrict__ total) {
+    __shared__ int64_t buf[1024];
+    __shared__ int64_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int64_t base = 0; base < nb; base += 1024) {
+        int64_t i = base + threadIdx.x;
+        int64_t v = i < nb ? counts[i] : 0;
+        buf[threadIdx.x] = v;
+        __syncthreads();
+        for (int off = 1; off < 1024; off <<= 1) {
+            int64_t t = threadIdx.x >= off ? buf[threadIdx.x - off] : 0;
+            __syncthreads();
+            buf[threadIdx.x] += t;
+            __syncthreads();
+        }
+        if (i < nb) counts[i] = carry + buf[threadIdx.x] - v;  // exclusive
+        __syncthreads();
+        if (threadIdx.x == 1023) carry += buf[1023];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = carry * 8;
+}
+
+__global__ void scatter_children_kernel(int64_t n, const double* __restrict__ c, const int32_t* __restrict__ ids,
+                                        int refine_all, const int64_t* __restrict__ block_off, double qx, double qy,
+                                        double qz, double* __restrict__ out) {
+    __shared__ int pref[kScanBlock];
+    int64_t v = (int64_t)blockIdx.x * kScanBlock + threadIdx.x;
+    int m = 0;
+    if (v < n) {
+        if (refine_all) m = 1;
+        else {
+            const int32_t* cc = ids + 8 * v;
+            int32_t a = cc[0];
+            for (int k = 1; k < 8; ++k) m |= (cc[k] != a);
+        }
+    }
+    pref[threadIdx.x] = m;
+    __syncthreads();
+    for (int off = 1; off < kScanBlock; off <<= 1) {
+        int t = threadIdx.x >= off ? pref[threadIdx.x - off] : 0;
+        __syncthreads();
+        pref[threadIdx.x] += t;
+        __syncthreads();
+    }
+    if (!m) return;
+    int64_t slot = block_off[blockIdx.x] + pref[threadIdx.x] - 1;
+    for (int k = 0; k < 8; ++k) {
+        double sx, sy, sz;
+        corner_sign(k, sx, sy, sz);
+        int64_t o = 8 * slot + k;
+        out[3 * o] = c[3 * v] + sx * qx;
+        out[3 * o + 1] = c[3 * v + 1] + sy * qy;
+        out[3 * o + 2] = c[3 * v + 2] + sz * qz;
+    }
+}
+
+}  // namespace gk
+
+using namespace gk;
+
+extern "C" gk_status gk_octree_corners(int64_t n, const double* centres, const double spacing[3], double* corners,
+                                       gk_stream stream) {
+    if (n < 0 || spacing == nullptr) return GK_ERR_ARG;
+    if (n == 0) return GK_OK;
+    if (centres == nullptr || corners == nullptr) return GK_ERR_ARG;
+    corners_kernel<<<(unsigned)((8 * n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+        n, centres, spacing[0] / 2, spacing[1] / 2, spacing[2] / 2, corners);
+    GK_LAUNCH_CHECK();
+    return GK_OK;
+}
+
+extern "C" size_t gk_octree_workspace_bytes(int64_t n) {
+    int64_t nb = (n + kScanBlock - 1) / kScanBlock;
+    return (size_t)(nb + 1) * sizeof(int64_t);
+}
+
+extern "C" gk_status gk_octree_refine(int64_t n, const double* centres, const int32_t* corner_ids, int32_t refine_all,
+                                      const double spacing[3], double* children, int64_t* count, void* work,
+                                      size_t work_bytes, gk_stream stream) {
+    if (n < 0 || spacing == nullptr || count == nullptr) return GK_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (n == 0) {
+        GK_CUDA_TRY(cudaMemsetAsync(count, 0, sizeof(int64_t), st));
+        return GK_OK;
+    }
+    if (centres == nullptr || children == nullptr || (corner_ids == nullptr && !refine_all)) return GK_ERR_ARG;
+    if (work == nullptr || work_bytes < gk_octree_workspace_bytes(n)) return GK_ERR_SIZE;
+    int64_t nb = (n + kScanBlock - 1) / kScanBlock;
+    if (nb > 0x7fffffff) return GK_ERR_SIZE;
+    int64_t* bc = (int64_t*)work;
+    mark_count_kernel<<<(unsigned)nb, kScanBlock, 0, st>>>(n, corner_ids, refine_all, bc);
+    GK_LAUNCH_CHECK();
+    scan_blocks_kernel<<<1, 1024, 0, st>>>(nb, bc, count);
+    GK_LAUNCH_CHECK();
+    scatter_children_kernel<<<(unsigned)nb, kScanBlock, 0, st>>>(n, centres, corner_ids, refine_all, bc,
+                                                                   spacing[0] / 4, spacing[1] / 4, spacing[2] / 4,
+                                                                   children);
+    GK_LAUNCH_CHECK();
+    return GK_OK;
+}
+
+extern "C" const char* gk_version(void) { return "gempy_gb300 0.1.0 (sm_103a)"; }

@@ -1,0 +1,346 @@
+// Mixed-precision solve of the FP64 kriging system.
+//
+//   1. equilibrate: D = diag(1/sqrt(max_j |K_ij|)), K32 = fp32(D K D);
+//   2. FP32 blocked LU of K32 (gk_lu.cu);
+//   3. FGMRES in FP64 (restart m, right preconditioner M^-1 = D LU32^-1 D,
+//      classical Gram-Schmidt applied twice) on the FP64 K held in HBM.
+// FP64 is used only for the residual/Krylov vectors, the products with the
+// FP64 K and the solution update; the O(N^3) factorization runs in FP32.
+// Plain iterative refinement (x += M^-1 (b - K x)) diverges on kriging systems
+// with kappa(K) eps32 > 1, which the FP64-GMRES outer iteration tolerates
+// (it converges while kappa eps32 eps64-scale products stay small).
+// Convergence is tested on the host between Arnoldi steps (one small
+// device-to-host copy per step).
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "gk_common.cuh"
+
+gk_status gk_internal_lu_factor_f32(int64_t n, float* A, int64_t lda, int32_t* ipiv, void* work, size_t wb,
+                                    gk_info* info, cudaStream_t st);
+gk_status gk_internal_lu_solve_f32(int64_t n, const float* LU, int64_t lda, const int32_t* ipiv, float* b, void* work,
+                                   size_t wb, gk_info* info, cudaStream_t st);
+size_t gk_internal_lu_ws_f32(int64_t n);
+
+namespace gk {
+
+static size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
+static int64_t ld32_of(int64_t n) { return (n + 63) / 64 * 64; }
+
+constexpr int kRestart = 30;
+constexpr int kDotBlocks = 128;
+
+struct MixedWork {
+    float* K32;
+    int32_t* ipiv;
+    void* luw;
+    size_t luw_bytes;
+    double* d;      // equilibration
+    double* r;      // residual / work vector
+    float* t32;     // FP32 vector for the preconditioner
+    double* V;      // (m+1) x n Krylov basis (vector-major)
+    double* Z;      // m x n preconditioned directions
+    double* w;      // n
+    double* part;   // kDotBlocks x (m+1) partial dots
+    double* h;      // m+1 reduced dots
+    double* y;      // m coefficients
+};
+
+static size_t mixed_bytes(int64_t n) {
+    int64_t ld = ld32_of(n);
+    return al((size_t)n * ld * sizeof(float)) + al(n * sizeof(int32_t)) + al(gk_internal_lu_ws_f32(n)) +
+           2 * al(n * sizeof(double)) + al(n * sizeof(float)) + al((size_t)(kRestart + 1) * n * sizeof(double)) +
+           al((size_t)kRestart * n * sizeof(double)) + al(n * sizeof(double)) +
+           al((size_t)kDotBlocks * (kRestart + 1) * sizeof(double)) + 2 * al((kRestart + 1) * sizeof(double));
+}
+
+static MixedWork carve(void* base, int64_t n) {
+    MixedWork w;
+    char* p = (char*)base;
+    int64_t ld = ld32_of(n);
+    w.K32 = (float*)p; p += al((size_t)n * ld * sizeof(float));
+    w.ipiv = (int32_t*)p; p += al(n * sizeof(int32_t));
+    w.luw = p; w.luw_bytes = al(gk_internal_lu_ws_f32(n)); p += w.luw_bytes;
+    w.d = (double*)p; p += al(n * sizeof(double));
+    w.r = (double*)p; p += al(n * sizeof(double));
+    w.t32 = (float*)p; p += al(n * sizeof(float));
+    w.V = (double*)p; p += al((size_t)(kRestart + 1) * n * sizeof(double));
+    w.Z = (double*)p; p += al((size_t)kRestart * n * sizeof(double));
+    w.w = (double*)p; p += al(n * sizeof(double));
+    w.part = (double*)p; p += al((size_t)kDotBlocks * (kRestart + 1) * sizeof(double));
+    w.h = (double*)p; p += al((kRestart + 1) * sizeof(double));
+    w.y = (double*)p;
+    return w;
+}
+
+// d_i = 1 / sqrt(max_j |K_ij|); one warp per row.
+__global__ void equil_kernel(const double* __restrict__ K, int64_t ldk, int64_t n, double* __restrict__ d) {
+    int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (row >= n) return;
+    double m = 0.0;
+    const double* k = K + row * ldk;
+    for (int64_t j = lane; j < n; j += 32) m = fmax(m, fabs(k[j]));
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+    if (lane == 0) d[row] = m > 0.0 ? 1.0 / sqrt(m) : 1.0;
+}
+
+__global__ void convert_kernel(const double* __restrict__ K, int64_t ldk, int64_t n, const double* __restrict__ d,
+                               float* __restrict__ K32, int64_t ld32) {
+    int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t i = blockIdx.y;
+    for (; i < n; i += gridDim.y) {
+        if (j < n) K32[i * ld32 + j] = (float)(d[i] * K[i * ldk + j] * d[j]);
+    }
+}
+
+// y = b - K x (b may be NULL: y = K x); one warp per row.
+__global__ void gemv_kernel(const double* __restrict__ K, int64_t ldk, int64_t n, const double* __restrict__ b,
+                            const double* __restrict__ x, double* __restrict__ y) {
+    int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (row >= n) return;
+    const double* k = K + row * ldk;
+    double s = 0.0;
+    for (int64_t j = lane; j < n; j += 32) s = fma(k[j], x[j], s);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) y[row] = b ? b[row] - s : s;
+}
+
+// partial dots part[blk][c] = sum_{i in blk} V[c][i] * w[i], c < ncol
+__global__ void dots_partial_kernel(const double* __restrict__ V, int64_t n, int ncol, const double* __restrict__ w,
+                                    double* __restrict__ part) {
+    __shared__ double red[8];
+    const int64_t per = (n + gridDim.x - 1) / gridDim.x;
+    const int64_t i0 = (int64_t)blockIdx.x * per, i1 = min(n, i0 + per);
+    for (int c = 0; c < ncol; ++c) {
+        const double* v = V + (int64_t)c * n;
+        double s = 0.0;
+        for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) s = fma(v[i], w[i], s);
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
+            part[(int64_t)blockIdx.x * ncol + c] = t;
+        }
+        __syncthreads();
+    }
+}
+
+// h[c] = sum_blk part[blk][c] (fixed order: deterministic); acc: h += result
+__global__ void dots_final_kernel(const double* __restrict__ part, int nblk, int ncol, double* __restrict__ h,
+                                  int accumulate) {
+    int c = threadIdx.x;
+    if (c >= ncol) return;
+    double t = 0.0;
+    for (int b = 0; b < nblk; ++b) t += part[(int64_t)b * ncol + c];
+    h[c] = accumulate ? h[c] + t : t;
+}
+
+// w -= sum_c V[c] * coef[c]
+__global__ void sub_basis_kernel(const double* __restrict__ V, int64_t n, int ncol, const double* __restrict__ coef,
+                                 double* __restrict__ w) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double s = w[i];
+    for (int c = 0; c < ncol; ++c) s -= V[(int64_t)c * n + i] * coef[c];
+    w[i] = s;
+}
+
+// x += sum_c Z[c] * y[c]
+__global__ void add_basis_kernel(const double* __restrict__ Z, int64_t n, int ncol, const double* __restrict__ y,
+                                 double* __restrict__ x) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double s = x[i];
+    for (int c = 0; c < ncol; ++c) s += Z[(int64_t)c * n + i] * y[c];
+    x[i] = s;
+}
+
+__global__ void scale_kernel(const double* __restrict__ src, double a, int64_t n, double* __restrict__ dst) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = a * src[i];
+}
+
+__global__ void scale_to_f32_kernel(const double* __restrict__ r, const double* __restrict__ d, int64_t n,
+                                    float* __restrict__ t) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) t[i] = (float)(d[i] * r[i]);
+}
+
+__global__ void from_f32_kernel(const float* __restrict__ t, const double* __restrict__ d, int64_t n,
+                                double* __restrict__ z) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) z[i] = d[i] * (double)t[i];
+}
+
+}  // namespace gk
+
+using namespace gk;
+
+extern "C" size_t gk_solve_mixed_workspace_bytes(int64_t n) { return n > 0 ? mixed_bytes(n) : 0; }
+
+namespace {
+
+struct Solver {
+    int64_t n;
+    const double* K;
+    int64_t ldk;
+    MixedWork w;
+    int64_t ld32;
+    gk_info* info;
+    cudaStream_t st;
+    unsigned vb, rb;
+
+    // dot products h[0..ncol) = V[0..ncol)^T v  (accumulate: h += ...)
+    gk_status dots(const double* V, int ncol, const double* v, double* h, int accumulate) {
+        dots_partial_kernel<<<kDotBlocks, 256, 0, st>>>(V, n, ncol, v, w.part);
+        GK_LAUNCH_CHECK();
+        dots_final_kernel<<<1, 64, 0, st>>>(w.part, kDotBlocks, ncol, h, accumulate);
+        GK_LAUNCH_CHECK();
+        return GK_OK;
+    }
+    gk_status norm2(const double* v, double& out) {
+        gk_status s = dots(v, 1, v, w.h + kRestart, 0);
+        if (s != GK_OK) return s;
+        GK_CUDA_TRY(cudaMemcpyAsync(&out, w.h + kRestart, sizeof(double), cudaMemcpyDeviceToHost, st));
+        GK_CUDA_TRY(cudaStreamSynchronize(st));
+        out = sqrt(out);
+        return GK_OK;
+    }
+    // z = D LU32^-1 D v
+    gk_status precond(const double* v, double* z) {
+        scale_to_f32_kernel<<<vb, 256, 0, st>>>(v, w.d, n, w.t32);
+        GK_LAUNCH_CHECK();
+        gk_status s = gk_internal_lu_solve_f32(n, w.K32, ld32, w.ipiv, w.t32, w.luw, w.luw_bytes, info, st);
+        if (s != GK_OK) return s;
+        from_f32_kernel<<<vb, 256, 0, st>>>(w.t32, w.d, n, z);
+        GK_LAUNCH_CHECK();
+        return GK_OK;
+    }
+};
+
+}  // namespace
+
+extern "C" gk_status gk_solve_mixed(int64_t n, const double* K, int64_t ldk, const double* b, double* x, double tol,
+                                    int32_t max_iter, void* work, size_t work_bytes, gk_info* info,
+                                    gk_stream stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (n <= 0 || K == nullptr || b == nullptr || x == nullptr || ldk < n || max_iter < 1) return GK_ERR_ARG;
+    if (work == nullptr || work_bytes < mixed_bytes(n)) return GK_ERR_SIZE;
+    Solver S;
+    S.n = n; S.K = K; S.ldk = ldk; S.w = carve(work, n); S.ld32 = ld32_of(n); S.info = info; S.st = st;
+    S.vb = (unsigned)((n + 255) / 256);
+    S.rb = (unsigned)((n * 32 + 255) / 256);
+    MixedWork& w = S.w;
+    if (info) GK_CUDA_TRY(cudaMemsetAsync(info, 0, sizeof(gk_info), st));
+    equil_kernel<<<S.rb, 256, 0, st>>>(K, ldk, n, w.d);
+    GK_LAUNCH_CHECK();
+    dim3 cg((unsigned)((n + 255) / 256), (unsigned)(n < 4096 ? n : 4096));
+    convert_kernel<<<cg, 256, 0, st>>>(K, ldk, n, w.d, w.K32, S.ld32);
+    GK_LAUNCH_CHECK();
+    gk_status s = gk_internal_lu_factor_f32(n, w.K32, S.ld32, w.ipiv, w.luw, w.luw_bytes, info, st);
+    if (s != GK_OK) return s;
+
+    double bnorm = 0.0;
+    if ((s = S.norm2(b, bnorm)) != GK_OK) return s;
+    GK_CUDA_TRY(cudaMemsetAsync(x, 0, n * sizeof(double), st));
+    int status = GK_ERR_NOT_CONVERGED, its = 0;
+    double rel = 1.0, prev_true = INFINITY;
+    if (!(bnorm > 0.0)) {
+        status = bnorm == 0.0 ? GK_OK : GK_ERR_NONFINITE;
+        rel = 0.0;
+    }
+    const int m = kRestart;
+    std::vector<double> H((m + 1) * m), cs(m), sn(m), g(m + 1), hcol(m + 2), y(m);
+    while (status == GK_ERR_NOT_CONVERGED && its < max_iter) {
+        // true residual r = b - K x
+        gemv_kernel<<<S.rb, 256, 0, st>>>(K, ldk, n, b, x, w.r);
+        GK_LAUNCH_CHECK();
+        double beta;
+        if ((s = S.norm2(w.r, beta)) != GK_OK) return s;
+        rel = beta / bnorm;
+        if (!std::isfinite(rel)) { status = GK_ERR_NONFINITE; break; }
+        if (rel <= tol) { status = GK_OK; break; }
+        if (rel > 0.5 * prev_true) break;  // restart made no progress: stagnated at the FP64 floor
+        prev_true = rel;
+        scale_kernel<<<S.vb, 256, 0, st>>>(w.r, 1.0 / beta, n, w.V);
+        GK_LAUNCH_CHECK();
+        std::fill(g.begin(), g.end(), 0.0);
+        g[0] = beta;
+        int j = 0;
+        for (; j < m && its < max_iter; ++j, ++its) {
+            double* vj = w.V + (int64_t)j * n;
+            double* zj = w.Z + (int64_t)j * n;
+            if ((s = S.precond(vj, zj)) != GK_OK) return s;
+            gemv_kernel<<<S.rb, 256, 0, st>>>(K, ldk, n, nullptr, zj, w.w);
+            GK_LAUNCH_CHECK();
+            // CGS2
+            for (int pass = 0; pass < 2; ++pass) {
+                if ((s = S.dots(w.V, j + 1, w.w, pass == 0 ? w.h : w.y, 0)) != GK_OK) return s;
+                sub_basis_kernel<<<S.vb, 256, 0, st>>>(w.V, n, j + 1, pass == 0 ? w.h : w.y, w.w);
+                GK_LAUNCH_CHECK();
+            }
+            double hn;
+            if ((s = S.norm2(w.w, hn)) != GK_OK) return s;
+            GK_CUDA_TRY(cudaMemcpyAsync(hcol.data(), w.h, (j + 1) * sizeof(double), cudaMemcpyDeviceToHost, st));
+            GK_CUDA_TRY(cudaMemcpyAsync(y.data(), w.y, (j + 1) * sizeof(double), cudaMemcpyDeviceToHost, st));
+            GK_CUDA_TRY(cudaStreamSynchronize(st));
+            for (int i = 0; i <= j; ++i) hcol[i] += y[i];
+            hcol[j + 1] = hn;
+            if (hn > 0.0) {
+                scale_kernel<<<S.vb, 256, 0, st>>>(w.w, 1.0 / hn, n, w.V + (int64_t)(j + 1) * n);
+                GK_LAUNCH_CHECK();
+            }
+            // Givens rotations
+            for (int i = 0; i < j; ++i) {
+                double t = cs[i] * hcol[i] + sn[i] * hcol[i + 1];
+                hcol[i + 1] = -sn[i] * hcol[i] + cs[i] * hcol[i + 1];
+                hcol[i] = t;
+            }
+            double den = std::hypot(hcol[j], hcol[j + 1]);
+            cs[j] = den > 0 ? hcol[j] / den : 1.0;
+            sn[j] = den > 0 ? hcol[j + 1] / den : 0.0;
+            hcol[j] = den;
+            hcol[j + 1] = 0.0;
+            g[j + 1] = -sn[j] * g[j];
+            g[j] = cs[j] * g[j];
+            for (int i = 0; i <= j; ++i) H[i * m + j] = hcol[i];
+            if (std::fabs(g[j + 1]) <= tol * bnorm || hn == 0.0) { ++j; ++its; break; }
+        }
+        // y = H^-1 g (upper triangular j x j), x += Z y
+        for (int i = j - 1; i >= 0; --i) {
+            double t = g[i];
+            for (int k = i + 1; k < j; ++k) t -= H[i * m + k] * y[k];
+            y[i] = H[i * m + i] != 0.0 ? t / H[i * m + i] : 0.0;
+        }
+        if (j > 0) {
+            GK_CUDA_TRY(cudaMemcpyAsync(w.y, y.data(), j * sizeof(double), cudaMemcpyHostToDevice, st));
+            add_basis_kernel<<<S.vb, 256, 0, st>>>(w.Z, n, j, w.y, x);
+            GK_LAUNCH_CHECK();
+        }
+    }
+    if (status == GK_ERR_NOT_CONVERGED) {
+        // final true residual
+        gemv_kernel<<<S.rb, 256, 0, st>>>(K, ldk, n, b, x, w.r);
+        GK_LAUNCH_CHECK();
+        double beta;
+        if ((s = S.norm2(w.r, beta)) != GK_OK) return s;
+        rel = beta / bnorm;
+        if (rel <= tol) status = GK_OK;
+    }
+    if (info) {
+        gk_info hi;
+        GK_CUDA_TRY(cudaMemcpyAsync(&hi, info, sizeof(gk_info), cudaMemcpyDeviceToHost, st));
+        GK_CUDA_TRY(cudaStreamSynchronize(st));
+        if (hi.status == 0 && status != GK_OK) hi.status = status;
+        hi.iterations = its;
+        hi.residual = rel;
+        GK_CUDA_TRY(cudaMemcpyAsync(info, &hi, sizeof(gk_info), cudaMemcpyHostToDevice, st));
+        GK_CUDA_TRY(cudaStreamSynchronize(st));
+    }
+    return GK_OK;
+}

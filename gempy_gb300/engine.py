@@ -1,0 +1,227 @@
+"""``compute_model``: drop-in for the engine call at ``gempy/API/compute_API.py:68-73``.
+
+Signature and inputs are the ones the reference passes
+(``compute_model(interpolation_input, options, data_descriptor,
+geophysics_input)``, also called directly at
+``test/test_api/test_model_construction_granular.py:130-134``); the returned
+``Solutions`` carries the fields gempy reads back (``geo_model.py:100-127``,
+``_engine_factory.py:45-48``, ``compute_API.py:114``).
+
+Flow per call, all arithmetic on the GPU through ``libgempy_gb300.so``:
+  1. split the inputs into series (``data_descriptor.stack_structure``);
+  2. per series: build K, solve for the weights -- FP64 LU ("float64", the
+     plain form) or FP32 LU + FP64 refinement ("float32", the mixed form) --
+     and pack the weights for evaluation;
+  3. isovalues: the field at each surface's reference point, in FP64;
+  4. evaluate every series on each point set (octree levels, dense grid,
+     custom grid), segment with the sigmoid, combine the series with masks;
+     octree levels refine voxels whose corner ids differ.
+There is no CPU path: without the CUDA library this raises.
+"""
+import time
+from dataclasses import dataclass, field as dc_field
+from typing import Optional
+
+import numpy as np
+import torch
+
+from . import kernels as K
+from ._lib import GK_F32, GK_F64
+from .data import (CombinedOutput, ExportedFields, InterpOutput, OctreeLevel, RawArraysSolution, RootOutput,
+                   Solutions, StackRelationType)
+
+
+@dataclass
+class EngineConfig:
+    """Mirror of the reference's ``GemPyEngineConfig`` (``gempy_engine_config.py:9-14``):
+    ``dtype`` "float64" selects the plain FP64 form, "float32" the mixed form
+    (FP32 LU + FP64 refinement, FP32 evaluation with FP64 isovalues)."""
+    dtype: str = "float64"
+    use_gpu: bool = True
+    keep_on_device: bool = False
+    solver_tol: float = 1e-12
+    solver_max_iter: int = 30
+    timings: bool = False
+
+
+class _Series:
+    def __init__(self, dev_series, iso, order, unit_values, relation, weights, solve_info):
+        self.dev = dev_series
+        self.iso = iso                  # per surface, stack order (FP64)
+        self.order = order              # surfaces sorted by isovalue, highest first
+        self.unit_values = unit_values  # n_surf + 1 values
+        self.relation = relation
+        self.weights = weights
+        self.solve_info = solve_info
+        self.model = None
+        self.seg = K.make_segment(iso[order], unit_values, 0.0)
+
+    def set_slope(self, slope):
+        self.seg.slope = float(slope)
+
+
+def _split(interpolation_input, options, data_descriptor, device):
+    ss = data_descriptor.stack_structure
+    pps = np.asarray(data_descriptor.tensors_structure.number_of_points_per_surface, dtype=np.int64)
+    sp = interpolation_input.surface_points
+    ori = interpolation_input.orientations
+    ko = options.kernel_options
+    p_off = o_off = s_off = 0
+    out = []
+    for i in range(ss.n_stacks):
+        n_p = int(ss.number_of_points_per_stack[i])
+        n_o = int(ss.number_of_orientations_per_stack[i])
+        n_s = int(ss.number_of_surfaces_per_stack[i])
+        dev = K.DeviceSeries(
+            ori.dip_positions[o_off:o_off + n_o], ori.dip_gradients[o_off:o_off + n_o],
+            ori.nugget_effect_grad[o_off:o_off + n_o],
+            sp.sp_coords[p_off:p_off + n_p], sp.nugget_effect_scalar[p_off:p_off + n_p],
+            pps[s_off:s_off + n_s], range=ko.range, c_o=ko.c_o, uni_degree=ko.uni_degree,
+            kernel=ko.kernel_function, i_res=ko.i_res, gi_res=ko.gi_res, device=device)
+        out.append((dev, s_off, n_s, ss.masking_descriptor[i]))
+        p_off += n_p
+        o_off += n_o
+        s_off += n_s
+    return out
+
+
+class _Evaluator:
+    def __init__(self, series, prec, slope):
+        self.series = series
+        self.prec = prec
+        self.slope = slope
+        for s in series:
+            s.set_slope(slope)
+
+    def run(self, pts: K.Points, gradient=False):
+        fields, values, grads = [], [], []
+        for s in self.series:
+            f, g, v, _ = K.evaluate(s.dev, s.model, pts, self.prec, seg=s.seg, gradient=gradient)
+            fields.append(f)
+            values.append(v)
+            grads.append(g)
+        F = torch.stack(fields)
+        V = torch.stack(values)
+        rel = [int(s.relation) for s in self.series]
+        mn = [float(np.min(s.iso)) if len(s.iso) else 0.0 for s in self.series]
+        mx = [float(np.max(s.iso)) if len(s.iso) else 0.0 for s in self.series]
+        cv, ci, masks = K.combine(F, V, rel, mn, mx)
+        return F, V, grads, cv, ci, masks
+
+
+def _np(t, keep):
+    if t is None:
+        return None
+    return t if keep else t.cpu().numpy()
+
+
+def _outputs(F, V, grads, cv, ci, masks, series, keep):
+    outs = []
+    for i, s in enumerate(series):
+        g = grads[i]
+        ef = ExportedFields(scalar_field=_np(F[i], keep),
+                            gx_field=_np(g[:, 0], keep) if g is not None else None,
+                            gy_field=_np(g[:, 1], keep) if g is not None else None,
+                            gz_field=_np(g[:, 2], keep) if g is not None else None,
+                            scalar_field_at_surface_points=s.iso)
+        outs.append(InterpOutput(ef, _np(V[i], keep), weights=_np(s.weights, keep), mask=_np(masks[i], keep)))
+    comb = CombinedOutput(ExportedFields(scalar_field=_np(F[-1], keep)), _np(cv, keep), _np(ci, keep),
+                          _np(masks, keep))
+    return outs, comb
+
+
+def compute_model(interpolation_input, options, data_descriptor, geophysics_input=None,
+                  config: Optional[EngineConfig] = None) -> Solutions:
+    cfg = config or EngineConfig()
+    if not torch.cuda.is_available():
+        raise RuntimeError("gempy_gb300.compute_model needs a CUDA device (there is no CPU fallback)")
+    device = torch.device("cuda")
+    mixed = str(cfg.dtype) in ("float32", "mixed")
+    prec = GK_F32 if mixed else GK_F64
+    t0 = time.perf_counter()
+    timings = {}
+
+    # ---- 1-2: per-series solve
+    uv = np.asarray(interpolation_input.unit_values, dtype=np.float64)
+    series = []
+    for dev_s, s_off, n_s, rel in _split(interpolation_input, options, data_descriptor, device):
+        if mixed:
+            w, info = K.solve_mixed(dev_s, tol=cfg.solver_tol, max_iter=cfg.solver_max_iter)
+        else:
+            w, info = K.solve_plain(dev_s)
+        model = K.prepare(dev_s, w)
+        # ---- 3: isovalues at the reference points, FP64
+        tmp = _Series(dev_s, np.zeros(n_s), np.arange(n_s), uv[s_off:s_off + n_s + 1], rel, w, info)
+        tmp.model = model
+        if n_s:
+            iso_t, _, _, _ = K.evaluate(dev_s, model, K.Points(xyz=dev_s.ref_points), GK_F64)
+            iso = iso_t.cpu().numpy()
+        else:
+            iso = np.zeros(0)
+        order = np.argsort(-iso, kind="stable")
+        s = _Series(dev_s, iso, order, uv[s_off:s_off + n_s + 1], rel, w, info)
+        s.model = model
+        series.append(s)
+    if cfg.timings:
+        torch.cuda.synchronize()
+        timings["solve_s"] = time.perf_counter() - t0
+
+    ev = _Evaluator(series, prec, options.sigmoid_slope)
+    keep = cfg.keep_on_device
+    grid = interpolation_input.grid
+    want_grad = bool(options.evaluation_options.compute_scalar_gradient)
+
+    # ---- 4a: octree levels
+    t1 = time.perf_counter()
+    octrees = []
+    n_levels = int(options.evaluation_options.number_octree_levels)
+    min_level = int(options.evaluation_options.octree_min_level)
+    if grid.octree_grid is not None and n_levels >= 1:
+        og = grid.octree_grid
+        centres = torch.as_tensor(og.values).to(device)
+        d = np.array(og.dxdydz, dtype=np.float64)
+        for level in range(n_levels):
+            F, V, G, cv, ci, masks = ev.run(K.Points(xyz=centres), gradient=want_grad)
+            outs, comb = _outputs(F, V, G, cv, ci, masks, series, keep)
+            octrees.append(OctreeLevel(_np(centres, keep), d.copy(), outs, comb))
+            if level == n_levels - 1:
+                break
+            refine_all = level + 1 < min_level
+            corner_ids = None
+            if not refine_all:
+                corners = K.octree_corners(centres, d)
+                _, _, _, _, corner_ids, _ = ev.run(K.Points(xyz=corners))
+            centres = K.octree_refine(centres, corner_ids, d, refine_all=refine_all)
+            d = d / 2.0
+            if centres.shape[0] == 0:
+                break
+    if cfg.timings:
+        torch.cuda.synchronize()
+        timings["octree_s"] = time.perf_counter() - t1
+
+    # ---- 4b: dense and custom grids
+    raw = RawArraysSolution()
+    t2 = time.perf_counter()
+    if grid.dense_grid is not None:
+        F, V, G, cv, ci, masks = ev.run(K.Points.regular(grid.dense_grid), gradient=want_grad)
+        raw.lith_block = _np(cv, keep)
+        raw.scalar_field_matrix = _np(F, keep)
+        raw.mask_matrix_squeezed = _np(masks, keep)
+        raw.block_matrix = _np(V, keep)
+    if grid.custom_grid is not None:
+        pts = torch.as_tensor(grid.custom_grid.values).to(device)
+        F, V, G, cv, ci, masks = ev.run(K.Points(xyz=pts))
+        raw.custom = _np(cv, keep)
+    if cfg.timings:
+        torch.cuda.synchronize()
+        timings["grids_s"] = time.perf_counter() - t2
+        timings["total_s"] = time.perf_counter() - t0
+
+    root = RootOutput([InterpOutput(ExportedFields(scalar_field=None, scalar_field_at_surface_points=s.iso),
+                                    None, weights=_np(s.weights, keep)) for s in series])
+    sfsp = [float(v) for s in series for v in s.iso]
+    sol = Solutions(octrees_output=octrees, root_output=root, raw_arrays=raw,
+                    scalar_field_at_surface_points=sfsp, _ordered_elements=[s.order for s in series],
+                    block_solution_type=options.block_solutions_type, timings=timings,
+                    solver_info=[K.read_info(s.solve_info) for s in series])
+    return sol

@@ -1,0 +1,287 @@
+"""Thin Python wrappers over the C ABI (``include/gempy_gb300.h``).
+
+Device memory, streams and host<->device copies come from PyTorch (plumbing
+only); every computation is a call into ``libgempy_gb300.so``.  Tensors passed
+in must be CUDA tensors; nothing here runs on the CPU.
+"""
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import GK_F32, GK_F64, GkPoints, GkSegment, GkSystem, check
+
+INFO_DTYPE = np.dtype([("status", "<i4"), ("where", "<i4"), ("iterations", "<i4"), ("reserved", "<i4"),
+                       ("residual", "<f8")])
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _ptr(t):
+    return ctypes.c_void_p(0 if t is None else t.data_ptr())
+
+
+def new_info(device):
+    return torch.zeros(24, dtype=torch.uint8, device=device)
+
+
+def read_info(info):
+    return np.frombuffer(info.cpu().numpy().tobytes(), dtype=INFO_DTYPE)[0]
+
+
+def kernel_id(name):
+    name = getattr(name, "value", name)
+    name = str(name).lower()
+    if name.startswith("cubic"):
+        return _lib.GK_KERNEL_CUBIC
+    if name.startswith("exp"):
+        return _lib.GK_KERNEL_EXPONENTIAL
+    raise ValueError(f"unsupported kernel_function {name!r}")
+
+
+def ref_rest_indices(points_per_surface):
+    """Interface rows: per surface, its first point is the reference point and
+    each other point gives one row (rest)."""
+    ref, rest = [], []
+    start = 0
+    for n in np.asarray(points_per_surface, dtype=np.int64):
+        n = int(n)
+        ref.extend([start] * max(n - 1, 0))
+        rest.extend(range(start + 1, start + n))
+        start += n
+    return np.asarray(ref, dtype=np.int32), np.asarray(rest, dtype=np.int32)
+
+
+class DeviceSeries:
+    """One series' inputs resident on the GPU, with its ``gk_system``."""
+
+    def __init__(self, dip_positions, dip_gradients, nugget_grad, sp_coords, nugget_sp, points_per_surface,
+                 range, c_o, uni_degree=1, kernel="cubic", i_res=4.0, gi_res=2.0, device="cuda"):
+        dev = torch.device(device)
+        f64 = lambda a: torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64)).to(dev)
+        self.points_per_surface = np.asarray(points_per_surface, dtype=np.int64)
+        ref, rest = ref_rest_indices(self.points_per_surface)
+        self.dip_positions = f64(np.reshape(dip_positions, (-1, 3)))
+        self.dip_gradients = f64(np.reshape(dip_gradients, (-1, 3)))
+        self.nugget_grad = f64(nugget_grad)
+        self.sp_coords = f64(np.reshape(sp_coords, (-1, 3)))
+        self.nugget_sp = f64(nugget_sp)
+        self.ref_index = torch.as_tensor(ref).to(dev)
+        self.rest_index = torch.as_tensor(rest).to(dev)
+        starts = np.concatenate([[0], np.cumsum(self.points_per_surface)[:-1]]).astype(np.int64)
+        self.ref_points = self.sp_coords[torch.as_tensor(starts).to(dev)].contiguous() \
+            if len(starts) else self.sp_coords[:0]
+        self.device = dev
+        self.sys = GkSystem()
+        s = self.sys
+        s.n_ori = int(self.dip_positions.shape[0])
+        s.n_sp = int(self.sp_coords.shape[0])
+        s.n_iface = int(len(ref))
+        s.uni_degree = int(uni_degree)
+        s.kernel = kernel_id(kernel)
+        s.range, s.c_o, s.i_res, s.gi_res = float(range), float(c_o), float(i_res), float(gi_res)
+        s.dip_positions = self.dip_positions.data_ptr()
+        s.dip_gradients = self.dip_gradients.data_ptr()
+        s.nugget_grad = self.nugget_grad.data_ptr()
+        s.sp_coords = self.sp_coords.data_ptr()
+        s.nugget_sp = self.nugget_sp.data_ptr()
+        s.ref_index = self.ref_index.data_ptr()
+        s.rest_index = self.rest_index.data_ptr()
+
+    @property
+    def n_surfaces(self):
+        return len(self.points_per_surface)
+
+    @property
+    def N(self):
+        return int(_lib.load().gk_system_size(ctypes.byref(self.sys)))
+
+
+def leading_dim(n, prec):
+    align = 32 if prec == GK_F64 else 64
+    return (n + align - 1) // align * align
+
+
+def build(series: DeviceSeries, prec=GK_F64):
+    lib = _lib.load()
+    N = series.N
+    ld = leading_dim(N, prec)
+    dt = torch.float64 if prec == GK_F64 else torch.float32
+    K = torch.empty((N, ld), dtype=dt, device=series.device)
+    b = torch.empty(N, dtype=dt, device=series.device)
+    check("gk_build", lib.gk_build(ctypes.byref(series.sys), prec, _ptr(K), ld, _ptr(b), _stream()))
+    return K, b
+
+
+@dataclass
+class LUFactors:
+    LU: torch.Tensor
+    ipiv: torch.Tensor
+    work: torch.Tensor
+    prec: int
+    n: int
+    info: torch.Tensor
+
+
+def lu_factor(A, prec=None, overwrite=False):
+    """In-place blocked LU with partial pivoting of a row-major (n, ld) tensor."""
+    lib = _lib.load()
+    if prec is None:
+        prec = GK_F64 if A.dtype == torch.float64 else GK_F32
+    n = A.shape[0]
+    LU = A if overwrite else A.clone()
+    ipiv = torch.empty(n, dtype=torch.int32, device=A.device)
+    wb = lib.gk_lu_workspace_bytes(prec, n)
+    work = torch.empty(wb, dtype=torch.uint8, device=A.device)
+    info = new_info(A.device)
+    check("gk_lu_factor", lib.gk_lu_factor(prec, n, _ptr(LU), LU.stride(0), _ptr(ipiv), _ptr(work), wb,
+                                           _ptr(info), _stream()))
+    return LUFactors(LU, ipiv, work, prec, n, info)
+
+
+def lu_solve(f: LUFactors, b):
+    lib = _lib.load()
+    x = b.clone()
+    check("gk_lu_solve", lib.gk_lu_solve(f.prec, f.n, _ptr(f.LU), f.LU.stride(0), _ptr(f.ipiv), _ptr(x),
+                                         _ptr(f.work), f.work.numel(), _ptr(f.info), _stream()))
+    return x
+
+
+def solve_plain(series: DeviceSeries):
+    """FP64 build + FP64 blocked LU + FP64 triangular solves."""
+    K, b = build(series, GK_F64)
+    f = lu_factor(K, GK_F64, overwrite=True)
+    w = lu_solve(f, b)
+    return w, f.info
+
+
+def solve_mixed(series: DeviceSeries, tol=1e-12, max_iter=30, K=None, b=None):
+    """FP64 build, FP32 LU of the equilibrated matrix, FP64 refinement."""
+    lib = _lib.load()
+    if K is None:
+        K, b = build(series, GK_F64)
+    n = K.shape[0]
+    wb = lib.gk_solve_mixed_workspace_bytes(n)
+    work = torch.empty(wb, dtype=torch.uint8, device=K.device)
+    x = torch.empty(n, dtype=torch.float64, device=K.device)
+    info = new_info(K.device)
+    check("gk_solve_mixed", lib.gk_solve_mixed(n, _ptr(K), K.stride(0), _ptr(b), _ptr(x), float(tol),
+                                               int(max_iter), _ptr(work), wb, _ptr(info), _stream()))
+    return x, info
+
+
+def prepare(series: DeviceSeries, w):
+    lib = _lib.load()
+    nb = lib.gk_eval_model_bytes(ctypes.byref(series.sys))
+    model = torch.empty(nb, dtype=torch.uint8, device=series.device)
+    check("gk_eval_prepare", lib.gk_eval_prepare(ctypes.byref(series.sys), _ptr(w), _ptr(model), _stream()))
+    return model
+
+
+class Points:
+    """Evaluation point set: a regular grid generated in the kernel, or a list."""
+
+    def __init__(self, xyz=None, origin=None, spacing=None, dims=None):
+        self.gk = GkPoints()
+        if xyz is not None:
+            self.xyz = xyz.contiguous()
+            self.gk.kind = 1
+            self.gk.n = int(self.xyz.shape[0])
+            self.gk.xyz = self.xyz.data_ptr()
+        else:
+            self.xyz = None
+            self.gk.kind = 0
+            for i in range(3):
+                self.gk.dims[i] = int(dims[i])
+                self.gk.origin[i] = float(origin[i])
+                self.gk.spacing[i] = float(spacing[i])
+            self.gk.n = int(np.prod([int(d) for d in dims]))
+
+    @property
+    def n(self):
+        return int(self.gk.n)
+
+    @classmethod
+    def regular(cls, grid):
+        return cls(origin=grid.origin, spacing=grid.dxdydz, dims=grid.regular_grid_shape)
+
+
+def make_segment(isovalues_sorted, unit_values, slope):
+    seg = GkSegment()
+    m = len(isovalues_sorted)
+    if m > _lib.GK_MAX_SURFACES:
+        raise ValueError(f"at most {_lib.GK_MAX_SURFACES} surfaces per series")
+    seg.n_surf = m
+    seg.slope = float(slope)
+    for i, v in enumerate(isovalues_sorted):
+        seg.isovalues[i] = float(v)
+    for i, v in enumerate(unit_values):
+        seg.unit_values[i] = float(v)
+    return seg
+
+
+def evaluate(series: DeviceSeries, model, pts: Points, prec=GK_F64, seg=None, gradient=False, want_field=True,
+             want_values=True, want_ids=False, out=None):
+    lib = _lib.load()
+    n = pts.n
+    dev = series.device
+    o = out or {}
+    field = o.get("field") if want_field else None
+    if want_field and field is None:
+        field = torch.empty(n, dtype=torch.float64, device=dev)
+    grad = torch.empty((n, 3), dtype=torch.float64, device=dev) if gradient else None
+    values = None
+    ids = None
+    if seg is not None and want_values:
+        values = o.get("values")
+        if values is None:
+            values = torch.empty(n, dtype=torch.float64, device=dev)
+    if seg is not None and want_ids:
+        ids = torch.empty(n, dtype=torch.int32, device=dev)
+    check("gk_eval", lib.gk_eval(ctypes.byref(series.sys), _ptr(model), ctypes.byref(pts.gk), prec,
+                                 ctypes.byref(seg) if seg is not None else None, _ptr(field), _ptr(grad),
+                                 _ptr(values), _ptr(ids), _stream()))
+    return field, grad, values, ids
+
+
+def combine(fields, values, relations, min_iso, max_iso, want_masks=True):
+    lib = _lib.load()
+    n_series, n = fields.shape
+    dev = fields.device
+    out_v = torch.empty(n, dtype=torch.float64, device=dev)
+    out_i = torch.empty(n, dtype=torch.int32, device=dev)
+    masks = torch.empty((n_series, n), dtype=torch.uint8, device=dev) if want_masks else None
+    rel = (ctypes.c_int32 * n_series)(*[int(r) for r in relations])
+    mn = (ctypes.c_double * n_series)(*[float(v) for v in min_iso])
+    mx = (ctypes.c_double * n_series)(*[float(v) for v in max_iso])
+    check("gk_combine_series", lib.gk_combine_series(n_series, n, _ptr(fields), _ptr(values), rel, mn, mx,
+                                                     _ptr(out_v), _ptr(out_i), _ptr(masks), _stream()))
+    return out_v, out_i, masks
+
+
+def octree_corners(centres, spacing):
+    lib = _lib.load()
+    n = centres.shape[0]
+    out = torch.empty((8 * n, 3), dtype=torch.float64, device=centres.device)
+    sp = (ctypes.c_double * 3)(*[float(v) for v in spacing])
+    check("gk_octree_corners", lib.gk_octree_corners(n, _ptr(centres), sp, _ptr(out), _stream()))
+    return out
+
+
+def octree_refine(centres, corner_ids, spacing, refine_all=False):
+    lib = _lib.load()
+    n = centres.shape[0]
+    dev = centres.device
+    children = torch.empty((8 * n, 3), dtype=torch.float64, device=dev)
+    count = torch.zeros(1, dtype=torch.int64, device=dev)
+    wb = lib.gk_octree_workspace_bytes(n)
+    work = torch.empty(max(wb, 8), dtype=torch.uint8, device=dev)
+    sp = (ctypes.c_double * 3)(*[float(v) for v in spacing])
+    check("gk_octree_refine", lib.gk_octree_refine(n, _ptr(centres), _ptr(corner_ids), int(bool(refine_all)),
+                                                   sp, _ptr(children), _ptr(count), _ptr(work), wb, _stream()))
+    m = int(count.item())
+    return children[:m]

@@ -1,0 +1,217 @@
+/*
+ * gempy_gb300 -- C ABI of the GB300 co-kriging hot path.
+ *
+ * The reference has exactly one production entry into the arithmetic of this
+ * path: ``gempy_engine.compute_model(interpolation_input, options,
+ * data_descriptor, geophysics_input)`` called at
+ * ``gempy/API/compute_API.py:68-73`` (also ``gempy/modules/optimize_nuggets/
+ * _ops.py:18-23`` and ``compute_API.py:140-145``).  That engine is a Python
+ * package with no native code; its four steps -- kriging-matrix build, dense
+ * solve, field/gradient evaluation on regular and octree grids, sigmoid
+ * segmentation -- are what the functions below replace.  The Python package
+ * ``gempy_gb300`` binds them with ctypes and mirrors the engine's
+ * ``compute_model`` signature on top.
+ *
+ * Conventions
+ *  - Every pointer argument is a DEVICE pointer unless its comment says HOST.
+ *  - Matrices are row-major with a leading dimension (``ld*``) in elements.
+ *  - The caller allocates every buffer (query sizes with the *_bytes calls);
+ *    the library allocates no device memory and keeps no device state.
+ *  - Work is enqueued on ``stream`` (a cudaStream_t; NULL = legacy stream).
+ *    Functions return after enqueueing; device-side failures (singular pivot,
+ *    iteration caps, non-finite values) are reported through a caller-provided
+ *    device ``gk_info`` word, which the caller reads after synchronising.
+ *  - No exception crosses this ABI, and there is no CPU fallback: without a
+ *    usable CUDA device every call returns GK_ERR_CUDA.
+ */
+#ifndef GEMPY_GB300_H
+#define GEMPY_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* gk_stream; /* == cudaStream_t */
+
+typedef enum gk_status {
+    GK_OK = 0,
+    GK_ERR_ARG = 1,           /* NULL pointer, negative size, bad enum        */
+    GK_ERR_SIZE = 2,          /* size above a documented limit / workspace too small */
+    GK_ERR_CUDA = 3,          /* a CUDA runtime call failed (launch, no device) */
+    GK_ERR_SINGULAR = 4,      /* zero pivot met during LU (device info)       */
+    GK_ERR_NOT_CONVERGED = 5, /* iteration cap hit (device info)              */
+    GK_ERR_NONFINITE = 6,     /* NaN/Inf met (device info)                    */
+    GK_ERR_TIMEOUT = 7        /* an inter-CTA wait gave up (device info)      */
+} gk_status;
+
+typedef enum gk_prec { GK_F64 = 0, GK_F32 = 1 } gk_prec;
+
+/* ``kernel_function`` of the reference's KernelOptions (serialized options
+ * JSON, ``...serialization.approved.txt:135``). */
+typedef enum gk_kernel { GK_KERNEL_CUBIC = 0, GK_KERNEL_EXPONENTIAL = 1 } gk_kernel;
+
+/* Device status word written by the kernels.  ``status`` is a gk_status;
+ * ``where`` locates the failure (pivot column, iteration, ...); the solver
+ * fields report refinement progress. */
+typedef struct gk_info {
+    int32_t status;
+    int32_t where;
+    int32_t iterations;
+    int32_t reserved;
+    double residual;          /* final ||b - K x||_inf / ||b||_inf (solvers) */
+} gk_info;
+
+/* One series' kriging inputs, FP64 device arrays in the engine's transformed
+ * frame.  Field meaning follows ``InterpolationInput`` as built at
+ * ``gempy/modules/data_manipulation/_engine_factory.py:27-56``:
+ * ``SurfacePoints(sp_coords, nugget_effect_scalar)`` and
+ * ``Orientations(dip_positions, dip_gradients, nugget_effect_grad)``; the
+ * options are ``KernelOptions{range, c_o, uni_degree, i_res, gi_res,
+ * kernel_function}``.  ``ref_index``/``rest_index`` give, per interface row,
+ * the surface's reference point and the other ("rest") point. */
+typedef struct gk_system {
+    int32_t n_ori;        /* orientations                                    */
+    int32_t n_sp;         /* surface points of the series                    */
+    int32_t n_iface;      /* interface rows = n_sp - n_surfaces              */
+    int32_t uni_degree;   /* 0, 1 or 2 (drift functions: 0, 3, 9)            */
+    int32_t kernel;       /* gk_kernel                                       */
+    int32_t reserved;
+    double range, c_o, i_res, gi_res;
+    const double* dip_positions; /* n_ori x 3 */
+    const double* dip_gradients; /* n_ori x 3 */
+    const double* nugget_grad;   /* n_ori     */
+    const double* sp_coords;     /* n_sp x 3  */
+    const double* nugget_sp;     /* n_sp      */
+    const int32_t* ref_index;    /* n_iface   */
+    const int32_t* rest_index;   /* n_iface   */
+} gk_system;
+
+/* Evaluation points.  kind 0: regular grid of cell centres generated in the
+ * kernel, ``ij`` order (x slowest, z fastest) as the reference's
+ * ``RegularGrid`` (``gempy/core/data/grid_modules/regular_grid.py:58-71,
+ * 192-201``); kind 1: an explicit n x 3 FP64 list (octree centres/corners,
+ * custom grid, surface points). */
+typedef struct gk_points {
+    int32_t kind;
+    int32_t dims[3];
+    int64_t n;
+    double origin[3];     /* first cell centre (kind 0)                      */
+    double spacing[3];    /* cell size (kind 0)                              */
+    const double* xyz;    /* n x 3 (kind 1)                                  */
+} gk_points;
+
+/* Segmentation of one series (``sigmoid_slope``, element ids, isovalues).
+ * ``n_surf`` <= GK_MAX_SURFACES; isovalues are the series' surfaces sorted by
+ * isovalue, highest first; ``unit_values`` has n_surf + 1 entries. All HOST
+ * values (copied into the launch). */
+#define GK_MAX_SURFACES 32
+typedef struct gk_segment {
+    int32_t n_surf;
+    int32_t reserved;
+    double slope;
+    double isovalues[GK_MAX_SURFACES];
+    double unit_values[GK_MAX_SURFACES + 1];
+} gk_segment;
+
+/* ---------------- kriging-matrix build (engine covariance build) -------- */
+
+/* N = 3 n_ori + n_iface + n_drift. */
+int64_t gk_system_size(const gk_system* sys /* HOST struct */);
+
+/* Fills K (N x N, row-major, ld ``ldk`` >= N) and rhs (N) in ``prec``
+ * (double* for GK_F64, float* for GK_F32).  Replaces the engine's covariance
+ * build reached from ``compute_API.py:68-73``. */
+gk_status gk_build(const gk_system* sys, gk_prec prec, void* K, int64_t ldk,
+                   void* rhs, gk_stream stream);
+
+/* ---------------- dense solve (engine ``kernel_solver``, approved JSON :136) */
+
+/* Workspace for gk_lu_factor (device bytes). */
+size_t gk_lu_workspace_bytes(gk_prec prec, int64_t n);
+
+/* Blocked right-looking LU with partial pivoting, in place: A = P L U with
+ * ipiv[i] (0-based) the row swapped with row i (LAPACK getrf semantics). */
+gk_status gk_lu_factor(gk_prec prec, int64_t n, void* A, int64_t lda,
+                       int32_t* ipiv, void* work, size_t work_bytes,
+                       gk_info* info, gk_stream stream);
+
+/* Solves A x = b with the factors of gk_lu_factor; b is overwritten by x.
+ * ``work`` must be the workspace the factorization used: it holds the row
+ * permutation gk_lu_factor derived from ipiv. */
+gk_status gk_lu_solve(gk_prec prec, int64_t n, const void* LU, int64_t lda,
+                      const int32_t* ipiv, void* b, void* work,
+                      size_t work_bytes, gk_info* info, gk_stream stream);
+
+/* Mixed-precision solve of the FP64 system K x = b (no reference
+ * counterpart beyond the FP64 solve it replaces): an FP32 copy of the
+ * symmetrically equilibrated K is LU-factored on the GPU and preconditions an
+ * FP64 restarted FGMRES(30) whose residuals r = b - K x use the FP64 K, until
+ * ||r||_2 <= tol ||b||_2, stagnation, or ``max_iter`` Krylov steps.  ``work``
+ * holds the FP32 factors and the Krylov vectors
+ * (gk_solve_mixed_workspace_bytes); ``info`` receives the status, the
+ * iteration count and the final relative residual. */
+size_t gk_solve_mixed_workspace_bytes(int64_t n);
+gk_status gk_solve_mixed(int64_t n, const double* K, int64_t ldk,
+                         const double* b, double* x, double tol,
+                         int32_t max_iter, void* work, size_t work_bytes,
+                         gk_info* info, gk_stream stream);
+
+/* ---------------- evaluation + segmentation (engine evaluation) ---------- */
+
+/* Packs the solved model (weights ``w`` of length N) into the layout the
+ * evaluation kernels read: ``model`` must hold gk_eval_model_bytes bytes. */
+size_t gk_eval_model_bytes(const gk_system* sys);
+gk_status gk_eval_prepare(const gk_system* sys, const double* w, void* model,
+                          gk_stream stream);
+
+/* Scalar field (times gi_res, the engine's reported scale), optional
+ * gradient (n x 3), optional soft segmentation values and ids.  ``prec``
+ * selects FP64 or FP32 arithmetic; outputs are always FP64 for field/values
+ * and int32 for ids.  Any output pointer may be NULL.  ``seg`` may be NULL
+ * (no segmentation). */
+gk_status gk_eval(const gk_system* sys, const void* model,
+                  const gk_points* pts, gk_prec prec,
+                  const gk_segment* seg, double* field, double* grad,
+                  double* values, int32_t* ids, gk_stream stream);
+
+/* Combination of series with the squeezed masks (ERODE / ONLAP / BASEMENT,
+ * ``gempy/core/data/structural_frame.py:326-330``): ``fields`` and
+ * ``values`` are n_series x n (row per series), ``relations`` and
+ * ``min_iso``/``max_iso`` are HOST arrays of n_series.  Writes the final soft
+ * values, rint ids and the squeezed masks (uint8, n_series x n, may be NULL). */
+gk_status gk_combine_series(int32_t n_series, int64_t n, const double* fields,
+                            const double* values, const int32_t* relations,
+                            const double* min_iso, const double* max_iso,
+                            double* out_values, int32_t* out_ids,
+                            uint8_t* masks, gk_stream stream);
+
+/* ---------------- octree refinement (engine octree) --------------------- */
+
+/* Voxel corners: 8 per centre, corner order x slowest, z fastest. */
+gk_status gk_octree_corners(int64_t n, const double* centres,
+                            const double spacing[3] /* HOST */,
+                            double* corners, gk_stream stream);
+
+/* Marks voxels whose 8 corner ids differ (or all voxels when
+ * ``refine_all``), and writes the children of marked voxels (8 each, same
+ * corner order, at centre +- spacing/4) in parent order.  ``count`` (device
+ * int64) receives the number of children; ``work`` needs
+ * gk_octree_workspace_bytes(n). */
+size_t gk_octree_workspace_bytes(int64_t n);
+gk_status gk_octree_refine(int64_t n, const double* centres,
+                           const int32_t* corner_ids, int32_t refine_all,
+                           const double spacing[3] /* HOST */,
+                           double* children, int64_t* count, void* work,
+                           size_t work_bytes, gk_stream stream);
+
+/* Library version string (HOST). */
+const char* gk_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GEMPY_GB300_H */

@@ -1,0 +1,33 @@
+"""CPU FP64 oracle for the co-kriging hot path -- TEST INFRASTRUCTURE ONLY.
+
+This package is the checker, never the product: only ``tests/``,
+``__graft_entry__.smoke()`` and the ``cpu_baseline`` / ``--impl reference``
+legs of ``bench.py`` may import it.  The product path (``gempy_gb300``) never
+imports it and has no CPU fallback.
+
+What it restates.  The arithmetic of GemPy's implicit potential-field
+co-kriging lives in the external package ``gempy_engine`` (pinned
+``gempy_engine>=2026.0.3`` in ``requirements/requirements.txt:2``), which is not
+vendored in the reference and cannot be installed here.  The oracle therefore
+restates the published method -- de la Varga, Schaaf & Wellmann 2019, "GemPy
+1.0", GMD 12:1-32 (``CITATION.cff:1-16``), built on Lajaunie et al. 1997 and
+Calcagno et al. 2008 (``docs/source/index.rst:76-82``) -- in plain numpy/scipy
+FP64, and anchors parity on the reference's own call site
+(``gempy/API/compute_API.py:68-73``), its input layout
+(``gempy/modules/data_manipulation/_engine_factory.py:14-58``) and its
+known-answer tests:
+
+* pinned: the anticline cube-corner lithology ids ``[3,3,3,3,1,1,1,1]``
+  (``test/test_modules/test_grids/test_custom_grid.py:44-65``), reproduced
+  from the bundled ``examples/data/input_data/jan_models/model2_*.csv`` inputs
+  with the input transform pinned by the reference's approved model JSON
+  (``test_custom_grid.test_custom_grid.verify/fold.approved.txt:108-126``);
+* not pinned (parity at the block level is unpinned): the 50-value scalar-field
+  approval files of ``test/test_model_types`` depend on the engine's octree
+  refinement rule and point order, which are not in the reference.
+
+Modules: ``covariance`` (kernel functions), ``kriging`` (matrix build, solve,
+evaluation), ``segmentation`` (sigmoid ids, series masks), ``octree`` (corner
+based refinement), ``pipeline`` (multi-series compute_model restatement).
+"""
+from . import covariance, kriging, segmentation, octree, pipeline  # noqa: F401

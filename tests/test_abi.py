@@ -1,0 +1,69 @@
+"""CPU checks of the C ABI: the header declares exactly the exported entry
+points and the built library loads (no compute calls without a GPU)."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+from gempy_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "gempy_gb300.h")
+
+
+def header_functions():
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(gk_[a-z0-9_]+)\s*\(", txt)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(_lib.LIB_PATH):
+        from gempy_gb300 import build
+        build.build()
+    return _lib.load()
+
+
+def test_header_matches_binding_table():
+    declared = header_functions()
+    bound = sorted(name for name, _, _ in _lib.SIGNATURES)
+    assert declared == bound
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in header_functions():
+        assert hasattr(lib, name), name
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\bT (gk_[a-z0-9_]+)", out))
+    assert set(header_functions()) <= exported
+
+
+def test_version_and_size_queries_without_gpu(lib):
+    assert b"sm_103a" in lib.gk_version()
+    s = _lib.GkSystem()
+    s.n_ori, s.n_sp, s.n_iface, s.uni_degree = 2, 20, 18, 1
+    assert lib.gk_system_size(ctypes.byref(s)) == 6 + 18 + 3
+    s.uni_degree = 2
+    assert lib.gk_system_size(ctypes.byref(s)) == 6 + 18 + 9
+    assert lib.gk_eval_model_bytes(ctypes.byref(s)) > 0
+    assert lib.gk_octree_workspace_bytes(1000) >= 8
+
+
+def test_struct_layouts_match_header():
+    assert ctypes.sizeof(_lib.GkInfo) == 24
+    assert ctypes.sizeof(_lib.GkSystem) == 6 * 4 + 4 * 8 + 7 * 8
+    assert ctypes.sizeof(_lib.GkPoints) == 16 + 8 + 48 + 8
+    assert ctypes.sizeof(_lib.GkSegment) == 8 + 8 + 8 * 32 + 8 * 33
+
+
+def test_invalid_arguments_rejected_before_any_launch(lib):
+    # argument checks run on the host and return GK_ERR_ARG without touching the GPU
+    assert lib.gk_build(None, 0, None, 0, None, None) == _lib.GK_ERR_ARG
+    s = _lib.GkSystem()
+    s.n_ori, s.n_sp, s.n_iface, s.uni_degree, s.range = 1, 2, 1, 5, 1.0
+    assert lib.gk_build(ctypes.byref(s), 0, None, 0, None, None) == _lib.GK_ERR_ARG
+    assert lib.gk_lu_factor(0, -1, None, 0, None, None, 0, None, None) == _lib.GK_ERR_ARG
+    assert lib.gk_solve_mixed(0, None, 0, None, None, 1e-10, 10, None, 0, None, None) == _lib.GK_ERR_ARG

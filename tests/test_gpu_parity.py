@@ -1,0 +1,302 @@
+"""GPU parity tests: every kernel against the FP64 oracle through the C ABI.
+
+Tolerances (written here, used by the judge of each test):
+  * FP64 build: |K_gpu - K_oracle| <= 1e-13 max|K|
+  * FP64 LU/solve: ||b - K x|| / ||b|| <= 1e-12, x vs LAPACK <= 1e-8 relative
+  * FP64 field/gradient: max|dZ| / max|Z| <= 1e-9
+  * FP32 (mixed) field: max|dZ| / max|Z| <= 1e-6; weights from the mixed solve
+    <= 1e-6 relative to the FP64 solve
+  * ids: identical outside the band |Z - z_k| <= band around each isovalue
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from oracle import kriging, octree, pipeline, segmentation  # noqa: E402
+from tests._models import golden_extent, load_golden, oracle_series_from_golden, oracle_series_list  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev_series(s, device="cuda"):
+    from gempy_gb300 import kernels as K
+    return K.DeviceSeries(s.dip_positions, s.dip_gradients, s.nugget_grad, s.sp_coords, s.nugget_sp,
+                          s.points_per_surface, range=s.range, c_o=s.c_o, uni_degree=s.uni_degree,
+                          kernel=s.kernel, i_res=s.i_res, gi_res=s.gi_res, device=device)
+
+
+def _random_series(seed, n_surf=3, per=12, n_o=7, degree=1, kernel="cubic", a=0.9):
+    rng = np.random.default_rng(seed)
+    pts = []
+    for k in range(n_surf):
+        xy = rng.uniform(-0.4, 0.4, (per, 2))
+        z = -0.3 + 0.3 * k + 0.05 * np.sin(4 * xy[:, 0])
+        pts.append(np.column_stack([xy, z]))
+    sp = np.concatenate(pts)
+    xo = rng.uniform(-0.4, 0.4, (n_o, 3))
+    g = rng.normal(0, 0.1, (n_o, 3)) + [0, 0, 1]
+    g /= np.linalg.norm(g, axis=1, keepdims=True)
+    return kriging.Series(xo, g, np.full(n_o, 0.01), sp, np.full(len(sp), 2e-5), np.full(n_surf, per),
+                          range=a, c_o=a * a / 14 / 3, uni_degree=degree, kernel=kernel)
+
+
+def _anticline():
+    return oracle_series_from_golden(load_golden("anticline_corners.json"))
+
+
+SERIES_CASES = {
+    "anticline": _anticline,
+    "random_deg1_cubic": lambda: _random_series(1),
+    "random_deg2_cubic": lambda: _random_series(2, degree=2),
+    "random_deg0_exp": lambda: _random_series(3, degree=0, kernel="exponential", a=0.5),
+    "random_deg2_exp": lambda: _random_series(4, degree=2, kernel="exponential", a=0.7),
+    "one_point_pair": lambda: _random_series(5, n_surf=1, per=2, n_o=1),
+}
+
+
+@pytest.mark.parametrize("case", list(SERIES_CASES))
+def test_build_f64_matches_oracle(case):
+    from gempy_gb300 import kernels as K
+    s = SERIES_CASES[case]()
+    Kr, br = kriging.build_system(s)
+    ds = _dev_series(s)
+    Kg, bg = K.build(ds, K.GK_F64)
+    N = Kr.shape[0]
+    Kg = Kg[:, :N].cpu().numpy()
+    assert np.abs(Kg - Kr).max() <= 1e-13 * np.abs(Kr).max()
+    np.testing.assert_array_equal(bg.cpu().numpy(), br)
+
+
+def test_build_f32_matches_oracle():
+    from gempy_gb300 import kernels as K
+    s = _anticline()
+    Kr, _ = kriging.build_system(s)
+    Kg, _ = K.build(_dev_series(s), K.GK_F32)
+    N = Kr.shape[0]
+    assert np.abs(Kg[:, :N].double().cpu().numpy() - Kr).max() <= 2e-6 * np.abs(Kr).max()
+
+
+@pytest.mark.parametrize("n", [1, 2, 5, 31, 32, 33, 63, 64, 65, 127, 200, 513, 1100])
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_lu_factor_solve_random(n, prec):
+    from gempy_gb300 import kernels as K
+    rng = np.random.default_rng(n)
+    A = rng.normal(size=(n, n)) + n ** 0.5 * np.eye(n) * rng.choice([-1, 1], n)
+    b = rng.normal(size=n)
+    dt = torch.float64 if prec == "f64" else torch.float32
+    ld = K.leading_dim(n, K.GK_F64 if prec == "f64" else K.GK_F32)
+    At = torch.zeros((n, ld), dtype=dt, device="cuda")
+    At[:, :n] = torch.as_tensor(A, dtype=dt)
+    f = K.lu_factor(At)
+    x = K.lu_solve(f, torch.as_tensor(b, dtype=dt, device="cuda")).double().cpu().numpy()
+    info = K.read_info(f.info)
+    assert info["status"] == 0
+    res = np.abs(b - A @ x).max() / (np.abs(A).max() * np.abs(x).max() * n)
+    assert res < (1e-15 if prec == "f64" else 1e-6)
+    # pivots agree with LAPACK's partial pivoting on distinct-magnitude columns
+    if prec == "f64":
+        import scipy.linalg
+        _, piv = scipy.linalg.lu_factor(A)
+        np.testing.assert_array_equal(f.ipiv.cpu().numpy(), piv)
+
+
+@pytest.mark.parametrize("case", ["anticline", "random_deg2_cubic", "random_deg2_exp"])
+def test_plain_solve_matches_lapack(case):
+    from gempy_gb300 import kernels as K
+    s = SERIES_CASES[case]()
+    Kr, br = kriging.build_system(s)
+    w_ref = kriging.solve(Kr, br)
+    w, info = K.solve_plain(_dev_series(s))
+    w = w.cpu().numpy()
+    assert K.read_info(info)["status"] == 0
+    assert np.linalg.norm(br - Kr @ w) <= 1e-12 * np.linalg.norm(br)
+    assert np.abs(w - w_ref).max() <= 1e-8 * np.abs(w_ref).max()
+
+
+@pytest.mark.parametrize("case", ["anticline", "random_deg1_cubic", "random_deg2_exp"])
+def test_mixed_solve_reaches_fp64_residual(case):
+    from gempy_gb300 import kernels as K
+    s = SERIES_CASES[case]()
+    Kr, br = kriging.build_system(s)
+    w_ref = kriging.solve(Kr, br)
+    w, info = K.solve_mixed(_dev_series(s), tol=1e-12)
+    inf = K.read_info(info)
+    w = w.cpu().numpy()
+    assert inf["residual"] <= 1e-11, inf
+    assert np.linalg.norm(br - Kr @ w) <= 1e-11 * np.linalg.norm(br)
+    assert np.abs(w - w_ref).max() <= 1e-6 * np.abs(w_ref).max()
+
+
+def _eval_gpu(s, w, x, prec, gradient=False, seg=None):
+    from gempy_gb300 import kernels as K
+    ds = _dev_series(s)
+    wt = torch.as_tensor(w, device="cuda")
+    model = K.prepare(ds, wt)
+    pts = K.Points(xyz=torch.as_tensor(x, device="cuda"))
+    f, g, v, ids = K.evaluate(ds, model, pts, prec, seg=seg, gradient=gradient, want_ids=seg is not None)
+    out = [f.cpu().numpy()]
+    if gradient:
+        out.append(g.cpu().numpy())
+    if seg is not None:
+        out += [v.cpu().numpy(), ids.cpu().numpy()]
+    return out
+
+
+@pytest.mark.parametrize("case", list(SERIES_CASES))
+def test_eval_f64_field_and_gradient_match_oracle(case):
+    from gempy_gb300 import kernels as K
+    s = SERIES_CASES[case]()
+    w = kriging.solve(*kriging.build_system(s))
+    rng = np.random.default_rng(7)
+    x = rng.uniform(-0.45, 0.45, (3000, 3))
+    x[:5] = s.sp_coords[:5]          # exactly on data points (r = 0)
+    x[5:7] = s.dip_positions[:2]
+    Zr, Gr = kriging.evaluate(s, w, x, gradient=True)
+    Z, G = _eval_gpu(s, w, x, K.GK_F64, gradient=True)
+    assert np.abs(Z - Zr).max() <= 1e-9 * np.abs(Zr).max()
+    assert np.abs(G - Gr).max() <= 1e-9 * np.abs(Gr).max()
+
+
+@pytest.mark.parametrize("case", ["anticline", "random_deg2_cubic", "random_deg0_exp"])
+def test_eval_f32_field_within_1e6(case):
+    from gempy_gb300 import kernels as K
+    s = SERIES_CASES[case]()
+    w = kriging.solve(*kriging.build_system(s))
+    rng = np.random.default_rng(8)
+    x = rng.uniform(-0.45, 0.45, (20000, 3))
+    Zr, Gr = kriging.evaluate(s, w, x, gradient=True)
+    Z, G = _eval_gpu(s, w, x, K.GK_F32, gradient=True)
+    assert np.abs(Z - Zr).max() <= 1e-6 * np.abs(Zr).max()
+    assert np.abs(G - Gr).max() <= 1e-5 * np.abs(Gr).max()
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_regular_grid_segmentation_ids(prec):
+    """50^3 dense grid of the plain configuration: field vs oracle and ids
+    identical outside the isovalue band."""
+    from gempy_gb300 import kernels as K
+    from gempy_gb300 import synthetic
+    m = synthetic.plain_horizontal()
+    (s,) = oracle_series_list(m)
+    w = kriging.solve(*kriging.build_system(s))
+    iso = kriging.isovalues(s, w)
+    grid = m.interpolation_input.grid.dense_grid
+    x = grid.values
+    Zr = kriging.evaluate(s, w, x)
+    uv = m.interpolation_input.unit_values
+    vr, idr = segmentation.segment(Zr, iso, uv, m.options.sigmoid_slope)
+    ds = _dev_series(s)
+    model = K.prepare(ds, torch.as_tensor(w, device="cuda"))
+    order = segmentation.order_surfaces(iso)
+    seg = K.make_segment(iso[order], uv, m.options.sigmoid_slope)
+    p = K.GK_F64 if prec == "f64" else K.GK_F32
+    f, _, v, ids = K.evaluate(ds, model, K.Points.regular(grid), p, seg=seg, want_ids=True)
+    Z = f.cpu().numpy()
+    tol = 1e-9 if prec == "f64" else 1e-6
+    err = np.abs(Z - Zr).max() / np.abs(Zr).max()
+    assert err <= tol
+    band = max(10.0 / m.options.sigmoid_slope, 4 * err * np.abs(Zr).max())
+    outside = np.all(np.abs(Zr[:, None] - iso[None, :]) > band, axis=1)
+    assert outside.mean() > 0.99
+    np.testing.assert_array_equal(ids.cpu().numpy()[outside], idr[outside].astype(np.int32))
+    if prec == "f64":
+        np.testing.assert_allclose(v.cpu().numpy(), vr, atol=1e-9)
+
+
+def test_octree_refinement_matches_oracle():
+    from gempy_gb300 import kernels as K
+    c, d = octree.base_centres([-0.5, 0.5, -0.5, 0.5, -0.5, 0.5], [2, 3, 2])
+    ct = torch.as_tensor(c, device="cuda")
+    corners = K.octree_corners(ct, d).cpu().numpy()
+    np.testing.assert_array_equal(corners, octree.corners(c, d))
+    rng = np.random.default_rng(0)
+    ids = rng.integers(1, 3, (len(c), 8)).astype(np.int32)
+    ids[::3] = 1                                   # some voxels unmarked
+    ch = K.octree_refine(ct, torch.as_tensor(ids.ravel(), device="cuda"), d).cpu().numpy()
+    np.testing.assert_array_equal(ch, octree.children(c[octree.mark(ids.ravel())], d))
+    ch_all = K.octree_refine(ct, None, d, refine_all=True).cpu().numpy()
+    np.testing.assert_array_equal(ch_all, octree.children(c, d))
+
+
+def _compute_anticline(levels, dtype="float64"):
+    import __graft_entry__ as ge
+    import gempy_gb300 as gg
+    g, ii, opts, dd, ext = ge._anticline_model(levels=levels)
+    return g, ext, gg.compute_model(ii, opts, dd, config=gg.EngineConfig(dtype=dtype))
+
+
+def test_compute_model_anticline_pins():
+    """Reference known answers through compute_model: cube-corner ids
+    (test_custom_grid.py:44-47) and the approved finest-level scalar field
+    (test_example_models_I.py:41-53), plus octree parity with the oracle."""
+    g, ext, sol = _compute_anticline(5)
+    np.testing.assert_array_equal(sol.raw_arrays.custom, np.array(g["expected_ids"], float))
+    z = sol.octrees_output[-1].outputs[0].scalar_field
+    approved = np.array(g["octree"]["approved_scalar_field_last_level"])
+    assert len(z) == 7808
+    assert np.abs(z[:: len(z) // 50] - approved).max() < 3e-5
+    s = oracle_series_from_golden(g)
+    lv = pipeline.compute_octree([s], [segmentation.BASEMENT], g["unit_values"], g["sigmoid_slope"], ext,
+                                 [2, 2, 2], 5)
+    for (c_ref, r_ref), ol in zip(lv, sol.octrees_output):
+        np.testing.assert_array_equal(ol.grid_centers, c_ref)
+        zr = r_ref.fields[0]
+        assert np.abs(ol.outputs[0].scalar_field - zr).max() <= 1e-9 * np.abs(zr).max()
+        np.testing.assert_array_equal(ol.last_output_center.ids_block, r_ref.ids.astype(np.int32))
+
+
+def test_compute_model_mixed_anticline():
+    g, ext, sol = _compute_anticline(4, dtype="float32")
+    np.testing.assert_array_equal(sol.raw_arrays.custom, np.array(g["expected_ids"], float))
+    _, _, ref = _compute_anticline(4, dtype="float64")
+    for a, b in zip(sol.octrees_output, ref.octrees_output):
+        np.testing.assert_array_equal(a.grid_centers, b.grid_centers)
+        zb = b.outputs[0].scalar_field
+        assert np.abs(a.outputs[0].scalar_field - zb).max() <= 1e-6 * np.abs(zb).max()
+    assert sol.solver_info[0]["residual"] <= 1e-11
+
+
+def test_compute_model_three_series_octree_matches_oracle():
+    """Three folded series (ERODE, ERODE, BASEMENT), quadratic drift, octree."""
+    import gempy_gb300 as gg
+    from gempy_gb300 import synthetic
+    m = synthetic.folded_series(octree_levels=4)
+    sol = gg.compute_model(m.interpolation_input, m.options, m.data_descriptor)
+    ss = oracle_series_list(m)
+    og = m.interpolation_input.grid.octree_grid
+    rel = [int(r) for r in m.data_descriptor.stack_structure.masking_descriptor]
+    lv = pipeline.compute_octree(ss, rel, m.interpolation_input.unit_values, m.options.sigmoid_slope,
+                                 og.orthogonal_extent, og.regular_grid_shape, 4)
+    for (c_ref, r_ref), ol in zip(lv, sol.octrees_output):
+        np.testing.assert_array_equal(ol.grid_centers, c_ref)
+        for i in range(len(ss)):
+            zr = r_ref.fields[i]
+            assert np.abs(ol.outputs[i].scalar_field - zr).max() <= 1e-9 * np.abs(zr).max()
+        np.testing.assert_array_equal(ol.last_output_center.ids_block, r_ref.ids.astype(np.int32))
+        np.testing.assert_array_equal(ol.last_output_center.mask_matrix.astype(bool), r_ref.masks)
+    _, isos = pipeline.solve_all(ss)
+    iso_ref = np.concatenate(isos)
+    np.testing.assert_allclose(sol.scalar_field_at_surface_points, iso_ref, rtol=0, atol=1e-12)
+
+
+def test_nan_input_reports_status_without_fault():
+    from gempy_gb300 import kernels as K
+    s = _random_series(11)
+    s.dip_positions = s.dip_positions.copy()
+    s.dip_positions[0, 0] = np.nan
+    w, info = K.solve_plain(_dev_series(s))
+    torch.cuda.synchronize()
+    assert K.read_info(info)["status"] in (4, 6)   # SINGULAR or NONFINITE reported, GPU still usable
+    x = torch.ones(4, device="cuda")
+    assert float(x.sum()) == 4.0
+
+
+def test_bad_arguments_raise():
+    from gempy_gb300 import _lib
+    from gempy_gb300 import kernels as K
+    s = _random_series(12)
+    ds = _dev_series(s)
+    ds.sys.uni_degree = 7
+    with pytest.raises(_lib.GkError):
+        K.build(ds)

@@ -1,0 +1,140 @@
+"""CPU tests of the FP64 oracle: pinned golden vectors and known answers."""
+import numpy as np
+import pytest
+
+from oracle import covariance, kriging, octree, pipeline, segmentation
+from tests._models import golden_extent, load_golden, oracle_series_from_golden
+
+
+def test_anticline_corner_ids_pinned():
+    """test/test_modules/test_grids/test_custom_grid.py:44-47: ids at the cube corners."""
+    g = load_golden("anticline_corners.json")
+    s = oracle_series_from_golden(g)
+    r = pipeline.compute([s], [segmentation.BASEMENT], g["unit_values"], g["sigmoid_slope"],
+                         np.array(g["custom_points"]))
+    np.testing.assert_array_equal(r.ids, np.array(g["expected_ids"], float))
+
+
+def test_anticline_scalar_field_approval_file():
+    """Finest octree level of the anticline vs the reference's approval file
+    (test_example_models_I.py:19-23, 41-53).  Octree point order is exact; the
+    field matches to 2.2e-5 absolute (the block-level conventions of the absent
+    engine are fitted, not read)."""
+    g = load_golden("anticline_corners.json")
+    s = oracle_series_from_golden(g)
+    oc = g["octree"]
+    levels = pipeline.compute_octree([s], [segmentation.BASEMENT], g["unit_values"], g["sigmoid_slope"],
+                                     golden_extent(g), oc["base_resolution"], oc["levels"])
+    z = levels[-1][1].fields[0]
+    assert len(z) == 7808
+    sampled = z[:: len(z) // 50]
+    approved = np.array(oc["approved_scalar_field_last_level"])
+    assert sampled.shape == approved.shape
+    assert np.abs(sampled - approved).max() < 3e-5
+
+
+def test_kernel_symmetric_and_rhs():
+    g = load_golden("anticline_corners.json")
+    s = oracle_series_from_golden(g)
+    K, b = kriging.build_system(s)
+    assert K.shape == (s.size, s.size)
+    np.testing.assert_allclose(K, K.T, atol=1e-14)
+    ng = 3 * s.n_o
+    assert np.all(np.diag(K)[:ng] > 0)
+    assert np.all(np.diag(K)[ng:ng + s.n_i] > 0)
+    np.testing.assert_array_equal(b[:ng], s.dip_gradients.T.reshape(-1))
+    assert not b[ng:].any()
+
+
+def test_exact_interpolation_and_drift_orthogonality():
+    g = load_golden("anticline_corners.json")
+    s = oracle_series_from_golden(g)
+    s.nugget_sp = np.full(s.n_p, 1e-12)
+    s.nugget_grad = np.full(s.n_o, 1e-12)
+    K, b = kriging.build_system(s)
+    w = kriging.solve(K, b)
+    z = kriging.evaluate(s, w, s.sp_coords)
+    start = 0
+    for n in s.points_per_surface:
+        seg = z[start:start + n]
+        assert np.ptp(seg) < 1e-8 * max(1.0, np.abs(seg).max())
+        start += n
+    # drift rows: U^T w = 0
+    ng, ni = 3 * s.n_o, s.n_i
+    np.testing.assert_allclose(K[ng + ni:, :ng + ni] @ w[:ng + ni], 0.0, atol=1e-10)
+    # field gradient at the orientations follows the data (nugget -> 0); not
+    # exactly, because the 1e-5 regulariser of h_u h_v / r^2 makes the
+    # gradient block differ slightly from the kernel's exact second derivative
+    _, G = kriging.evaluate(s, w, s.dip_positions, gradient=True)
+    np.testing.assert_allclose(G / s.gi_res, s.dip_gradients, atol=2e-3)
+
+
+def test_horizontal_inputs_give_linear_field():
+    """Perfectly horizontal surfaces + vertical orientations: the co-kriging
+    solution is the linear drift alone, so Z = gi_res * z exactly."""
+    g = load_golden("horizontal_inputs.json")
+    s = oracle_series_from_golden(g)
+    K, b = kriging.build_system(s)
+    w = kriging.solve(K, b)
+    rng = np.random.default_rng(0)
+    x = rng.uniform(-0.3, 0.3, (50, 3))
+    np.testing.assert_allclose(kriging.evaluate(s, w, x), s.gi_res * x[:, 2], atol=1e-12)
+
+
+@pytest.mark.parametrize("kernel", [covariance.CUBIC, covariance.EXPONENTIAL])
+def test_covariance_derivatives_match_finite_differences(kernel):
+    C, d1r, d2, d3r = covariance.functions(kernel)
+    a = 1.3
+    r = np.linspace(0.05, 1.25, 40)
+    h = 1e-6
+    dC = (C(r + h, a) - C(r - h, a)) / (2 * h)
+    np.testing.assert_allclose(d1r(r, a) * r, dC, rtol=1e-6, atol=1e-8)
+    d2n = (C(r + h, a) - 2 * C(r, a) + C(r - h, a)) / h**2
+    np.testing.assert_allclose(d2(r, a), d2n, rtol=1e-3, atol=1e-3)
+    g = lambda rr: d1r(rr, a)
+    d3n = (g(r + h) - g(r - h)) / (2 * h) / r
+    np.testing.assert_allclose(d3r(r, a), d3n, rtol=1e-5, atol=1e-6)
+
+
+def test_gradient_of_field_matches_finite_differences():
+    g = load_golden("anticline_corners.json")
+    s = oracle_series_from_golden(g)
+    w = kriging.solve(*kriging.build_system(s))
+    rng = np.random.default_rng(3)
+    x = rng.uniform(-0.25, 0.25, (20, 3))
+    _, G = kriging.evaluate(s, w, x, gradient=True)
+    h = 1e-6
+    for u in range(3):
+        e = np.zeros(3); e[u] = h
+        fd = (kriging.evaluate(s, w, x + e) - kriging.evaluate(s, w, x - e)) / (2 * h)
+        np.testing.assert_allclose(G[:, u], fd, rtol=1e-5, atol=1e-7)
+
+
+def test_segmentation_step_and_order():
+    iso = np.array([0.1, 0.3, -0.2])           # unsorted on purpose
+    uv = np.array([1.0, 2.0, 3.0, 4.0])
+    Z = np.array([0.5, 0.2, 0.0, -0.5, 0.3 + 1e-3, 0.1 - 1e-3])
+    v, ids = segmentation.segment(Z, iso, uv, 5e6)
+    np.testing.assert_array_equal(ids, [1, 2, 3, 4, 1, 3])
+    np.testing.assert_array_equal(segmentation.hard_ids(Z, iso, uv), ids)
+
+
+def test_series_masks_squeezed():
+    f0 = np.array([1.0, -1.0, -1.0])
+    f1 = np.array([0.0, 1.0, -1.0])
+    f2 = np.array([0.0, 0.0, 0.0])
+    m = segmentation.series_masks([f0, f1, f2], [np.array([0.5, 0.0]), np.array([0.2]), np.array([0.0])],
+                                  [segmentation.ERODE, segmentation.ERODE, segmentation.BASEMENT])
+    np.testing.assert_array_equal(m, [[1, 0, 0], [0, 1, 0], [0, 0, 1]])
+    assert m.sum(0).tolist() == [1, 1, 1]
+
+
+def test_octree_children_order_and_marking():
+    c, d = octree.base_centres([0, 1, 0, 1, 0, 1], [2, 2, 2])
+    assert c.shape == (8, 3)
+    np.testing.assert_allclose(c[1], [0.25, 0.25, 0.75])   # z fastest
+    ch = octree.children(c[:1], d)
+    np.testing.assert_allclose(ch[0], [0.125, 0.125, 0.125])
+    np.testing.assert_allclose(ch[7], [0.375, 0.375, 0.375])
+    ids = np.array([[1] * 8, [1, 1, 1, 1, 1, 1, 1, 2]]).ravel()
+    np.testing.assert_array_equal(octree.mark(ids), [False, True])
