@@ -14,7 +14,7 @@ GK_OK, GK_ERR_ARG, GK_ERR_SIZE, GK_ERR_CUDA = 0, 1, 2, 3
 GK_ERR_SINGULAR, GK_ERR_NOT_CONVERGED, GK_ERR_NONFINITE, GK_ERR_TIMEOUT = 4, 5, 6, 7
 STATUS_NAMES = {0: "OK", 1: "ERR_ARG", 2: "ERR_SIZE", 3: "ERR_CUDA", 4: "ERR_SINGULAR",
                 5: "ERR_NOT_CONVERGED", 6: "ERR_NONFINITE", 7: "ERR_TIMEOUT"}
-GK_F64, GK_F32 = 0, 1
+GK_F64, GK_F32, GK_FF = 0, 1, 2
 GK_KERNEL_CUBIC, GK_KERNEL_EXPONENTIAL = 0, 1
 GK_MAX_SURFACES = 32
 

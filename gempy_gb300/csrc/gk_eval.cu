@@ -15,13 +15,14 @@
 #include <cstring>
 
 #include "gk_common.cuh"
+#include "gk_ff.cuh"
 
 namespace gk {
 
 static size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct ModelLayout {
-    size_t ori64, sp64, mu64, ori32, sp32, alpha, total;
+    size_t ori64, sp64, mu64, ori32, sp32, alpha, ffori, ffsp, ffmeta, total;
 };
 
 static ModelLayout model_layout(int n_ori, int n_sp) {
@@ -33,6 +34,9 @@ static ModelLayout model_layout(int n_ori, int n_sp) {
     L.ori32 = o; o += al256((size_t)n_ori * 8 * sizeof(float));
     L.sp32 = o;  o += al256((size_t)n_sp * 4 * sizeof(float));
     L.alpha = o; o += al256((size_t)n_sp * sizeof(double));
+    L.ffori = o; o += al256((size_t)n_ori * 16 * sizeof(float));
+    L.ffsp = o;  o += al256((size_t)n_sp * 8 * sizeof(float));
+    L.ffmeta = o; o += al256(8 * sizeof(double));
     L.total = o;
     return L;
 }
@@ -71,6 +75,59 @@ __global__ void pack_kernel(int n_ori, int n_sp, int n_iface, int n_drift, doubl
         for (int k = 0; k < 4; ++k) { sp64[4 * i + k] = rec[k]; sp32[4 * i + k] = (float)rec[k]; }
     }
     if (i < 16) mu64[i] = i < n_drift ? gi * w[3 * n_ori + n_iface + i] : 0.0;
+}
+
+// Float-float records.  Coordinates are scaled by 1/range (so s = |x-p|/a
+// directly) and split into hi + lo with hi a multiple of the quantum q: every
+// hi with |hi| <= 2^23 q differs from another such hi by an exactly
+// representable float, so x_hi - p_hi is exact.  q = 2^(ceil(log2 max|u|) + 4
+// - 23) leaves room for evaluation points 16x farther out than any datum;
+// points beyond that take an exact two-sum path.  meta[0] = q,
+// meta[1] = max|u| bits (as float), meta[2] = 1/range.
+__global__ void ff_maxabs_kernel(const double* __restrict__ a, int n3, double inv_a, unsigned int* maxbits) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float v = i < n3 ? (float)fabs(a[i] * inv_a) : 0.f;
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(maxbits, __float_as_uint(v));
+}
+
+__device__ __forceinline__ double ff_quantum(const unsigned int* maxbits) {
+    float m = __uint_as_float(*maxbits);
+    if (!(m > 1e-30f)) m = 1.f;
+    int e = (int)ceil(log2((double)m));
+    return ldexp(1.0, e + 4 - 23);
+}
+
+__device__ __forceinline__ void ff_split(double u, double q, float& h, float& l) {
+    double hi = rint(u / q) * q;
+    h = (float)hi;
+    l = (float)(u - hi);
+}
+
+__global__ void pack_ff_kernel(int n_ori, int n_sp, double inv_a, double w_scale_ori, double w_scale_sp,
+                               const double* __restrict__ dip, const double* __restrict__ sp,
+                               const double* __restrict__ w, const double* __restrict__ alpha,
+                               const unsigned int* maxbits, float* ffori, float* ffsp, double* meta) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const double q = ff_quantum(maxbits);
+    if (i == 0) { meta[0] = q; meta[2] = inv_a; }
+    if (i < n_ori) {
+        float* r = ffori + 16 * i;
+        for (int k = 0; k < 3; ++k) ff_split(dip[3 * i + k] * inv_a, q, r[2 * k], r[2 * k + 1]);
+        for (int k = 0; k < 3; ++k) {
+            ff v = ff_from_double(w_scale_ori * w[k * n_ori + i]);
+            r[6 + 2 * k] = v.h;
+            r[7 + 2 * k] = v.l;
+        }
+        for (int k = 12; k < 16; ++k) r[k] = 0.f;
+    }
+    if (i < n_sp) {
+        float* r = ffsp + 8 * i;
+        for (int k = 0; k < 3; ++k) ff_split(sp[3 * i + k] * inv_a, q, r[2 * k], r[2 * k + 1]);
+        ff v = ff_from_double(w_scale_sp * alpha[i]);
+        r[6] = v.h;
+        r[7] = v.l;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -333,6 +390,214 @@ drain:
 }
 
 // ---------------------------------------------------------------------------
+// float-float evaluation (cubic kernel, field only)
+// ---------------------------------------------------------------------------
+struct PointFF {
+    float h[3], l[3];
+    bool exact;
+};
+
+__device__ __forceinline__ void ff_point(const double* xd, double inv_a, double q, PointFF& P) {
+    const double lim = ldexp(q, 23);
+    P.exact = true;
+    for (int k = 0; k < 3; ++k) {
+        double u = xd[k] * inv_a;
+        double hi = rint(u / q) * q;
+        P.h[k] = (float)hi;
+        P.l[k] = (float)(u - hi);
+        if (fabs(hi) > lim) P.exact = false;
+    }
+}
+
+// r^2 of d = x - p as float-float; d_k = dh_k + dl_k with dh_k exact when the
+// split is exact, else recovered with a two-sum.
+__device__ __forceinline__ ff ff_dist2(const PointFF& X, const float* ph, const float* pl, float* dh, float* dl) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        if (X.exact) {
+            dh[k] = X.h[k] - ph[k];
+            dl[k] = X.l[k] - pl[k];
+        } else {
+            ff t = two_sum(X.h[k], -ph[k]);
+            dh[k] = t.h;
+            dl[k] = t.l + (X.l[k] - pl[k]);
+        }
+    }
+    ff a0 = two_prod(dh[0], dh[0]), a1 = two_prod(dh[1], dh[1]), a2 = two_prod(dh[2], dh[2]);
+    ff s1 = two_sum(a0.h, a1.h);
+    ff s2 = two_sum(s1.h, a2.h);
+    float low = s1.l + s2.l + a0.l + a1.l + a2.l;
+    low = __fmaf_rn(dl[0], 2.f * dh[0] + dl[0], low);
+    low = __fmaf_rn(dl[1], 2.f * dh[1] + dl[1], low);
+    low = __fmaf_rn(dl[2], 2.f * dh[2] + dl[2], low);
+    return fast_two_sum(s2.h, low);
+}
+
+template <int PPT>
+__global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const double* __restrict__ meta) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ int s_fail;
+    const int tid = threadIdx.x;
+    unsigned char* stage[2] = {smem, smem + P.stage_bytes};
+    if (tid == 0) {
+        mbar_init(&mbar[0], 1);
+        mbar_init(&mbar[1], 1);
+        mbar_fence_init();
+        s_fail = 0;
+    }
+    __syncthreads();
+    const double q = meta[0], inv_a = meta[2];
+    const int64_t chunk_pts = (int64_t)blockDim.x * PPT;
+    const int64_t n_chunks = (P.n + chunk_pts - 1) / chunk_pts;
+    const int n_tiles = P.tiles_ori + P.tiles_sp;
+    const int64_t my_chunks = n_chunks > blockIdx.x ? (n_chunks - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    const int64_t n_items = my_chunks * n_tiles;
+
+    auto issue = [&](int64_t item) {
+        if (tid != 0) return;
+        int s = (int)(item & 1);
+        int t = (int)(item % n_tiles);
+        const void* src;
+        uint32_t bytes;
+        if (t < P.tiles_ori) {
+            int r0 = t * P.rec_ori;
+            int nr = min(P.rec_ori, P.n_ori - r0);
+            bytes = (uint32_t)(nr * 16 * sizeof(float));
+            src = (const float*)P.ori + (size_t)r0 * 16;
+        } else {
+            int r0 = (t - P.tiles_ori) * P.rec_sp;
+            int nr = min(P.rec_sp, P.n_sp - r0);
+            bytes = (uint32_t)(nr * 8 * sizeof(float));
+            src = (const float*)P.sp + (size_t)r0 * 8;
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(&mbar[s], bytes);
+        bulk_g2s(stage[s], src, bytes, &mbar[s]);
+    };
+    if (n_items > 0) issue(0);
+    if (n_items > 1) issue(1);
+
+    int64_t item = 0;
+    for (int64_t lc = 0; lc < my_chunks; ++lc) {
+        const int64_t chunk = blockIdx.x + lc * gridDim.x;
+        double xd[PPT][3];
+        int64_t pid[PPT];
+        PointFF X[PPT];
+#pragma unroll
+        for (int p = 0; p < PPT; ++p) {
+            pid[p] = chunk * chunk_pts + tid + (int64_t)p * blockDim.x;
+            int64_t qd = pid[p] < P.n ? pid[p] : P.n - 1;
+            if (P.kind == 0) {
+                int64_t nyz = (int64_t)P.dims[1] * P.dims[2];
+                int64_t ix = qd / nyz, rem = qd - ix * nyz;
+                int64_t iy = rem / P.dims[2], iz = rem - iy * P.dims[2];
+                xd[p][0] = P.origin[0] + (double)ix * P.spacing[0];
+                xd[p][1] = P.origin[1] + (double)iy * P.spacing[1];
+                xd[p][2] = P.origin[2] + (double)iz * P.spacing[2];
+            } else {
+                xd[p][0] = P.xyz[3 * qd];
+                xd[p][1] = P.xyz[3 * qd + 1];
+                xd[p][2] = P.xyz[3 * qd + 2];
+            }
+            ff_point(xd[p], inv_a, q, X[p]);
+        }
+        double Z[PPT];
+#pragma unroll
+        for (int p = 0; p < PPT; ++p) Z[p] = 0.0;
+
+        for (int t = 0; t < n_tiles; ++t, ++item) {
+            const int s = (int)(item & 1);
+            const uint32_t parity = (uint32_t)((item >> 1) & 1);
+            if (!mbar_wait(&mbar[s], parity)) {
+                if (P.err) atomicExch(P.err, GK_ERR_TIMEOUT);
+                s_fail = 1;
+            }
+            __syncthreads();
+            if (s_fail) goto drain;
+            {
+                ff acc[PPT];
+#pragma unroll
+                for (int p = 0; p < PPT; ++p) acc[p] = {0.f, 0.f};
+                const float* rec = reinterpret_cast<const float*>(stage[s]);
+                if (t < P.tiles_ori) {
+                    const int nr = min(P.rec_ori, P.n_ori - t * P.rec_ori);
+                    for (int qr = 0; qr < nr; ++qr) {
+                        const float* R = rec + 16 * qr;
+                        const float ph[3] = {R[0], R[2], R[4]}, pl[3] = {R[1], R[3], R[5]};
+                        const ff wx = {R[6], R[7]}, wy = {R[8], R[9]}, wz = {R[10], R[11]};
+#pragma unroll
+                        for (int p = 0; p < PPT; ++p) {
+                            float dh[3], dl[3];
+                            ff r2 = ff_dist2(X[p], ph, pl, dh, dl);
+                            if (r2.h >= 1.f) continue;  // beyond the range: C'/r = 0
+                            ff sr = ff_sqrt(r2);
+                            ff k = ff_add_f(ff_mul_f(r2, 5.25f), -17.5f);
+                            k = ff_horner(r2, k, 26.25f);
+                            k = ff_horner(sr, k, -14.f);
+                            // h = x_o - x = -(dh + dl)
+                            ff wh = ff_mul(wx, ff{-dh[0], -dl[0]});
+                            wh = ff_add(wh, ff_mul(wy, ff{-dh[1], -dl[1]}));
+                            wh = ff_add(wh, ff_mul(wz, ff{-dh[2], -dl[2]}));
+                            acc[p] = ff_add(acc[p], ff_mul(k, wh));
+                        }
+                    }
+                } else {
+                    const int nr = min(P.rec_sp, P.n_sp - (t - P.tiles_ori) * P.rec_sp);
+                    for (int qr = 0; qr < nr; ++qr) {
+                        const float* R = rec + 8 * qr;
+                        const float ph[3] = {R[0], R[2], R[4]}, pl[3] = {R[1], R[3], R[5]};
+                        const ff W = {R[6], R[7]};
+#pragma unroll
+                        for (int p = 0; p < PPT; ++p) {
+                            float dh[3], dl[3];
+                            ff r2 = ff_dist2(X[p], ph, pl, dh, dl);
+                            if (r2.h >= 1.f) continue;  // beyond the range: C = 0
+                            ff sr = ff_sqrt(r2);
+                            ff c = ff_add_f(ff_mul_f(r2, 0.75f), -3.5f);
+                            c = ff_horner(r2, c, 8.75f);
+                            c = ff_horner(sr, c, -7.f);
+                            c = ff_horner(r2, c, 1.f);
+                            acc[p] = ff_add(acc[p], ff_mul(c, W));
+                        }
+                    }
+                }
+#pragma unroll
+                for (int p = 0; p < PPT; ++p) Z[p] += ff_to_double(acc[p]);
+            }
+            __syncthreads();
+            if (item + 2 < n_items) issue(item + 2);
+        }
+#pragma unroll
+        for (int p = 0; p < PPT; ++p) {
+            if (pid[p] >= P.n) continue;
+            const double* mu = P.mu;
+            const double Xx = xd[p][0], Yy = xd[p][1], Zc = xd[p][2];
+            double z = Z[p];
+            if (P.n_drift >= 3) z += mu[0] * Xx + mu[1] * Yy + mu[2] * Zc;
+            if (P.n_drift >= 9)
+                z += mu[3] * Xx * Xx + mu[4] * Yy * Yy + mu[5] * Zc * Zc + mu[6] * Xx * Yy + mu[7] * Xx * Zc +
+                     mu[8] * Yy * Zc;
+            if (P.field) P.field[pid[p]] = z;
+            if (P.has_seg) {
+                double v = P.seg.unit_values[0];
+                for (int k = 0; k < P.seg.n_surf; ++k)
+                    v += (P.seg.unit_values[k + 1] - P.seg.unit_values[k]) *
+                         (double)sigm<float>(P.seg.slope * (P.seg.isovalues[k] - z));
+                if (P.values) P.values[pid[p]] = v;
+                if (P.ids) P.ids[pid[p]] = (int32_t)rint(v);
+            }
+        }
+    }
+    return;
+drain:
+    if (tid == 0) {
+        for (int64_t it = item; it < n_items && it < item + 2; ++it) mbar_wait(&mbar[it & 1], (uint32_t)((it >> 1) & 1));
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
 // series combination
 // ---------------------------------------------------------------------------
 struct CombineParams {
@@ -404,6 +669,25 @@ extern "C" gk_status gk_eval_prepare(const gk_system* s, const double* w, void* 
         alpha, (double*)(m + L.ori64), (double*)(m + L.sp64), (double*)(m + L.mu64), (float*)(m + L.ori32),
         (float*)(m + L.sp32));
     GK_LAUNCH_CHECK();
+    // float-float records (coordinates / range, weights with every constant folded in)
+    double* meta = (double*)(m + L.ffmeta);
+    unsigned int* maxbits = (unsigned int*)(meta + 1);
+    GK_CUDA_TRY(cudaMemsetAsync(meta, 0, 8 * sizeof(double), cs));
+    const double inv_a = 1.0 / s->range;
+    if (s->n_ori > 0) {
+        ff_maxabs_kernel<<<(unsigned)((3 * s->n_ori + 255) / 256), 256, 0, cs>>>(s->dip_positions, 3 * s->n_ori,
+                                                                                inv_a, maxbits);
+        GK_LAUNCH_CHECK();
+    }
+    if (s->n_sp > 0) {
+        ff_maxabs_kernel<<<(unsigned)((3 * s->n_sp + 255) / 256), 256, 0, cs>>>(s->sp_coords, 3 * s->n_sp, inv_a,
+                                                                               maxbits);
+        GK_LAUNCH_CHECK();
+    }
+    pack_ff_kernel<<<(unsigned)((nmax + 255) / 256), 256, 0, cs>>>(
+        s->n_ori, s->n_sp, inv_a, s->c_o * s->gi_res * inv_a, s->c_o * s->gi_res, s->dip_positions, s->sp_coords, w,
+        alpha, maxbits, (float*)(m + L.ffori), (float*)(m + L.ffsp), meta);
+    GK_LAUNCH_CHECK();
     return GK_OK;
 }
 
@@ -431,6 +715,30 @@ static gk_status launch_eval(EvalParams& P, cudaStream_t st) {
         P.tiles_sp = 0;
     }
     k<<<(unsigned)grid, 256, smem, st>>>(P);
+    GK_LAUNCH_CHECK();
+    return GK_OK;
+}
+
+template <int PPT>
+static gk_status launch_eval_ff(EvalParams& P, const double* meta, cudaStream_t st) {
+    const int stage_bytes = 32 * 1024;
+    P.stage_bytes = stage_bytes;
+    P.rec_ori = stage_bytes / (16 * sizeof(float));
+    P.rec_sp = stage_bytes / (8 * sizeof(float));
+    P.tiles_ori = (P.n_ori + P.rec_ori - 1) / P.rec_ori;
+    P.tiles_sp = (P.n_sp + P.rec_sp - 1) / P.rec_sp;
+    auto k = eval_ff_kernel<PPT>;
+    size_t smem = 2 * (size_t)stage_bytes;
+    GK_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int occ = 0;
+    GK_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, 256, smem));
+    if (occ < 1) occ = 1;
+    const int64_t chunk_pts = 256LL * PPT;
+    int64_t n_chunks = (P.n + chunk_pts - 1) / chunk_pts;
+    int64_t grid = (int64_t)occ * device_sm_count();
+    if (grid > n_chunks) grid = n_chunks;
+    if (grid < 1) grid = 1;
+    k<<<(unsigned)grid, 256, smem, st>>>(P, meta);
     GK_LAUNCH_CHECK();
     return GK_OK;
 }
@@ -488,6 +796,12 @@ extern "C" gk_status gk_eval(const gk_system* s, const void* model, const gk_poi
         P.ori = m + L.ori32;
         P.sp = m + L.sp32;
         return grad ? launch_eval<float, 2, true>(P, cs) : launch_eval<float, 2, false>(P, cs);
+    }
+    if (prec == GK_FF) {
+        if (grad != nullptr || s->kernel != GK_KERNEL_CUBIC) return GK_ERR_ARG;
+        P.ori = m + L.ffori;
+        P.sp = m + L.ffsp;
+        return launch_eval_ff<2>(P, (const double*)(m + L.ffmeta), cs);
     }
     return GK_ERR_ARG;
 }

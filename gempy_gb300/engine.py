@@ -26,7 +26,7 @@ import numpy as np
 import torch
 
 from . import kernels as K
-from ._lib import GK_F32, GK_F64
+from ._lib import GK_F32, GK_F64, GK_FF
 from .data import (CombinedOutput, ExportedFields, InterpOutput, OctreeLevel, RawArraysSolution, RootOutput,
                    Solutions, StackRelationType)
 
@@ -34,13 +34,18 @@ from .data import (CombinedOutput, ExportedFields, InterpOutput, OctreeLevel, Ra
 @dataclass
 class EngineConfig:
     """Mirror of the reference's ``GemPyEngineConfig`` (``gempy_engine_config.py:9-14``):
-    ``dtype`` "float64" selects the plain FP64 form, "float32" the mixed form
-    (FP32 LU + FP64 refinement, FP32 evaluation with FP64 isovalues)."""
+    ``dtype`` "float64" selects the plain FP64 form; "float32" the mixed form:
+    FP32 LU preconditioning an FP64 FGMRES solve, and the field evaluated in
+    float-float on the FP32 pipe (cubic kernel; other kernels evaluate in
+    FP64) with FP64 isovalues.  ``eval_precision`` overrides the evaluation
+    arithmetic ("f64", "ff" or "f32"; "f32" is only accurate to ~1e-7 times
+    the cancellation factor sum|w_j k_j| / |Z| of the kriging sum)."""
     dtype: str = "float64"
     use_gpu: bool = True
     keep_on_device: bool = False
     solver_tol: float = 1e-12
-    solver_max_iter: int = 30
+    solver_max_iter: int = 60
+    eval_precision: Optional[str] = None
     timings: bool = False
 
 
@@ -96,7 +101,11 @@ class _Evaluator:
     def run(self, pts: K.Points, gradient=False):
         fields, values, grads = [], [], []
         for s in self.series:
-            f, g, v, _ = K.evaluate(s.dev, s.model, pts, self.prec, seg=s.seg, gradient=gradient)
+            f, _, v, _ = K.evaluate(s.dev, s.model, pts, self.prec, seg=s.seg)
+            g = None
+            if gradient:   # gradients in FP64 (the float-float kernel computes the field only)
+                _, g, _, _ = K.evaluate(s.dev, s.model, pts, GK_F64 if self.prec == GK_FF else self.prec,
+                                        gradient=True, want_field=False)
             fields.append(f)
             values.append(v)
             grads.append(g)
@@ -137,7 +146,12 @@ def compute_model(interpolation_input, options, data_descriptor, geophysics_inpu
         raise RuntimeError("gempy_gb300.compute_model needs a CUDA device (there is no CPU fallback)")
     device = torch.device("cuda")
     mixed = str(cfg.dtype) in ("float32", "mixed")
-    prec = GK_F32 if mixed else GK_F64
+    ko = options.kernel_options
+    cubic = K.kernel_id(ko.kernel_function) == 0
+    if cfg.eval_precision is not None:
+        prec = {"f64": GK_F64, "ff": GK_FF, "f32": GK_F32}[cfg.eval_precision]
+    else:
+        prec = GK_FF if (mixed and cubic) else GK_F64
     t0 = time.perf_counter()
     timings = {}
 

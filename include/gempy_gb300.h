@@ -47,7 +47,10 @@ typedef enum gk_status {
     GK_ERR_TIMEOUT = 7        /* an inter-CTA wait gave up (device info)      */
 } gk_status;
 
-typedef enum gk_prec { GK_F64 = 0, GK_F32 = 1 } gk_prec;
+/* Arithmetic of a kernel.  GK_FF is float-float ("double-single"): values
+ * carried as pairs of FP32 words (~48-bit significand) on the FP32 pipe,
+ * available for the field evaluation of the cubic kernel. */
+typedef enum gk_prec { GK_F64 = 0, GK_F32 = 1, GK_FF = 2 } gk_prec;
 
 /* ``kernel_function`` of the reference's KernelOptions (serialized options
  * JSON, ``...serialization.approved.txt:135``). */
@@ -169,9 +172,9 @@ gk_status gk_eval_prepare(const gk_system* sys, const double* w, void* model,
 
 /* Scalar field (times gi_res, the engine's reported scale), optional
  * gradient (n x 3), optional soft segmentation values and ids.  ``prec``
- * selects FP64 or FP32 arithmetic; outputs are always FP64 for field/values
- * and int32 for ids.  Any output pointer may be NULL.  ``seg`` may be NULL
- * (no segmentation). */
+ * selects FP64, FP32 or float-float arithmetic (GK_FF: field only, cubic
+ * kernel); outputs are always FP64 for field/values and int32 for ids.  Any
+ * output pointer may be NULL.  ``seg`` may be NULL (no segmentation). */
 gk_status gk_eval(const gk_system* sys, const void* model,
                   const gk_points* pts, gk_prec prec,
                   const gk_segment* seg, double* field, double* grad,
