@@ -83,6 +83,7 @@ SIGNATURES = [
                                         c_double_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_size_t, ctypes.c_void_p]),
     ("gk_version", ctypes.c_char_p, []),
+    ("gk_launch_count", ctypes.c_uint64, []),
 ]
 
 _lib = None

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "../../include/gempy_gb300.h"
 
 #define GK_CUDA_TRY(expr)                                   \
@@ -13,8 +15,15 @@
         if (_e != cudaSuccess) return GK_ERR_CUDA;          \
     } while (0)
 
+// Process-wide count of kernels this library has launched (telemetry).
+inline std::atomic<unsigned long long>& gk_launch_counter() {
+    static std::atomic<unsigned long long> c{0};
+    return c;
+}
+
 #define GK_LAUNCH_CHECK()                                   \
     do {                                                    \
+        gk_launch_counter().fetch_add(1, std::memory_order_relaxed); \
         if (cudaPeekAtLastError() != cudaSuccess) {         \
             (void)cudaGetLastError();                       \
             return GK_ERR_CUDA;                             \

@@ -495,6 +495,7 @@ static gk_status lu_factor(int64_t n, T* A, int64_t lda, int32_t* ipiv, void* wo
         int chunk = pl.chunk;
         void* args[] = {&A, &lda, &n, &kk, &kb, &chunk, &W, &ipiv, &info};
         GK_CUDA_TRY(cudaLaunchCooperativeKernel((void*)pk, dim3(pl.P), dim3(256), args, pl.smem, st));
+        gk_launch_counter().fetch_add(1, std::memory_order_relaxed);
         int64_t others = n - kb;
         if (others > 0) {
             laswp_kernel<T><<<(unsigned)((others + 255) / 256), 256, 0, st>>>(A, lda, n, k, kb, ipiv);

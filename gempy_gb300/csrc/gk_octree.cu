@@ -157,3 +157,5 @@ extern "C" gk_status gk_octree_refine(int64_t n, const double* centres, const in
 }
 
 extern "C" const char* gk_version(void) { return "gempy_gb300 0.1.0 (sm_103a)"; }
+
+extern "C" uint64_t gk_launch_count(void) { return gk_launch_counter().load(std::memory_order_relaxed); }

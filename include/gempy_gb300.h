@@ -213,6 +213,9 @@ gk_status gk_octree_refine(int64_t n, const double* centres,
 /* Library version string (HOST). */
 const char* gk_version(void);
 
+/* Number of kernels this library has launched in the process (telemetry). */
+uint64_t gk_launch_count(void);
+
 #ifdef __cplusplus
 }
 #endif
