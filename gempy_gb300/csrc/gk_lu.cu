@@ -19,6 +19,7 @@
 // Solves use a permutation gather and two blocked triangular solves whose
 // CTAs claim block rows in order and wait (bounded) on earlier blocks' flags.
 #include <cooperative_groups.h>
+#include <cstdlib>
 
 #include "gk_common.cuh"
 
@@ -173,6 +174,148 @@ __global__ void __launch_bounds__(256) panel_kernel(T* __restrict__ A, int64_t l
 }
 
 // ----------------------------------------------------------------------------
+// Panel factorization inside one thread-block cluster (<= 16 CTAs).  Each CTA
+// holds a contiguous chunk of the panel rows in shared memory.  Per column,
+// every CTA posts its pivot candidate (value, row, and a copy of the whole
+// panel row) and the owner of the diagonal row posts that row in its own
+// shared-memory mailbox; after one hardware cluster barrier all CTAs read the
+// mailboxes through distributed shared memory, agree on the pivot (largest
+// magnitude, lowest row on ties), swap locally and apply the rank-1 update.
+// Mailboxes alternate by column parity, so a mailbox is only rewritten after
+// the next barrier, when every reader is done with it.
+// ----------------------------------------------------------------------------
+namespace cg = cooperative_groups;
+
+template <typename T, int NB>
+__global__ void __launch_bounds__(256) panel_cluster_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k,
+                                                            int kb, int chunk, int32_t* __restrict__ ipiv,
+                                                            gk_info* info) {
+    extern __shared__ unsigned char smem_raw[];
+    T* S = reinterpret_cast<T*>(smem_raw);  // chunk x NB
+    __shared__ T mb_val[2];
+    __shared__ int mb_row[2];
+    __shared__ T mb_rowdata[2][NB];
+    __shared__ T mb_cur[2][NB];
+    __shared__ T red_v[8];
+    __shared__ int red_r[8];
+    __shared__ T piv_row[NB];
+    __shared__ T cur_row[NB];
+    __shared__ int s_p, s_win;
+
+    cg::cluster_group cl = cg::this_cluster();
+    const int C = (int)cl.num_blocks();
+    const int me = (int)cl.block_rank();
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int64_t m = n - k;
+    const int64_t rb = (int64_t)me * chunk;
+    const int64_t re = min(m, rb + chunk);
+    const int nr = (int)max((int64_t)0, re - rb);
+
+    for (int idx = tid; idx < nr * NB; idx += blockDim.x) {
+        int r = idx / NB, c = idx % NB;
+        S[idx] = c < kb ? A[(k + rb + r) * lda + k + c] : (T)0;
+    }
+    __syncthreads();
+
+    for (int j = 0; j < kb; ++j) {
+        const int buf = j & 1;
+        const int64_t dj = j;
+        if (dj >= rb && dj < re)
+            for (int c = tid; c < NB; c += blockDim.x) mb_cur[buf][c] = S[(dj - rb) * NB + c];
+        T best = (T)-1;
+        int brow = -1;
+        for (int r = tid; r < nr; r += blockDim.x) {
+            int64_t gr = rb + r;
+            if (gr < dj) continue;
+            T v = gabs(S[r * NB + j]);
+            if (v > best) { best = v; brow = (int)gr; }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            T ov = __shfl_down_sync(0xffffffffu, best, o);
+            int orow = __shfl_down_sync(0xffffffffu, brow, o);
+            if (orow >= 0 && (ov > best || (ov == best && (brow < 0 || orow < brow)))) { best = ov; brow = orow; }
+        }
+        if (lane == 0) { red_v[wid] = best; red_r[wid] = brow; }
+        __syncthreads();
+        if (tid == 0) {
+            for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+                if (red_r[w] >= 0 && (red_v[w] > best || (red_v[w] == best && (brow < 0 || red_r[w] < brow)))) {
+                    best = red_v[w]; brow = red_r[w];
+                }
+            mb_val[buf] = best;
+            mb_row[buf] = brow;
+            red_r[0] = brow;
+        }
+        __syncthreads();
+        brow = red_r[0];
+        if (brow >= 0)
+            for (int c = tid; c < NB; c += blockDim.x) mb_rowdata[buf][c] = S[(brow - rb) * NB + c];
+        cl.sync();
+
+        if (tid < 32) {
+            T bv = (T)-1;
+            int br = -1, bw = -1;
+            for (int c = tid; c < C; c += 32) {
+                T v = *cl.map_shared_rank(&mb_val[buf], c);
+                int r = *cl.map_shared_rank(&mb_row[buf], c);
+                if (r >= 0 && (v > bv || (v == bv && (br < 0 || r < br)))) { bv = v; br = r; bw = c; }
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                T ov = __shfl_down_sync(0xffffffffu, bv, o);
+                int orr = __shfl_down_sync(0xffffffffu, br, o);
+                int ow = __shfl_down_sync(0xffffffffu, bw, o);
+                if (orr >= 0 && (ov > bv || (ov == bv && (br < 0 || orr < br)))) { bv = ov; br = orr; bw = ow; }
+            }
+            if (tid == 0) { s_p = br; s_win = bw; }
+        }
+        __syncthreads();
+        const int p = s_p, win = s_win;
+        if (p < 0) {
+            if (tid == 0) report(info, GK_ERR_NONFINITE, (int)(k + j));
+            if (me == 0 && tid == 0) ipiv[k + j] = (int32_t)(k + j);
+            continue;
+        }
+        const T* wrow = cl.map_shared_rank(&mb_rowdata[buf][0], win);
+        const int owner_dj = (int)(dj / chunk);
+        const T* crow = cl.map_shared_rank(&mb_cur[buf][0], owner_dj);
+        for (int c = tid; c < NB; c += blockDim.x) {
+            piv_row[c] = wrow[c];
+            cur_row[c] = crow[c];
+        }
+        __syncthreads();
+        if (me == 0 && tid == 0) ipiv[k + j] = (int32_t)(k + p);
+        if (p != dj) {
+            if (p >= rb && p < re)
+                for (int c = tid; c < NB; c += blockDim.x) S[(p - rb) * NB + c] = cur_row[c];
+            if (dj >= rb && dj < re)
+                for (int c = tid; c < NB; c += blockDim.x) S[(dj - rb) * NB + c] = piv_row[c];
+        }
+        __syncthreads();
+        const T pv = piv_row[j];
+        if (pv == (T)0) {
+            if (me == 0 && tid == 0) report(info, GK_ERR_SINGULAR, (int)(k + j));
+            continue;
+        }
+        const T inv = (T)1 / pv;
+        for (int r = wid; r < nr; r += (int)(blockDim.x >> 5)) {
+            int64_t gr = rb + r;
+            if (gr <= dj) continue;
+            T l = S[r * NB + j] * inv;
+            for (int c = j + 1 + lane; c < kb; c += 32) S[r * NB + c] -= l * piv_row[c];
+            __syncwarp();
+            if (lane == 0) S[r * NB + j] = l;
+        }
+        __syncthreads();
+    }
+    // keep every CTA's mailboxes alive until all remote reads are done
+    cl.sync();
+    for (int idx = tid; idx < nr * NB; idx += blockDim.x) {
+        int r = idx / NB, c = idx % NB;
+        if (c < kb) A[(k + rb + r) * lda + k + c] = S[idx];
+    }
+}
+
+// ----------------------------------------------------------------------------
 // Row interchanges on the columns outside the panel
 // ----------------------------------------------------------------------------
 template <typename T>
@@ -280,6 +423,111 @@ __global__ void __launch_bounds__(256) gemm_update_kernel(T* __restrict__ A, int
     }
 }
 
+// FP32 trailing update for aligned panels (offsets and lda multiples of 4):
+// 128 x 128 tile per CTA, 16 x 16 threads each owning an 8 x 8 block split in
+// four 4 x 4 quadrants, float4 shared-memory reads (A stored k-major), the
+// next k-slice prefetched into registers while the current one is consumed.
+__global__ void __launch_bounds__(256, 2) sgemm_update_kernel(float* __restrict__ A, int64_t lda, int64_t n, int64_t k,
+                                                           int kb) {
+    constexpr int BM = 128, BN = 128, BK = 16;
+    __shared__ __align__(16) float As[2][BK][BM];
+    __shared__ __align__(16) float Bs[2][BK][BN];
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    const int64_t off = k + kb;
+    const int64_t i0 = off + (int64_t)blockIdx.y * BM, j0 = off + (int64_t)blockIdx.x * BN;
+    float acc[8][8];
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) acc[a][b] = 0.f;
+    // loader mapping
+    const int la_row = tid >> 1, la_k = (tid & 1) * 8;          // A: 128 rows x 16 k
+    const int lb_row = tid >> 5, lb_col = (tid & 31) * 4;        // B: rows lb_row, lb_row + 8
+    float4 ra[2], rb[2];
+    auto gload = [&](int p0) {
+        const int64_t gi = i0 + la_row;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int kk = p0 + la_k + 4 * h;
+            if (gi < n && kk + 3 < kb) {
+                ra[h] = *reinterpret_cast<const float4*>(A + gi * lda + k + kk);
+            } else {
+                float t[4];
+                for (int e = 0; e < 4; ++e) t[e] = (gi < n && kk + e < kb) ? A[gi * lda + k + kk + e] : 0.f;
+                ra[h] = make_float4(t[0], t[1], t[2], t[3]);
+            }
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int kk = p0 + lb_row + 8 * h;
+            const int64_t gj = j0 + lb_col;
+            if (kk < kb && gj + 3 < n) {
+                rb[h] = *reinterpret_cast<const float4*>(A + (k + kk) * lda + gj);
+            } else {
+                float t[4];
+                for (int e = 0; e < 4; ++e) t[e] = (kk < kb && gj + e < n) ? A[(k + kk) * lda + gj + e] : 0.f;
+                rb[h] = make_float4(t[0], t[1], t[2], t[3]);
+            }
+        }
+    };
+    auto sstore = [&](int buf) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            As[buf][la_k + 4 * h + 0][la_row] = ra[h].x;
+            As[buf][la_k + 4 * h + 1][la_row] = ra[h].y;
+            As[buf][la_k + 4 * h + 2][la_row] = ra[h].z;
+            As[buf][la_k + 4 * h + 3][la_row] = ra[h].w;
+            *reinterpret_cast<float4*>(&Bs[buf][lb_row + 8 * h][lb_col]) = rb[h];
+        }
+    };
+    const int nk = (kb + BK - 1) / BK;
+    gload(0);
+    sstore(0);
+    __syncthreads();
+    for (int it = 0; it < nk; ++it) {
+        const int buf = it & 1;
+        if (it + 1 < nk) gload((it + 1) * BK);
+#pragma unroll
+        for (int p = 0; p < BK; ++p) {
+            const float4 a0 = *reinterpret_cast<const float4*>(&As[buf][p][ty * 4]);
+            const float4 a1 = *reinterpret_cast<const float4*>(&As[buf][p][64 + ty * 4]);
+            const float4 b0 = *reinterpret_cast<const float4*>(&Bs[buf][p][tx * 4]);
+            const float4 b1 = *reinterpret_cast<const float4*>(&Bs[buf][p][64 + tx * 4]);
+            const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+            for (int a = 0; a < 8; ++a)
+#pragma unroll
+                for (int b = 0; b < 8; ++b) acc[a][b] = __fmaf_rn(av[a], bv[b], acc[a][b]);
+        }
+        if (it + 1 < nk) {
+            sstore(buf ^ 1);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int a = 0; a < 8; ++a) {
+        const int64_t gi = i0 + (a < 4 ? ty * 4 + a : 64 + ty * 4 + a - 4);
+        if (gi >= n) continue;
+#pragma unroll
+        for (int hb = 0; hb < 2; ++hb) {
+            const int64_t gj = j0 + hb * 64 + tx * 4;
+            float* c = A + gi * lda + gj;
+            if (gj + 3 < n) {
+                float4 v = *reinterpret_cast<float4*>(c);
+                v.x -= acc[a][4 * hb + 0];
+                v.y -= acc[a][4 * hb + 1];
+                v.z -= acc[a][4 * hb + 2];
+                v.w -= acc[a][4 * hb + 3];
+                *reinterpret_cast<float4*>(c) = v;
+            } else {
+                for (int e = 0; e < 4; ++e)
+                    if (gj + e < n) c[e] -= acc[a][4 * hb + e];
+            }
+        }
+    }
+}
+
 // ----------------------------------------------------------------------------
 // Solves
 // ----------------------------------------------------------------------------
@@ -316,13 +564,18 @@ __global__ void gather_kernel(const Tin* __restrict__ src, const int32_t* __rest
 
 // Blocked triangular solve, in place on x.  lower: unit-diagonal L, forward;
 // upper: U with diagonal, backward.  CTAs claim block rows in solve order
-// through ``counter``; block b waits for every earlier block's flag.
+// through ``counter``; block b waits (bounded) for every earlier block's flag.
+// The diagonal block is staged in shared memory while the CTA waits, and is
+// solved by one warp holding two rows per lane, the solved unknown broadcast
+// by register shuffle (no dependent global loads on the critical path).
 template <typename T, int BS>
 __global__ void __launch_bounds__(256) trsv_kernel(const T* __restrict__ A, int64_t lda, int64_t n, T* x,
                                                    int lower, int* counter, int* flags, gk_info* info) {
+    static_assert(BS == 64, "two rows per lane");
     __shared__ int s_blk;
-    __shared__ T part[8][BS];
+    __shared__ T part[BS];
     __shared__ T xs[BS];
+    __shared__ T D[BS][BS + 1];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int nblk = (int)((n + BS - 1) / BS);
     if (tid == 0) s_blk = atomicAdd(counter, 1);
@@ -332,6 +585,11 @@ __global__ void __launch_bounds__(256) trsv_kernel(const T* __restrict__ A, int6
     const int blk = lower ? ord : nblk - 1 - ord;
     const int64_t r0 = (int64_t)blk * BS;
     const int rows = (int)min((int64_t)BS, n - r0);
+    // stage the diagonal block
+    for (int idx = tid; idx < BS * BS; idx += blockDim.x) {
+        int r = idx / BS, c = idx % BS;
+        D[r][c] = (r < rows && c < rows) ? A[(r0 + r) * lda + r0 + c] : (T)0;
+    }
     // accumulate contributions of solved blocks: warp w handles rows w, w+8, ...
     T acc[BS / 8];
 #pragma unroll
@@ -344,7 +602,7 @@ __global__ void __launch_bounds__(256) trsv_kernel(const T* __restrict__ A, int6
                 int f;
                 asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(f) : "l"(flags + dep) : "memory");
                 if (f) break;
-                if (++spins > kSpinLimit) { report(info, GK_ERR_TIMEOUT, dep); f = -1; break; }
+                if (++spins > kSpinLimit) { report(info, GK_ERR_TIMEOUT, dep); break; }
             }
         }
         __syncthreads();
@@ -364,41 +622,40 @@ __global__ void __launch_bounds__(256) trsv_kernel(const T* __restrict__ A, int6
         }
         __syncthreads();
     }
-    // reduce per row
 #pragma unroll
     for (int q = 0; q < BS / 8; ++q) {
         T s = acc[q];
         for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-        if (lane == 0) part[0][wid + 8 * q] = s;
+        if (lane == 0) part[wid + 8 * q] = s;
     }
     __syncthreads();
-    // diagonal block solve by warp 0
     if (wid == 0) {
-        // load rhs minus contributions
-        for (int r = lane; r < rows; r += 32) xs[r] = x[r0 + r] - part[0][r];
-        __syncwarp();
+        // lane l holds rows l (v0) and l + 32 (v1)
+        T v0 = lane < rows ? x[r0 + lane] - part[lane] : (T)0;
+        T v1 = lane + 32 < rows ? x[r0 + lane + 32] - part[lane + 32] : (T)0;
         if (lower) {
-            for (int r = 0; r < rows; ++r) {
-                T s = (T)0;
-                for (int c = lane; c < r; c += 32) s += A[(r0 + r) * lda + r0 + c] * xs[c];
-                for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-                if (lane == 0) xs[r] -= s;
-                __syncwarp();
+            for (int c = 0; c < rows; ++c) {
+                T xc = __shfl_sync(0xffffffffu, c < 32 ? v0 : v1, c & 31);
+                if (lane > c) v0 -= D[lane][c] * xc;
+                if (lane + 32 > c) v1 -= D[lane + 32][c] * xc;
             }
         } else {
-            for (int r = rows - 1; r >= 0; --r) {
-                T s = (T)0;
-                for (int c = r + 1 + lane; c < rows; c += 32) s += A[(r0 + r) * lda + r0 + c] * xs[c];
-                for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-                if (lane == 0) {
-                    T d = A[(r0 + r) * lda + r0 + r];
-                    if (d == (T)0) { report(info, GK_ERR_SINGULAR, (int)(r0 + r)); xs[r] = (T)0; }
-                    else xs[r] = (xs[r] - s) / d;
+            for (int c = rows - 1; c >= 0; --c) {
+                T mine = c < 32 ? v0 : v1;
+                T d = D[c][c];
+                T xc = (T)0;
+                if (lane == (c & 31)) {
+                    if (d == (T)0) { report(info, GK_ERR_SINGULAR, (int)(r0 + c)); xc = (T)0; }
+                    else xc = mine / d;
+                    if (c < 32) v0 = xc; else v1 = xc;
                 }
-                __syncwarp();
+                xc = __shfl_sync(0xffffffffu, xc, c & 31);
+                if (lane < c) v0 -= D[lane][c] * xc;
+                if (lane + 32 < c) v1 -= D[lane + 32][c] * xc;
             }
         }
-        for (int r = lane; r < rows; r += 32) x[r0 + r] = xs[r];
+        if (lane < rows) x[r0 + lane] = v0;
+        if (lane + 32 < rows) x[r0 + lane + 32] = v1;
         __threadfence();
         __syncwarp();
         if (lane == 0) {
@@ -470,6 +727,41 @@ static size_t lu_ws_bytes(int64_t n) {
            align256((size_t)((n + 63) / 64 + 2) * sizeof(int)) + align256((size_t)n * sizeof(T));
 }
 
+// Largest cluster size (<= 16) the device can schedule with ~200 KB of shared
+// memory per CTA; 0 when clusters are unavailable.
+template <typename T, int NB>
+static int cluster_capacity() {
+    static int cached = -1;
+    if (cached >= 0) return cached;
+    cached = 0;
+    auto ck = panel_cluster_kernel<T, NB>;
+    if (cudaFuncSetAttribute(ck, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) != cudaSuccess ||
+        cudaFuncSetAttribute(ck, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return cached;
+    }
+    for (int C = 16; C >= 2; C /= 2) {
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = C;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.gridDim = dim3(C);
+        cfg.blockDim = dim3(256);
+        cfg.dynamicSmemBytes = 200 * 1024;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int nc = 0;
+        if (cudaOccupancyMaxActiveClusters(&nc, ck, &cfg) == cudaSuccess && nc > 0) {
+            cached = C;
+            return cached;
+        }
+        (void)cudaGetLastError();
+    }
+    return cached;
+}
+
 template <typename T>
 static gk_status lu_factor(int64_t n, T* A, int64_t lda, int32_t* ipiv, void* work, size_t wbytes, gk_info* info,
                            cudaStream_t st) {
@@ -483,8 +775,41 @@ static gk_status lu_factor(int64_t n, T* A, int64_t lda, int32_t* ipiv, void* wo
     if (info) GK_CUDA_TRY(cudaMemsetAsync(info, 0, sizeof(gk_info), st));
     auto pk = panel_kernel<T, NB>;
     GK_CUDA_TRY(cudaFuncSetAttribute(pk, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    auto ck = panel_cluster_kernel<T, NB>;
+    GK_CUDA_TRY(cudaFuncSetAttribute(ck, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    GK_CUDA_TRY(cudaFuncSetAttribute(ck, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    // GK_PANEL_COOPERATIVE=1 selects the grid-barrier panel for every size
+    // (the path large panels take), so both implementations can be tested.
+    const char* force_coop = getenv("GK_PANEL_COOPERATIVE");
+    const int max_cluster = (force_coop && force_coop[0] == '1') ? 0 : cluster_capacity<T, NB>();
     for (int64_t k = 0; k < n; k += NB) {
         int kb = (int)min((int64_t)NB, n - k);
+        if (max_cluster > 0) {
+            const int64_t m = n - k;
+            const int max_rows = (int)((200 * 1024) / (NB * sizeof(T)));
+            int C = (int)((m + 127) / 128);
+            if (C < 1) C = 1;
+            if (C > max_cluster) C = max_cluster;
+            int chunk = (int)((m + C - 1) / C);
+            if (chunk <= max_rows) {
+                cudaLaunchConfig_t cfg = {};
+                cudaLaunchAttribute attr[1];
+                attr[0].id = cudaLaunchAttributeClusterDimension;
+                attr[0].val.clusterDim.x = C;
+                attr[0].val.clusterDim.y = 1;
+                attr[0].val.clusterDim.z = 1;
+                cfg.gridDim = dim3(C);
+                cfg.blockDim = dim3(256);
+                cfg.dynamicSmemBytes = (size_t)chunk * NB * sizeof(T);
+                cfg.stream = st;
+                cfg.attrs = attr;
+                cfg.numAttrs = 1;
+                GK_CUDA_TRY(cudaLaunchKernelEx(&cfg, ck, A, lda, n, (int64_t)k, kb, chunk, ipiv, info));
+                gk_launch_counter().fetch_add(1, std::memory_order_relaxed);
+                goto after_panel;
+            }
+        }
+        {
         PanelPlan<T, NB> pl;
         gk_status s = plan_panel<T, NB>(n - k, sms, pl);
         if (s != GK_OK) return s;
@@ -496,6 +821,8 @@ static gk_status lu_factor(int64_t n, T* A, int64_t lda, int32_t* ipiv, void* wo
         void* args[] = {&A, &lda, &n, &kk, &kb, &chunk, &W, &ipiv, &info};
         GK_CUDA_TRY(cudaLaunchCooperativeKernel((void*)pk, dim3(pl.P), dim3(256), args, pl.smem, st));
         gk_launch_counter().fetch_add(1, std::memory_order_relaxed);
+        }
+    after_panel:
         int64_t others = n - kb;
         if (others > 0) {
             laswp_kernel<T><<<(unsigned)((others + 255) / 256), 256, 0, st>>>(A, lda, n, k, kb, ipiv);
@@ -508,7 +835,12 @@ static gk_status lu_factor(int64_t n, T* A, int64_t lda, int32_t* ipiv, void* wo
             constexpr int BM = sizeof(T) == 8 ? 64 : 128;
             constexpr int BN = BM;
             dim3 grid((unsigned)((rest + BN - 1) / BN), (unsigned)((rest + BM - 1) / BM));
-            gemm_update_kernel<T, BM, BN, 16><<<grid, 256, 0, st>>>(A, lda, n, k, kb);
+            if (sizeof(T) == 4 && ((k + kb) % 4) == 0 && (lda % 4) == 0 &&
+                ((uintptr_t)A % 16) == 0) {
+                sgemm_update_kernel<<<grid, 256, 0, st>>>((float*)A, lda, n, k, kb);
+            } else {
+                gemm_update_kernel<T, BM, BN, 16><<<grid, 256, 0, st>>>(A, lda, n, k, kb);
+            }
             GK_LAUNCH_CHECK();
         }
     }

@@ -77,10 +77,13 @@ def test_build_f32_matches_oracle():
     assert np.abs(Kg[:, :N].double().cpu().numpy() - Kr).max() <= 2e-6 * np.abs(Kr).max()
 
 
+@pytest.mark.parametrize("panel", ["cluster", "cooperative"])
 @pytest.mark.parametrize("n", [1, 2, 5, 31, 32, 33, 63, 64, 65, 127, 200, 513, 1100])
 @pytest.mark.parametrize("prec", ["f64", "f32"])
-def test_lu_factor_solve_random(n, prec):
+def test_lu_factor_solve_random(n, prec, panel, monkeypatch):
     from gempy_gb300 import kernels as K
+    if panel == "cooperative":
+        monkeypatch.setenv("GK_PANEL_COOPERATIVE", "1")
     rng = np.random.default_rng(n)
     A = rng.normal(size=(n, n)) + n ** 0.5 * np.eye(n) * rng.choice([-1, 1], n)
     b = rng.normal(size=n)
