@@ -32,6 +32,26 @@ template <> struct LuCfg<float>  { static constexpr int NB = 64; };
 template <typename T>
 __device__ __forceinline__ T gabs(T x) { return x < (T)0 ? -x : x; }
 
+// Rank-1 update of the panel rows below the diagonal, parallel over
+// (row, column): first the multipliers l_r = S[r][j] / pivot are written in
+// place, then every thread updates elements S[r][c], c > j.
+template <typename T, int NB>
+__device__ __forceinline__ void rank1_update(T* S, int nr, int64_t rb, int64_t dj, int j, int kb, T inv,
+                                             const T* piv_row) {
+    const int r_first = (int)max((int64_t)0, dj + 1 - rb);
+    for (int r = r_first + (int)threadIdx.x; r < nr; r += blockDim.x) S[r * NB + j] *= inv;
+    __syncthreads();
+    const int w = kb - j - 1;
+    if (w > 0) {
+        const int cnt = (nr - r_first) * w;
+        for (int idx = threadIdx.x; idx < cnt; idx += blockDim.x) {
+            const int r = r_first + idx / w, c = j + 1 + idx % w;
+            S[r * NB + c] -= S[r * NB + j] * piv_row[c];
+        }
+    }
+    __syncthreads();
+}
+
 // ----------------------------------------------------------------------------
 // Panel factorization
 // ----------------------------------------------------------------------------
@@ -155,16 +175,7 @@ __global__ void __launch_bounds__(256) panel_kernel(T* __restrict__ A, int64_t l
             continue;
         }
         const T inv = (T)1 / pv;
-        // rank-1 update of rows below the diagonal: one warp per row
-        for (int r = wid; r < nr; r += (int)(blockDim.x >> 5)) {
-            int64_t gr = rb + r;
-            if (gr <= dj) continue;
-            T l = S[r * NB + j] * inv;
-            for (int c = j + 1 + lane; c < kb; c += 32) S[r * NB + c] -= l * piv_row[c];
-            __syncwarp();
-            if (lane == 0) S[r * NB + j] = l;
-        }
-        __syncthreads();
+        rank1_update<T, NB>(S, nr, rb, dj, j, kb, inv, piv_row);
     }
     // write back
     for (int idx = tid; idx < nr * NB; idx += blockDim.x) {
@@ -297,15 +308,7 @@ __global__ void __launch_bounds__(256) panel_cluster_kernel(T* __restrict__ A, i
             continue;
         }
         const T inv = (T)1 / pv;
-        for (int r = wid; r < nr; r += (int)(blockDim.x >> 5)) {
-            int64_t gr = rb + r;
-            if (gr <= dj) continue;
-            T l = S[r * NB + j] * inv;
-            for (int c = j + 1 + lane; c < kb; c += 32) S[r * NB + c] -= l * piv_row[c];
-            __syncwarp();
-            if (lane == 0) S[r * NB + j] = l;
-        }
-        __syncthreads();
+        rank1_update<T, NB>(S, nr, rb, dj, j, kb, inv, piv_row);
     }
     // keep every CTA's mailboxes alive until all remote reads are done
     cl.sync();
@@ -562,106 +565,141 @@ __global__ void gather_kernel(const Tin* __restrict__ src, const int32_t* __rest
     if (i < n) dst[i] = (Tout)src[perm[i]];
 }
 
-// Blocked triangular solve, in place on x.  lower: unit-diagonal L, forward;
-// upper: U with diagonal, backward.  CTAs claim block rows in solve order
-// through ``counter``; block b waits (bounded) for every earlier block's flag.
-// The diagonal block is staged in shared memory while the CTA waits, and is
-// solved by one warp holding two rows per lane, the solved unknown broadcast
-// by register shuffle (no dependent global loads on the critical path).
-template <typename T, int BS>
+// Inverses of the 128 x 128 diagonal blocks of L (unit lower) and U (upper),
+// computed once per factorization: CTA b, thread c solves for column c of the
+// inverse, all threads stepping through the rows together (L/U entries are
+// warp-broadcast loads, the partial inverse lives in shared memory).
+constexpr int kTB = 128;  // triangular-solve block
+
+template <typename T>
+__global__ void __launch_bounds__(kTB) tri_inv_kernel(const T* __restrict__ A, int64_t lda, int64_t n,
+                                                      T* __restrict__ invL, T* __restrict__ invU, gk_info* info) {
+    extern __shared__ unsigned char smem_raw[];
+    T* Y = reinterpret_cast<T*>(smem_raw);  // kTB x kTB, Y[r * kTB + c]
+    const int b = blockIdx.x, c = threadIdx.x;
+    const int64_t r0 = (int64_t)b * kTB;
+    const int rows = (int)min((int64_t)kTB, n - r0);
+    auto at = [&](int r, int k) -> T { return A[(r0 + r) * lda + r0 + k]; };
+    // L^-1 (unit diagonal; padding rows act as identity)
+    for (int r = 0; r < kTB; ++r) {
+        T v = (r == c) ? (T)1 : (T)0;
+        if (r > c && r < rows) {
+            for (int k = c; k < r; ++k) v -= at(r, k) * Y[k * kTB + c];
+        }
+        Y[r * kTB + c] = v;
+        __syncwarp();
+        __syncthreads();
+    }
+    for (int r = 0; r < kTB; ++r) invL[((int64_t)b * kTB + r) * kTB + c] = Y[r * kTB + c];
+    __syncthreads();
+    // U^-1
+    for (int r = kTB - 1; r >= 0; --r) {
+        T v = (r == c) ? (T)1 : (T)0;
+        if (r < rows) {
+            if (r < c) {
+                for (int k = r + 1; k <= c && k < rows; ++k) v -= at(r, k) * Y[k * kTB + c];
+            }
+            T d = at(r, r);
+            if (d == (T)0) {
+                if (c == 0) report(info, GK_ERR_SINGULAR, (int)(r0 + r));
+                v = (T)0;
+            } else {
+                v = (r <= c) ? v / d : (T)0;
+            }
+        }
+        Y[r * kTB + c] = v;
+        __syncthreads();
+    }
+    for (int r = 0; r < kTB; ++r) invU[((int64_t)b * kTB + r) * kTB + c] = Y[r * kTB + c];
+}
+
+// Blocked triangular solve, in place on x.  lower: L (unit), forward; upper:
+// U, backward.  CTAs claim 128-row blocks in solve order through ``counter``;
+// each warp owns 16 rows and, per earlier block, polls that block's flag
+// (bounded) and accumulates its 16 x 128 product without block-wide barriers.
+// The block's unknowns are then x_b = inv(D_b) (x_b - acc), a warp-parallel
+// matvec with the precomputed inverse of the diagonal block.
+template <typename T>
 __global__ void __launch_bounds__(256) trsv_kernel(const T* __restrict__ A, int64_t lda, int64_t n, T* x,
-                                                   int lower, int* counter, int* flags, gk_info* info) {
-    static_assert(BS == 64, "two rows per lane");
+                                                   const T* __restrict__ dinv, int lower, int* counter, int* flags,
+                                                   gk_info* info) {
     __shared__ int s_blk;
-    __shared__ T part[BS];
-    __shared__ T xs[BS];
-    __shared__ T D[BS][BS + 1];
+    __shared__ T rhs[kTB];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    const int nblk = (int)((n + BS - 1) / BS);
+    const int nblk = (int)((n + kTB - 1) / kTB);
     if (tid == 0) s_blk = atomicAdd(counter, 1);
     __syncthreads();
     const int ord = s_blk;
     if (ord >= nblk) return;
     const int blk = lower ? ord : nblk - 1 - ord;
-    const int64_t r0 = (int64_t)blk * BS;
-    const int rows = (int)min((int64_t)BS, n - r0);
-    // stage the diagonal block
-    for (int idx = tid; idx < BS * BS; idx += blockDim.x) {
-        int r = idx / BS, c = idx % BS;
-        D[r][c] = (r < rows && c < rows) ? A[(r0 + r) * lda + r0 + c] : (T)0;
-    }
-    // accumulate contributions of solved blocks: warp w handles rows w, w+8, ...
-    T acc[BS / 8];
+    const int64_t r0 = (int64_t)blk * kTB;
+    const int rows = (int)min((int64_t)kTB, n - r0);
+    T acc[16];
 #pragma unroll
-    for (int q = 0; q < BS / 8; ++q) acc[q] = (T)0;
+    for (int q = 0; q < 16; ++q) acc[q] = (T)0;
     for (int o = 0; o < ord; ++o) {
         const int dep = lower ? o : nblk - 1 - o;
-        if (tid == 0) {
-            long long spins = 0;
-            while (true) {
-                int f;
-                asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(f) : "l"(flags + dep) : "memory");
-                if (f) break;
-                if (++spins > kSpinLimit) { report(info, GK_ERR_TIMEOUT, dep); break; }
-            }
+        long long spins = 0;
+        while (true) {
+            int f;
+            asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(f) : "l"(flags + dep) : "memory");
+            if (f) break;
+            if (++spins > kSpinLimit) { if (lane == 0) report(info, GK_ERR_TIMEOUT, dep); break; }
         }
-        __syncthreads();
-        const int64_t c0 = (int64_t)dep * BS;
-        const int cols = (int)min((int64_t)BS, n - c0);
-        if (tid < cols) xs[tid] = ((volatile T*)x)[c0 + tid];
-        __syncthreads();
+        const int64_t c0 = (int64_t)dep * kTB;
+        const int cols = (int)min((int64_t)kTB, n - c0);
+        T xv[4];
 #pragma unroll
-        for (int q = 0; q < BS / 8; ++q) {
-            int r = wid + 8 * q;
+        for (int e = 0; e < 4; ++e) {
+            const int c = lane + 32 * e;
+            xv[e] = c < cols ? ((volatile T*)x)[c0 + c] : (T)0;
+        }
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            const int r = wid * 16 + q;
             if (r < rows) {
                 const T* row = A + (r0 + r) * lda + c0;
-                T s = (T)0;
-                for (int c = lane; c < cols; c += 32) s += row[c] * xs[c];
-                acc[q] += s;
+                T sacc = (T)0;
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const int c = lane + 32 * e;
+                    if (c < cols) sacc += row[c] * xv[e];
+                }
+                acc[q] += sacc;
             }
         }
-        __syncthreads();
     }
 #pragma unroll
-    for (int q = 0; q < BS / 8; ++q) {
-        T s = acc[q];
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-        if (lane == 0) part[wid + 8 * q] = s;
+    for (int q = 0; q < 16; ++q) {
+        T sv = acc[q];
+        for (int o = 16; o > 0; o >>= 1) sv += __shfl_down_sync(0xffffffffu, sv, o);
+        const int r = wid * 16 + q;
+        if (lane == 0) rhs[r] = r < rows ? x[r0 + r] - sv : (T)0;
     }
     __syncthreads();
-    if (wid == 0) {
-        // lane l holds rows l (v0) and l + 32 (v1)
-        T v0 = lane < rows ? x[r0 + lane] - part[lane] : (T)0;
-        T v1 = lane + 32 < rows ? x[r0 + lane + 32] - part[lane + 32] : (T)0;
-        if (lower) {
-            for (int c = 0; c < rows; ++c) {
-                T xc = __shfl_sync(0xffffffffu, c < 32 ? v0 : v1, c & 31);
-                if (lane > c) v0 -= D[lane][c] * xc;
-                if (lane + 32 > c) v1 -= D[lane + 32][c] * xc;
-            }
-        } else {
-            for (int c = rows - 1; c >= 0; --c) {
-                T mine = c < 32 ? v0 : v1;
-                T d = D[c][c];
-                T xc = (T)0;
-                if (lane == (c & 31)) {
-                    if (d == (T)0) { report(info, GK_ERR_SINGULAR, (int)(r0 + c)); xc = (T)0; }
-                    else xc = mine / d;
-                    if (c < 32) v0 = xc; else v1 = xc;
-                }
-                xc = __shfl_sync(0xffffffffu, xc, c & 31);
-                if (lane < c) v0 -= D[lane][c] * xc;
-                if (lane + 32 < c) v1 -= D[lane + 32][c] * xc;
-            }
-        }
-        if (lane < rows) x[r0 + lane] = v0;
-        if (lane + 32 < rows) x[r0 + lane + 32] = v1;
-        __threadfence();
-        __syncwarp();
-        if (lane == 0) {
-            asm volatile("st.release.gpu.global.b32 [%0], %1;" :: "l"(flags + blk), "r"(1) : "memory");
+    // x_b = inv(D_b) rhs
+    const T* Di = dinv + (int64_t)blk * kTB * kTB;
+    T outv[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+        const int r = wid * 16 + q;
+        const T* drow = Di + (int64_t)r * kTB;
+        T sv = (T)0;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) sv += drow[lane + 32 * e] * rhs[lane + 32 * e];
+        for (int o = 16; o > 0; o >>= 1) sv += __shfl_down_sync(0xffffffffu, sv, o);
+        outv[q] = sv;
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            const int r = wid * 16 + q;
+            if (r < rows) x[r0 + r] = outv[q];
         }
     }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) asm volatile("st.release.gpu.global.b32 [%0], %1;" :: "l"(flags + blk), "r"(1) : "memory");
 }
 
 // ----------------------------------------------------------------------------
@@ -719,12 +757,27 @@ static PanelWork<T, NB> panel_ws_carve(void* base, int sms) {
     return w;
 }
 
+// Workspace: [panel exchange][perm (n+1)][flags + counter][tmp vector (n)]
+//            [inverse diagonal blocks of L][... of U]
 template <typename T>
 static size_t lu_ws_bytes(int64_t n) {
     constexpr int NB = LuCfg<T>::NB;
     int sms = device_sm_count();
+    const size_t nblk = (size_t)((n + kTB - 1) / kTB);
     return panel_ws_bytes<T, NB>(sms) + align256((size_t)(n + 1) * sizeof(int32_t)) * 2 +
-           align256((size_t)((n + 63) / 64 + 2) * sizeof(int)) + align256((size_t)n * sizeof(T));
+           align256((size_t)((n + 63) / 64 + 2) * sizeof(int)) + align256((size_t)n * sizeof(T)) +
+           2 * align256(nblk * kTB * kTB * sizeof(T));
+}
+
+template <typename T>
+static T* lu_ws_dinv(void* work, int64_t n, int upper) {
+    constexpr int NB = LuCfg<T>::NB;
+    int sms = device_sm_count();
+    const size_t nblk = (size_t)((n + kTB - 1) / kTB);
+    char* p = (char*)work + panel_ws_bytes<T, NB>(sms) + align256((size_t)(n + 1) * sizeof(int32_t)) * 2 +
+              align256((size_t)((n + 63) / 64 + 2) * sizeof(int)) + align256((size_t)n * sizeof(T));
+    if (upper) p += align256(nblk * kTB * kTB * sizeof(T));
+    return (T*)p;
 }
 
 // Largest cluster size (<= 16) the device can schedule with ~200 KB of shared
@@ -850,6 +903,12 @@ static gk_status lu_factor(int64_t n, T* A, int64_t lda, int32_t* ipiv, void* wo
     GK_CUDA_TRY(cudaFuncSetAttribute(perm_from_ipiv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPermSmem * 4));
     perm_from_ipiv_kernel<<<1, 256, psmem, st>>>(ipiv, n, perm);
     GK_LAUNCH_CHECK();
+    // inverses of the diagonal blocks for the triangular solves
+    const size_t ysmem = (size_t)kTB * kTB * sizeof(T);
+    GK_CUDA_TRY(cudaFuncSetAttribute(tri_inv_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ysmem));
+    tri_inv_kernel<T><<<(unsigned)((n + kTB - 1) / kTB), kTB, ysmem, st>>>(A, lda, n, lu_ws_dinv<T>(work, n, 0),
+                                                                          lu_ws_dinv<T>(work, n, 1), info);
+    GK_LAUNCH_CHECK();
     return GK_OK;
 }
 
@@ -860,7 +919,7 @@ template <typename T>
 static gk_status lu_solve(int64_t n, const T* LU, int64_t lda, const int32_t* ipiv, T* b, void* work, size_t wbytes,
                           gk_info* info, cudaStream_t st) {
     constexpr int NB = LuCfg<T>::NB;
-    constexpr int BS = 64;
+    constexpr int BS = kTB;
     if (n <= 0 || LU == nullptr || ipiv == nullptr || b == nullptr) return GK_ERR_ARG;
     if (work == nullptr || wbytes < lu_ws_bytes<T>(n)) return GK_ERR_SIZE;
     int sms = device_sm_count();
@@ -876,7 +935,8 @@ static gk_status lu_solve(int64_t n, const T* LU, int64_t lda, const int32_t* ip
         GK_CUDA_TRY(cudaMemsetAsync(flags, 0, (nblk + 1) * sizeof(int), st));
         // one CTA per block row; CTAs claim rows in solve order, so a CTA only
         // ever waits on rows claimed by CTAs that are already running
-        trsv_kernel<T, BS><<<nblk, 256, 0, st>>>(LU, lda, n, tmp, pass == 0 ? 1 : 0, counter, flags, info);
+        trsv_kernel<T><<<nblk, 256, 0, st>>>(LU, lda, n, tmp, lu_ws_dinv<T>(work, n, pass), pass == 0 ? 1 : 0,
+                                             counter, flags, info);
         GK_LAUNCH_CHECK();
     }
     GK_CUDA_TRY(cudaMemcpyAsync(b, tmp, n * sizeof(T), cudaMemcpyDeviceToDevice, st));
