@@ -397,6 +397,21 @@ struct PointFF {
     bool exact;
 };
 
+__device__ __forceinline__ void point_coords(const EvalParams& P, int64_t q, double* xd) {
+    if (P.kind == 0) {
+        const int64_t nyz = (int64_t)P.dims[1] * P.dims[2];
+        const int64_t ix = q / nyz, rem = q - ix * nyz;
+        const int64_t iy = rem / P.dims[2], iz = rem - iy * P.dims[2];
+        xd[0] = P.origin[0] + (double)ix * P.spacing[0];
+        xd[1] = P.origin[1] + (double)iy * P.spacing[1];
+        xd[2] = P.origin[2] + (double)iz * P.spacing[2];
+    } else {
+        xd[0] = P.xyz[3 * q];
+        xd[1] = P.xyz[3 * q + 1];
+        xd[2] = P.xyz[3 * q + 2];
+    }
+}
+
 __device__ __forceinline__ void ff_point(const double* xd, double inv_a, double q, PointFF& P) {
     const double lim = ldexp(q, 23);
     P.exact = true;
@@ -481,26 +496,13 @@ __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const 
     int64_t item = 0;
     for (int64_t lc = 0; lc < my_chunks; ++lc) {
         const int64_t chunk = blockIdx.x + lc * gridDim.x;
-        double xd[PPT][3];
-        int64_t pid[PPT];
         PointFF X[PPT];
 #pragma unroll
         for (int p = 0; p < PPT; ++p) {
-            pid[p] = chunk * chunk_pts + tid + (int64_t)p * blockDim.x;
-            int64_t qd = pid[p] < P.n ? pid[p] : P.n - 1;
-            if (P.kind == 0) {
-                int64_t nyz = (int64_t)P.dims[1] * P.dims[2];
-                int64_t ix = qd / nyz, rem = qd - ix * nyz;
-                int64_t iy = rem / P.dims[2], iz = rem - iy * P.dims[2];
-                xd[p][0] = P.origin[0] + (double)ix * P.spacing[0];
-                xd[p][1] = P.origin[1] + (double)iy * P.spacing[1];
-                xd[p][2] = P.origin[2] + (double)iz * P.spacing[2];
-            } else {
-                xd[p][0] = P.xyz[3 * qd];
-                xd[p][1] = P.xyz[3 * qd + 1];
-                xd[p][2] = P.xyz[3 * qd + 2];
-            }
-            ff_point(xd[p], inv_a, q, X[p]);
+            const int64_t pidp = chunk * chunk_pts + tid + (int64_t)p * blockDim.x;
+            double xd[3];
+            point_coords(P, pidp < P.n ? pidp : P.n - 1, xd);
+            ff_point(xd, inv_a, q, X[p]);
         }
         double Z[PPT];
 #pragma unroll
@@ -523,9 +525,10 @@ __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const 
                 if (t < P.tiles_ori) {
                     const int nr = min(P.rec_ori, P.n_ori - t * P.rec_ori);
                     for (int qr = 0; qr < nr; ++qr) {
-                        const float* R = rec + 16 * qr;
-                        const float ph[3] = {R[0], R[2], R[4]}, pl[3] = {R[1], R[3], R[5]};
-                        const ff wx = {R[6], R[7]}, wy = {R[8], R[9]}, wz = {R[10], R[11]};
+                        const float4* R4 = reinterpret_cast<const float4*>(rec + 16 * qr);
+                        const float4 a0 = R4[0], a1 = R4[1], a2 = R4[2];
+                        const float ph[3] = {a0.x, a0.z, a1.x}, pl[3] = {a0.y, a0.w, a1.y};
+                        const ff wx = {a1.z, a1.w}, wy = {a2.x, a2.y}, wz = {a2.z, a2.w};
 #pragma unroll
                         for (int p = 0; p < PPT; ++p) {
                             float dh[3], dl[3];
@@ -545,9 +548,10 @@ __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const 
                 } else {
                     const int nr = min(P.rec_sp, P.n_sp - (t - P.tiles_ori) * P.rec_sp);
                     for (int qr = 0; qr < nr; ++qr) {
-                        const float* R = rec + 8 * qr;
-                        const float ph[3] = {R[0], R[2], R[4]}, pl[3] = {R[1], R[3], R[5]};
-                        const ff W = {R[6], R[7]};
+                        const float4* R4 = reinterpret_cast<const float4*>(rec + 8 * qr);
+                        const float4 a0 = R4[0], a1 = R4[1];
+                        const float ph[3] = {a0.x, a0.z, a1.x}, pl[3] = {a0.y, a0.w, a1.y};
+                        const ff W = {a1.z, a1.w};
 #pragma unroll
                         for (int p = 0; p < PPT; ++p) {
                             float dh[3], dl[3];
@@ -570,22 +574,25 @@ __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const 
         }
 #pragma unroll
         for (int p = 0; p < PPT; ++p) {
-            if (pid[p] >= P.n) continue;
+            const int64_t pidp = chunk * chunk_pts + tid + (int64_t)p * blockDim.x;
+            if (pidp >= P.n) continue;
+            double xd[3];
+            point_coords(P, pidp, xd);
             const double* mu = P.mu;
-            const double Xx = xd[p][0], Yy = xd[p][1], Zc = xd[p][2];
+            const double Xx = xd[0], Yy = xd[1], Zc = xd[2];
             double z = Z[p];
             if (P.n_drift >= 3) z += mu[0] * Xx + mu[1] * Yy + mu[2] * Zc;
             if (P.n_drift >= 9)
                 z += mu[3] * Xx * Xx + mu[4] * Yy * Yy + mu[5] * Zc * Zc + mu[6] * Xx * Yy + mu[7] * Xx * Zc +
                      mu[8] * Yy * Zc;
-            if (P.field) P.field[pid[p]] = z;
+            if (P.field) P.field[pidp] = z;
             if (P.has_seg) {
                 double v = P.seg.unit_values[0];
                 for (int k = 0; k < P.seg.n_surf; ++k)
                     v += (P.seg.unit_values[k + 1] - P.seg.unit_values[k]) *
                          (double)sigm<float>(P.seg.slope * (P.seg.isovalues[k] - z));
-                if (P.values) P.values[pid[p]] = v;
-                if (P.ids) P.ids[pid[p]] = (int32_t)rint(v);
+                if (P.values) P.values[pidp] = v;
+                if (P.ids) P.ids[pidp] = (int32_t)rint(v);
             }
         }
     }
@@ -801,7 +808,7 @@ extern "C" gk_status gk_eval(const gk_system* s, const void* model, const gk_poi
         if (grad != nullptr || s->kernel != GK_KERNEL_CUBIC) return GK_ERR_ARG;
         P.ori = m + L.ffori;
         P.sp = m + L.ffsp;
-        return launch_eval_ff<2>(P, (const double*)(m + L.ffmeta), cs);
+        return launch_eval_ff<4>(P, (const double*)(m + L.ffmeta), cs);
     }
     return GK_ERR_ARG;
 }

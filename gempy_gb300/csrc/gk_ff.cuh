@@ -58,8 +58,14 @@ __device__ __forceinline__ ff ff_mul_f(ff a, float c) {
     return fast_two_sum(p.h, e);
 }
 
-// c + x * t, the Horner step
-__device__ __forceinline__ ff ff_horner(ff x, ff t, float c) { return ff_add_f(ff_mul(x, t), c); }
+// c + x * t, the Horner step: the product is left unnormalized, the add
+// renormalizes.
+__device__ __forceinline__ ff ff_horner(ff x, ff t, float c) {
+    ff p = two_prod(x.h, t.h);
+    float e = __fmaf_rn(x.h, t.l, __fmaf_rn(x.l, t.h, p.l));
+    ff s = two_sum(p.h, c);
+    return fast_two_sum(s.h, s.l + e);
+}
 
 // sqrt of a non-negative float-float: one Newton correction of rsqrt-based
 // sqrt (the 2-ulp start squares to ~2^-44 relative error).

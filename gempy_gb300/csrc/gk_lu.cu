@@ -38,15 +38,16 @@ __device__ __forceinline__ T gabs(T x) { return x < (T)0 ? -x : x; }
 template <typename T, int NB>
 __device__ __forceinline__ void rank1_update(T* S, int nr, int64_t rb, int64_t dj, int j, int kb, T inv,
                                              const T* piv_row) {
+    constexpr int SP = NB + 1;  // padded row stride: column accesses hit distinct banks
     const int r_first = (int)max((int64_t)0, dj + 1 - rb);
-    for (int r = r_first + (int)threadIdx.x; r < nr; r += blockDim.x) S[r * NB + j] *= inv;
+    for (int r = r_first + (int)threadIdx.x; r < nr; r += blockDim.x) S[r * SP + j] *= inv;
     __syncthreads();
     const int w = kb - j - 1;
     if (w > 0) {
         const int cnt = (nr - r_first) * w;
         for (int idx = threadIdx.x; idx < cnt; idx += blockDim.x) {
             const int r = r_first + idx / w, c = j + 1 + idx % w;
-            S[r * NB + c] -= S[r * NB + j] * piv_row[c];
+            S[r * SP + c] -= S[r * SP + j] * piv_row[c];
         }
     }
     __syncthreads();
@@ -70,7 +71,7 @@ __global__ void __launch_bounds__(256) panel_kernel(T* __restrict__ A, int64_t l
                                                     int chunk, PanelWork<T, NB> W, int32_t* __restrict__ ipiv,
                                                     gk_info* info) {
     extern __shared__ unsigned char smem_raw[];
-    T* S = reinterpret_cast<T*>(smem_raw);  // chunk x NB
+    T* S = reinterpret_cast<T*>(smem_raw);  // chunk x (NB + 1)
     __shared__ T red_v[8];
     __shared__ int red_r[8];
     __shared__ T piv_row[NB];
@@ -88,7 +89,7 @@ __global__ void __launch_bounds__(256) panel_kernel(T* __restrict__ A, int64_t l
     // load owned rows
     for (int idx = tid; idx < nr * NB; idx += blockDim.x) {
         int r = idx / NB, c = idx % NB;
-        S[idx] = c < kb ? A[(k + rb + r) * lda + k + c] : (T)0;
+        S[r * (NB + 1) + c] = c < kb ? A[(k + rb + r) * lda + k + c] : (T)0;
     }
     __syncthreads();
 
@@ -97,7 +98,7 @@ __global__ void __launch_bounds__(256) panel_kernel(T* __restrict__ A, int64_t l
         const int64_t dj = j;  // diagonal row, panel-local
         // publish the current diagonal row (its owner)
         if (dj >= rb && dj < re) {
-            for (int c = tid; c < NB; c += blockDim.x) W.cur_row[buf * NB + c] = S[(dj - rb) * NB + c];
+            for (int c = tid; c < NB; c += blockDim.x) W.cur_row[buf * NB + c] = S[(dj - rb) * (NB + 1) + c];
         }
         // local argmax of |S[:, j]| over rows >= dj
         T best = (T)-1;
@@ -105,7 +106,7 @@ __global__ void __launch_bounds__(256) panel_kernel(T* __restrict__ A, int64_t l
         for (int r = tid; r < nr; r += blockDim.x) {
             int64_t gr = rb + r;
             if (gr < dj) continue;
-            T v = gabs(S[r * NB + j]);
+            T v = gabs(S[r * (NB + 1) + j]);
             if (v > best || (v == best && brow >= 0 && gr < brow)) { best = v; brow = (int)gr; }
         }
         for (int o = 16; o > 0; o >>= 1) {
@@ -129,7 +130,7 @@ __global__ void __launch_bounds__(256) panel_kernel(T* __restrict__ A, int64_t l
         brow = red_r[0];
         if (brow >= 0) {
             for (int c = tid; c < NB; c += blockDim.x)
-                W.cand_rows[((int64_t)buf * P + blockIdx.x) * NB + c] = S[(brow - rb) * NB + c];
+                W.cand_rows[((int64_t)buf * P + blockIdx.x) * NB + c] = S[(brow - rb) * (NB + 1) + c];
         }
         __threadfence();
         if (!gb.sync(P)) return;
@@ -164,9 +165,9 @@ __global__ void __launch_bounds__(256) panel_kernel(T* __restrict__ A, int64_t l
         // swap rows dj <-> p (panel-local)
         if (p != dj) {
             if (p >= rb && p < re)
-                for (int c = tid; c < NB; c += blockDim.x) S[(p - rb) * NB + c] = __ldcg(&W.cur_row[buf * NB + c]);
+                for (int c = tid; c < NB; c += blockDim.x) S[(p - rb) * (NB + 1) + c] = __ldcg(&W.cur_row[buf * NB + c]);
             if (dj >= rb && dj < re)
-                for (int c = tid; c < NB; c += blockDim.x) S[(dj - rb) * NB + c] = piv_row[c];
+                for (int c = tid; c < NB; c += blockDim.x) S[(dj - rb) * (NB + 1) + c] = piv_row[c];
         }
         __syncthreads();
         const T pv = piv_row[j];
@@ -180,7 +181,7 @@ __global__ void __launch_bounds__(256) panel_kernel(T* __restrict__ A, int64_t l
     // write back
     for (int idx = tid; idx < nr * NB; idx += blockDim.x) {
         int r = idx / NB, c = idx % NB;
-        if (c < kb) A[(k + rb + r) * lda + k + c] = S[idx];
+        if (c < kb) A[(k + rb + r) * lda + k + c] = S[r * (NB + 1) + c];
     }
 }
 
@@ -202,7 +203,7 @@ __global__ void __launch_bounds__(256) panel_cluster_kernel(T* __restrict__ A, i
                                                             int kb, int chunk, int32_t* __restrict__ ipiv,
                                                             gk_info* info) {
     extern __shared__ unsigned char smem_raw[];
-    T* S = reinterpret_cast<T*>(smem_raw);  // chunk x NB
+    T* S = reinterpret_cast<T*>(smem_raw);  // chunk x (NB + 1)
     __shared__ T mb_val[2];
     __shared__ int mb_row[2];
     __shared__ T mb_rowdata[2][NB];
@@ -224,7 +225,7 @@ __global__ void __launch_bounds__(256) panel_cluster_kernel(T* __restrict__ A, i
 
     for (int idx = tid; idx < nr * NB; idx += blockDim.x) {
         int r = idx / NB, c = idx % NB;
-        S[idx] = c < kb ? A[(k + rb + r) * lda + k + c] : (T)0;
+        S[r * (NB + 1) + c] = c < kb ? A[(k + rb + r) * lda + k + c] : (T)0;
     }
     __syncthreads();
 
@@ -232,13 +233,13 @@ __global__ void __launch_bounds__(256) panel_cluster_kernel(T* __restrict__ A, i
         const int buf = j & 1;
         const int64_t dj = j;
         if (dj >= rb && dj < re)
-            for (int c = tid; c < NB; c += blockDim.x) mb_cur[buf][c] = S[(dj - rb) * NB + c];
+            for (int c = tid; c < NB; c += blockDim.x) mb_cur[buf][c] = S[(dj - rb) * (NB + 1) + c];
         T best = (T)-1;
         int brow = -1;
         for (int r = tid; r < nr; r += blockDim.x) {
             int64_t gr = rb + r;
             if (gr < dj) continue;
-            T v = gabs(S[r * NB + j]);
+            T v = gabs(S[r * (NB + 1) + j]);
             if (v > best) { best = v; brow = (int)gr; }
         }
         for (int o = 16; o > 0; o >>= 1) {
@@ -260,7 +261,7 @@ __global__ void __launch_bounds__(256) panel_cluster_kernel(T* __restrict__ A, i
         __syncthreads();
         brow = red_r[0];
         if (brow >= 0)
-            for (int c = tid; c < NB; c += blockDim.x) mb_rowdata[buf][c] = S[(brow - rb) * NB + c];
+            for (int c = tid; c < NB; c += blockDim.x) mb_rowdata[buf][c] = S[(brow - rb) * (NB + 1) + c];
         cl.sync();
 
         if (tid < 32) {
@@ -297,9 +298,9 @@ __global__ void __launch_bounds__(256) panel_cluster_kernel(T* __restrict__ A, i
         if (me == 0 && tid == 0) ipiv[k + j] = (int32_t)(k + p);
         if (p != dj) {
             if (p >= rb && p < re)
-                for (int c = tid; c < NB; c += blockDim.x) S[(p - rb) * NB + c] = cur_row[c];
+                for (int c = tid; c < NB; c += blockDim.x) S[(p - rb) * (NB + 1) + c] = cur_row[c];
             if (dj >= rb && dj < re)
-                for (int c = tid; c < NB; c += blockDim.x) S[(dj - rb) * NB + c] = piv_row[c];
+                for (int c = tid; c < NB; c += blockDim.x) S[(dj - rb) * (NB + 1) + c] = piv_row[c];
         }
         __syncthreads();
         const T pv = piv_row[j];
@@ -314,7 +315,7 @@ __global__ void __launch_bounds__(256) panel_cluster_kernel(T* __restrict__ A, i
     cl.sync();
     for (int idx = tid; idx < nr * NB; idx += blockDim.x) {
         int r = idx / NB, c = idx % NB;
-        if (c < kb) A[(k + rb + r) * lda + k + c] = S[idx];
+        if (c < kb) A[(k + rb + r) * lda + k + c] = S[r * (NB + 1) + c];
     }
 }
 
@@ -569,7 +570,8 @@ __global__ void gather_kernel(const Tin* __restrict__ src, const int32_t* __rest
 // computed once per factorization: CTA b, thread c solves for column c of the
 // inverse, all threads stepping through the rows together (L/U entries are
 // warp-broadcast loads, the partial inverse lives in shared memory).
-constexpr int kTB = 128;  // triangular-solve block
+constexpr int kTB = 128;         // triangular-solve block
+constexpr int kFlagStride = 32;  // one 128-byte line per block flag
 
 template <typename T>
 __global__ void __launch_bounds__(kTB) tri_inv_kernel(const T* __restrict__ A, int64_t lda, int64_t n,
@@ -639,13 +641,18 @@ __global__ void __launch_bounds__(256) trsv_kernel(const T* __restrict__ A, int6
     for (int q = 0; q < 16; ++q) acc[q] = (T)0;
     for (int o = 0; o < ord; ++o) {
         const int dep = lower ? o : nblk - 1 - o;
-        long long spins = 0;
-        while (true) {
-            int f;
-            asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(f) : "l"(flags + dep) : "memory");
-            if (f) break;
-            if (++spins > kSpinLimit) { if (lane == 0) report(info, GK_ERR_TIMEOUT, dep); break; }
+        if (lane == 0) {
+            long long spins = 0;
+            while (true) {
+                int f;
+                asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(f) : "l"(flags + kFlagStride * dep)
+                             : "memory");
+                if (f) break;
+                if (++spins > kSpinLimit) { report(info, GK_ERR_TIMEOUT, dep); break; }
+                if (spins > 8) __nanosleep(32);
+            }
         }
+        __syncwarp();
         const int64_t c0 = (int64_t)dep * kTB;
         const int cols = (int)min((int64_t)kTB, n - c0);
         T xv[4];
@@ -699,7 +706,8 @@ __global__ void __launch_bounds__(256) trsv_kernel(const T* __restrict__ A, int6
     }
     __threadfence();
     __syncthreads();
-    if (tid == 0) asm volatile("st.release.gpu.global.b32 [%0], %1;" :: "l"(flags + blk), "r"(1) : "memory");
+    if (tid == 0)
+        asm volatile("st.release.gpu.global.b32 [%0], %1;" :: "l"(flags + kFlagStride * blk), "r"(1) : "memory");
 }
 
 // ----------------------------------------------------------------------------
@@ -717,7 +725,7 @@ template <typename T, int NB>
 static gk_status plan_panel(int64_t m, int sms, PanelPlan<T, NB>& pl) {
     // enough CTAs that each holds <= max_rows panel rows; at least 32 rows each
     const size_t max_smem = 200 * 1024;
-    const int max_rows = (int)(max_smem / (NB * sizeof(T)));
+    const int max_rows = (int)(max_smem / ((NB + 1) * sizeof(T)));
     int P = (int)((m + 63) / 64);
     if (P < 1) P = 1;
     if (P > sms) P = sms;
@@ -729,7 +737,7 @@ static gk_status plan_panel(int64_t m, int sms, PanelPlan<T, NB>& pl) {
     }
     pl.P = P;
     pl.chunk = chunk;
-    pl.smem = (size_t)chunk * NB * sizeof(T);
+    pl.smem = (size_t)chunk * (NB + 1) * sizeof(T);
     return GK_OK;
 }
 
@@ -765,8 +773,8 @@ static size_t lu_ws_bytes(int64_t n) {
     int sms = device_sm_count();
     const size_t nblk = (size_t)((n + kTB - 1) / kTB);
     return panel_ws_bytes<T, NB>(sms) + align256((size_t)(n + 1) * sizeof(int32_t)) * 2 +
-           align256((size_t)((n + 63) / 64 + 2) * sizeof(int)) + align256((size_t)n * sizeof(T)) +
-           2 * align256(nblk * kTB * kTB * sizeof(T));
+           align256(((size_t)(n + kTB - 1) / kTB + 2) * kFlagStride * sizeof(int)) +
+           align256((size_t)n * sizeof(T)) + 2 * align256(nblk * kTB * kTB * sizeof(T));
 }
 
 template <typename T>
@@ -775,7 +783,8 @@ static T* lu_ws_dinv(void* work, int64_t n, int upper) {
     int sms = device_sm_count();
     const size_t nblk = (size_t)((n + kTB - 1) / kTB);
     char* p = (char*)work + panel_ws_bytes<T, NB>(sms) + align256((size_t)(n + 1) * sizeof(int32_t)) * 2 +
-              align256((size_t)((n + 63) / 64 + 2) * sizeof(int)) + align256((size_t)n * sizeof(T));
+              align256(((size_t)(n + kTB - 1) / kTB + 2) * kFlagStride * sizeof(int)) +
+              align256((size_t)n * sizeof(T));
     if (upper) p += align256(nblk * kTB * kTB * sizeof(T));
     return (T*)p;
 }
@@ -839,7 +848,7 @@ static gk_status lu_factor(int64_t n, T* A, int64_t lda, int32_t* ipiv, void* wo
         int kb = (int)min((int64_t)NB, n - k);
         if (max_cluster > 0) {
             const int64_t m = n - k;
-            const int max_rows = (int)((200 * 1024) / (NB * sizeof(T)));
+            const int max_rows = (int)((200 * 1024) / ((NB + 1) * sizeof(T)));
             int C = (int)((m + 127) / 128);
             if (C < 1) C = 1;
             if (C > max_cluster) C = max_cluster;
@@ -853,7 +862,7 @@ static gk_status lu_factor(int64_t n, T* A, int64_t lda, int32_t* ipiv, void* wo
                 attr[0].val.clusterDim.z = 1;
                 cfg.gridDim = dim3(C);
                 cfg.blockDim = dim3(256);
-                cfg.dynamicSmemBytes = (size_t)chunk * NB * sizeof(T);
+                cfg.dynamicSmemBytes = (size_t)chunk * (NB + 1) * sizeof(T);
                 cfg.stream = st;
                 cfg.attrs = attr;
                 cfg.numAttrs = 1;
@@ -926,13 +935,13 @@ static gk_status lu_solve(int64_t n, const T* LU, int64_t lda, const int32_t* ip
     char* p = (char*)work + panel_ws_bytes<T, NB>(sms);
     int32_t* perm = (int32_t*)p; p += align256((size_t)(n + 1) * sizeof(int32_t)) * 2;
     int nblk = (int)((n + BS - 1) / BS);
-    int* flags = (int*)p; p += align256((size_t)((n + 63) / 64 + 2) * sizeof(int));
+    int* flags = (int*)p; p += align256(((size_t)nblk + 2) * kFlagStride * sizeof(int));
     T* tmp = (T*)p;
     gather_kernel<T, T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(b, perm, n, tmp);
     GK_LAUNCH_CHECK();
-    int* counter = flags + nblk;
+    int* counter = flags + (size_t)nblk * kFlagStride;
     for (int pass = 0; pass < 2; ++pass) {
-        GK_CUDA_TRY(cudaMemsetAsync(flags, 0, (nblk + 1) * sizeof(int), st));
+        GK_CUDA_TRY(cudaMemsetAsync(flags, 0, ((size_t)nblk + 1) * kFlagStride * sizeof(int), st));
         // one CTA per block row; CTAs claim rows in solve order, so a CTA only
         // ever waits on rows claimed by CTAs that are already running
         trsv_kernel<T><<<nblk, 256, 0, st>>>(LU, lda, n, tmp, lu_ws_dinv<T>(work, n, pass), pass == 0 ? 1 : 0,
