@@ -44,10 +44,13 @@ __device__ __forceinline__ void rank1_update(T* S, int nr, int64_t rb, int64_t d
     __syncthreads();
     const int w = kb - j - 1;
     if (w > 0) {
-        const int cnt = (nr - r_first) * w;
-        for (int idx = threadIdx.x; idx < cnt; idx += blockDim.x) {
-            const int r = r_first + idx / w, c = j + 1 + idx % w;
-            S[r * SP + c] -= S[r * SP + j] * piv_row[c];
+        // w threads per row, rows_par rows at a time: one division per thread
+        const int rows_par = (int)blockDim.x / w;
+        const int t = (int)threadIdx.x;
+        if (t < rows_par * w) {
+            const int c = j + 1 + t % w;
+            const T pc = piv_row[c];
+            for (int r = r_first + t / w; r < nr; r += rows_par) S[r * SP + c] -= S[r * SP + j] * pc;
         }
     }
     __syncthreads();
