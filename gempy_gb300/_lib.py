@@ -24,7 +24,7 @@ c_double_p = ctypes.POINTER(ctypes.c_double)
 
 class GkInfo(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int32), ("where", ctypes.c_int32), ("iterations", ctypes.c_int32),
-                ("reserved", ctypes.c_int32), ("residual", ctypes.c_double)]
+                ("pivoted", ctypes.c_int32), ("residual", ctypes.c_double)]
 
 
 class GkSystem(ctypes.Structure):

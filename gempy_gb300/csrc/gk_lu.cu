@@ -323,6 +323,84 @@ __global__ void __launch_bounds__(256) panel_cluster_kernel(T* __restrict__ A, i
 }
 
 // ----------------------------------------------------------------------------
+// LU without pivoting (preconditioner factorization of the mixed solve).
+// After symmetric equilibration the covariance block of the kriging matrix is
+// SPD with unit diagonal, so the natural order (covariance unknowns first,
+// drift last) has non-zero pivots; the drift rows end with negative pivots
+// of the Schur complement.  No pivot search means no inter-CTA exchange:
+// per panel one CTA factors the diagonal block, L21 = A21 U11^-1 and
+// U12 = L11^-1 A12 are row/column parallel, then the trailing GEMM.
+// A zero or non-finite pivot is reported as GK_ERR_SINGULAR so the caller can
+// fall back to partial pivoting.
+// ----------------------------------------------------------------------------
+template <typename T, int NB>
+__global__ void __launch_bounds__(256) diag_lu_kernel(T* __restrict__ A, int64_t lda, int64_t k, int kb,
+                                                      int32_t* __restrict__ ipiv, gk_info* info) {
+    __shared__ T S[NB][NB + 1];
+    const int tid = threadIdx.x;
+    for (int idx = tid; idx < NB * NB; idx += blockDim.x) {
+        int r = idx / NB, c = idx % NB;
+        S[r][c] = (r < kb && c < kb) ? A[(k + r) * lda + k + c] : (T)0;
+    }
+    if (tid < kb) ipiv[k + tid] = (int32_t)(k + tid);
+    __syncthreads();
+    for (int j = 0; j < kb; ++j) {
+        const T pv = S[j][j];
+        const bool bad = !(pv == pv) || pv == (T)0 || !(gabs(pv) < (T)INFINITY);
+        if (bad) {
+            if (tid == 0) report(info, GK_ERR_SINGULAR, (int)(k + j));
+            break;  // uniform: every thread sees the same pivot
+        }
+        const T inv = (T)1 / pv;
+        for (int i = j + 1 + tid; i < kb; i += blockDim.x) S[i][j] *= inv;
+        __syncthreads();
+        const int w = kb - j - 1;
+        for (int idx = tid; idx < w * w; idx += blockDim.x) {
+            const int i = j + 1 + idx / w, c = j + 1 + idx % w;
+            S[i][c] -= S[i][j] * S[j][c];
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+    for (int idx = tid; idx < NB * NB; idx += blockDim.x) {
+        int r = idx / NB, c = idx % NB;
+        if (r < kb && c < kb) A[(k + r) * lda + k + c] = S[r][c];
+    }
+}
+
+// L21 = A21 U11^-1: rows r >= k + kb, 64 rows per CTA staged in shared memory
+// (transposed so a thread walks its row without bank conflicts).
+template <typename T, int NB>
+__global__ void __launch_bounds__(64) trsm_right_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k,
+                                                        int kb) {
+    __shared__ T U[NB][NB + 1];
+    __shared__ T X[NB][64 + 1];  // X[c][row]
+    const int tid = threadIdx.x;
+    for (int idx = tid; idx < NB * NB; idx += blockDim.x) {
+        int r = idx / NB, c = idx % NB;
+        U[r][c] = (r < kb && c < kb) ? A[(k + r) * lda + k + c] : (T)0;
+    }
+    const int64_t row0 = k + kb + (int64_t)blockIdx.x * 64;
+    for (int idx = tid; idx < 64 * NB; idx += blockDim.x) {
+        int r = idx / NB, c = idx % NB;
+        int64_t gr = row0 + r;
+        X[c][r] = (gr < n && c < kb) ? A[gr * lda + k + c] : (T)0;
+    }
+    __syncthreads();
+    for (int j = 0; j < kb; ++j) {
+        T v = X[j][tid];
+        for (int i = 0; i < j; ++i) v -= X[i][tid] * U[i][j];
+        X[j][tid] = v / U[j][j];
+    }
+    __syncthreads();
+    for (int idx = tid; idx < 64 * NB; idx += blockDim.x) {
+        int r = idx / NB, c = idx % NB;
+        int64_t gr = row0 + r;
+        if (gr < n && c < kb) A[gr * lda + k + c] = X[c][r];
+    }
+}
+
+// ----------------------------------------------------------------------------
 // Row interchanges on the columns outside the panel
 // ----------------------------------------------------------------------------
 template <typename T>
@@ -924,6 +1002,48 @@ static gk_status lu_factor(int64_t n, T* A, int64_t lda, int32_t* ipiv, void* wo
     return GK_OK;
 }
 
+template <typename T>
+static gk_status lu_factor_nopiv(int64_t n, T* A, int64_t lda, int32_t* ipiv, void* work, size_t wbytes,
+                                 gk_info* info, cudaStream_t st) {
+    constexpr int NB = LuCfg<T>::NB;
+    if (n <= 0 || A == nullptr || ipiv == nullptr || lda < n) return GK_ERR_ARG;
+    if (work == nullptr || wbytes < lu_ws_bytes<T>(n)) return GK_ERR_SIZE;
+    int sms = device_sm_count();
+    if (info) GK_CUDA_TRY(cudaMemsetAsync(info, 0, sizeof(gk_info), st));
+    for (int64_t k = 0; k < n; k += NB) {
+        int kb = (int)min((int64_t)NB, n - k);
+        diag_lu_kernel<T, NB><<<1, 256, 0, st>>>(A, lda, k, kb, ipiv, info);
+        GK_LAUNCH_CHECK();
+        int64_t rest = n - k - kb;
+        if (rest > 0) {
+            trsm_right_kernel<T, NB><<<(unsigned)((rest + 63) / 64), 64, 0, st>>>(A, lda, n, k, kb);
+            GK_LAUNCH_CHECK();
+            trsm_kernel<T, NB><<<(unsigned)((rest + 127) / 128), 128, 0, st>>>(A, lda, n, k, kb);
+            GK_LAUNCH_CHECK();
+            constexpr int BM = sizeof(T) == 8 ? 64 : 128;
+            constexpr int BN = BM;
+            dim3 grid((unsigned)((rest + BN - 1) / BN), (unsigned)((rest + BM - 1) / BM));
+            if (sizeof(T) == 4 && ((k + kb) % 4) == 0 && (lda % 4) == 0 && ((uintptr_t)A % 16) == 0) {
+                sgemm_update_kernel<<<grid, 256, 0, st>>>((float*)A, lda, n, k, kb);
+            } else {
+                gemm_update_kernel<T, BM, BN, 16><<<grid, 256, 0, st>>>(A, lda, n, k, kb);
+            }
+            GK_LAUNCH_CHECK();
+        }
+    }
+    int32_t* perm = (int32_t*)((char*)work + panel_ws_bytes<T, NB>(sms));
+    size_t psmem = n <= kPermSmem ? (size_t)n * sizeof(int32_t) : 0;
+    GK_CUDA_TRY(cudaFuncSetAttribute(perm_from_ipiv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPermSmem * 4));
+    perm_from_ipiv_kernel<<<1, 256, psmem, st>>>(ipiv, n, perm);
+    GK_LAUNCH_CHECK();
+    const size_t ysmem = (size_t)kTB * kTB * sizeof(T);
+    GK_CUDA_TRY(cudaFuncSetAttribute(tri_inv_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ysmem));
+    tri_inv_kernel<T><<<(unsigned)((n + kTB - 1) / kTB), kTB, ysmem, st>>>(A, lda, n, lu_ws_dinv<T>(work, n, 0),
+                                                                          lu_ws_dinv<T>(work, n, 1), info);
+    GK_LAUNCH_CHECK();
+    return GK_OK;
+}
+
 // Solve with the factors.  ``work`` is the workspace of the factorization:
 // after the panel area it holds perm (n+1, written by lu_factor), then the
 // block flags + claim counter, then a temporary vector.  ``b`` is overwritten.
@@ -990,3 +1110,7 @@ gk_status gk_internal_lu_solve_f32(int64_t n, const float* LU, int64_t lda, cons
     return lu_solve<float>(n, LU, lda, ipiv, b, work, wb, info, st);
 }
 size_t gk_internal_lu_ws_f32(int64_t n) { return lu_ws_bytes<float>(n); }
+gk_status gk_internal_lu_factor_nopiv_f32(int64_t n, float* A, int64_t lda, int32_t* ipiv, void* work, size_t wb,
+                                          gk_info* info, cudaStream_t st) {
+    return lu_factor_nopiv<float>(n, A, lda, ipiv, work, wb, info, st);
+}

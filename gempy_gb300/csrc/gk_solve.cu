@@ -22,6 +22,8 @@ gk_status gk_internal_lu_factor_f32(int64_t n, float* A, int64_t lda, int32_t* i
 gk_status gk_internal_lu_solve_f32(int64_t n, const float* LU, int64_t lda, const int32_t* ipiv, float* b, void* work,
                                    size_t wb, gk_info* info, cudaStream_t st);
 size_t gk_internal_lu_ws_f32(int64_t n);
+gk_status gk_internal_lu_factor_nopiv_f32(int64_t n, float* A, int64_t lda, int32_t* ipiv, void* work, size_t wb,
+                                          gk_info* info, cudaStream_t st);
 
 namespace gk {
 
@@ -45,6 +47,7 @@ struct MixedWork {
     double* part;   // kDotBlocks x (m+1) partial dots
     double* h;      // m+1 reduced dots
     double* y;      // m coefficients
+    gk_info* iinfo; // status word used when the caller passes none
 };
 
 static size_t mixed_bytes(int64_t n) {
@@ -52,7 +55,8 @@ static size_t mixed_bytes(int64_t n) {
     return al((size_t)n * ld * sizeof(float)) + al(n * sizeof(int32_t)) + al(gk_internal_lu_ws_f32(n)) +
            2 * al(n * sizeof(double)) + al(n * sizeof(float)) + al((size_t)(kRestart + 1) * n * sizeof(double)) +
            al((size_t)kRestart * n * sizeof(double)) + al(n * sizeof(double)) +
-           al((size_t)kDotBlocks * (kRestart + 1) * sizeof(double)) + 2 * al((kRestart + 1) * sizeof(double));
+           al((size_t)kDotBlocks * (kRestart + 1) * sizeof(double)) + 2 * al((kRestart + 1) * sizeof(double)) +
+           al(sizeof(gk_info));
 }
 
 static MixedWork carve(void* base, int64_t n) {
@@ -70,7 +74,8 @@ static MixedWork carve(void* base, int64_t n) {
     w.w = (double*)p; p += al(n * sizeof(double));
     w.part = (double*)p; p += al((size_t)kDotBlocks * (kRestart + 1) * sizeof(double));
     w.h = (double*)p; p += al((kRestart + 1) * sizeof(double));
-    w.y = (double*)p;
+    w.y = (double*)p; p += al((kRestart + 1) * sizeof(double));
+    w.iinfo = (gk_info*)p;
     return w;
 }
 
@@ -232,18 +237,35 @@ extern "C" gk_status gk_solve_mixed(int64_t n, const double* K, int64_t ldk, con
     if (n <= 0 || K == nullptr || b == nullptr || x == nullptr || ldk < n || max_iter < 1) return GK_ERR_ARG;
     if (work == nullptr || work_bytes < mixed_bytes(n)) return GK_ERR_SIZE;
     Solver S;
-    S.n = n; S.K = K; S.ldk = ldk; S.w = carve(work, n); S.ld32 = ld32_of(n); S.info = info; S.st = st;
+    S.n = n; S.K = K; S.ldk = ldk; S.w = carve(work, n); S.ld32 = ld32_of(n); S.st = st;
+    if (info == nullptr) info = S.w.iinfo;
+    S.info = info;
     S.vb = (unsigned)((n + 255) / 256);
     S.rb = (unsigned)((n * 32 + 255) / 256);
     MixedWork& w = S.w;
-    if (info) GK_CUDA_TRY(cudaMemsetAsync(info, 0, sizeof(gk_info), st));
+    GK_CUDA_TRY(cudaMemsetAsync(info, 0, sizeof(gk_info), st));
     equil_kernel<<<S.rb, 256, 0, st>>>(K, ldk, n, w.d);
     GK_LAUNCH_CHECK();
     dim3 cg((unsigned)((n + 255) / 256), (unsigned)(n < 4096 ? n : 4096));
     convert_kernel<<<cg, 256, 0, st>>>(K, ldk, n, w.d, w.K32, S.ld32);
     GK_LAUNCH_CHECK();
-    gk_status s = gk_internal_lu_factor_f32(n, w.K32, S.ld32, w.ipiv, w.luw, w.luw_bytes, info, st);
+    // FP32 LU of the equilibrated matrix: first without pivoting (no inter-CTA
+    // pivot exchange); on a zero / non-finite pivot, again with partial pivoting.
+    gk_status s = gk_internal_lu_factor_nopiv_f32(n, w.K32, S.ld32, w.ipiv, w.luw, w.luw_bytes, info, st);
     if (s != GK_OK) return s;
+    int pivoted = 0;
+    {
+        int32_t fst = 0;
+        GK_CUDA_TRY(cudaMemcpyAsync(&fst, &info->status, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+        GK_CUDA_TRY(cudaStreamSynchronize(st));
+        if (fst != 0) {
+            convert_kernel<<<cg, 256, 0, st>>>(K, ldk, n, w.d, w.K32, S.ld32);
+            GK_LAUNCH_CHECK();
+            s = gk_internal_lu_factor_f32(n, w.K32, S.ld32, w.ipiv, w.luw, w.luw_bytes, info, st);
+            if (s != GK_OK) return s;
+            pivoted = 1;
+        }
+    }
 
     double bnorm = 0.0;
     if ((s = S.norm2(b, bnorm)) != GK_OK) return s;
@@ -332,12 +354,13 @@ extern "C" gk_status gk_solve_mixed(int64_t n, const double* K, int64_t ldk, con
         rel = beta / bnorm;
         if (rel <= tol) status = GK_OK;
     }
-    if (info) {
+    {
         gk_info hi;
         GK_CUDA_TRY(cudaMemcpyAsync(&hi, info, sizeof(gk_info), cudaMemcpyDeviceToHost, st));
         GK_CUDA_TRY(cudaStreamSynchronize(st));
         if (hi.status == 0 && status != GK_OK) hi.status = status;
         hi.iterations = its;
+        hi.pivoted = pivoted;
         hi.residual = rel;
         GK_CUDA_TRY(cudaMemcpyAsync(info, &hi, sizeof(gk_info), cudaMemcpyHostToDevice, st));
         GK_CUDA_TRY(cudaStreamSynchronize(st));

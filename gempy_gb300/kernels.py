@@ -13,7 +13,7 @@ import torch
 from . import _lib
 from ._lib import GK_F32, GK_F64, GK_FF, GkPoints, GkSegment, GkSystem, check
 
-INFO_DTYPE = np.dtype([("status", "<i4"), ("where", "<i4"), ("iterations", "<i4"), ("reserved", "<i4"),
+INFO_DTYPE = np.dtype([("status", "<i4"), ("where", "<i4"), ("iterations", "<i4"), ("pivoted", "<i4"),
                        ("residual", "<f8")])
 
 

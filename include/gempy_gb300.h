@@ -58,12 +58,13 @@ typedef enum gk_kernel { GK_KERNEL_CUBIC = 0, GK_KERNEL_EXPONENTIAL = 1 } gk_ker
 
 /* Device status word written by the kernels.  ``status`` is a gk_status;
  * ``where`` locates the failure (pivot column, iteration, ...); the solver
- * fields report refinement progress. */
+ * fields report refinement progress; ``pivoted`` is set by gk_solve_mixed
+ * when its FP32 factorization had to fall back to partial pivoting. */
 typedef struct gk_info {
     int32_t status;
     int32_t where;
     int32_t iterations;
-    int32_t reserved;
+    int32_t pivoted;
     double residual;          /* final ||b - K x||_inf / ||b||_inf (solvers) */
 } gk_info;
 
@@ -150,7 +151,10 @@ gk_status gk_lu_solve(gk_prec prec, int64_t n, const void* LU, int64_t lda,
 
 /* Mixed-precision solve of the FP64 system K x = b (no reference
  * counterpart beyond the FP64 solve it replaces): an FP32 copy of the
- * symmetrically equilibrated K is LU-factored on the GPU and preconditions an
+ * symmetrically equilibrated K is LU-factored on the GPU -- without pivoting
+ * (the equilibrated covariance block is SPD with unit diagonal; the drift
+ * block comes last), or with partial pivoting if a pivot is zero or
+ * non-finite -- and preconditions an
  * FP64 restarted FGMRES(30) whose residuals r = b - K x use the FP64 K, until
  * ||r||_2 <= tol ||b||_2, stagnation, or ``max_iter`` Krylov steps.  ``work``
  * holds the FP32 factors and the Krylov vectors

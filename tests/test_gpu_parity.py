@@ -342,3 +342,42 @@ def test_bad_arguments_raise():
     ds.sys.uni_degree = 7
     with pytest.raises(_lib.GkError):
         K.build(ds)
+
+
+def _mixed_solve_raw(A, b):
+    from gempy_gb300 import _lib
+    from gempy_gb300 import kernels as K
+    import ctypes
+    lib = _lib.load()
+    n = A.shape[0]
+    ld = K.leading_dim(n, K.GK_F64)
+    Kt = torch.zeros((n, ld), dtype=torch.float64, device="cuda")
+    Kt[:, :n] = torch.as_tensor(A)
+    bt = torch.as_tensor(b, device="cuda")
+    x = torch.empty(n, dtype=torch.float64, device="cuda")
+    wb = lib.gk_solve_mixed_workspace_bytes(n)
+    work = torch.empty(wb, dtype=torch.uint8, device="cuda")
+    info = K.new_info("cuda")
+    _lib.check("gk_solve_mixed", lib.gk_solve_mixed(n, K._ptr(Kt), ld, K._ptr(bt), K._ptr(x), 1e-12, 60,
+                                                    K._ptr(work), wb, K._ptr(info), K._stream()))
+    return x.cpu().numpy(), K.read_info(info)
+
+
+def test_mixed_solve_falls_back_to_pivoting_on_zero_pivot():
+    rng = np.random.default_rng(21)
+    n = 300
+    A = rng.normal(size=(n, n)) + 30 * np.eye(n)
+    A[0, 0] = 0.0                       # the unpivoted factorization breaks down at once
+    b = rng.normal(size=n)
+    x, info = _mixed_solve_raw(A, b)
+    assert info["pivoted"] == 1
+    assert info["status"] == 0
+    assert np.linalg.norm(b - A @ x) <= 1e-11 * np.linalg.norm(b)
+
+
+def test_mixed_solve_without_pivoting_on_kriging_matrix():
+    s = _anticline()
+    Kr, br = kriging.build_system(s)
+    x, info = _mixed_solve_raw(Kr, br)
+    assert info["pivoted"] == 0
+    assert np.linalg.norm(br - Kr @ x) <= 1e-11 * np.linalg.norm(br)
