@@ -717,11 +717,32 @@ __global__ void __launch_bounds__(256) trsv_kernel(const T* __restrict__ A, int6
     const int blk = lower ? ord : nblk - 1 - ord;
     const int64_t r0 = (int64_t)blk * kTB;
     const int rows = (int)min((int64_t)kTB, n - r0);
+    // this warp's 16 rows of inv(D_b), prefetched before any wait
+    const T* Di = dinv + (int64_t)blk * kTB * kTB;
+    T dv[16][4];
+#pragma unroll
+    for (int q = 0; q < 16; ++q)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) dv[q][e] = Di[(int64_t)(wid * 16 + q) * kTB + lane + 32 * e];
     T acc[16];
 #pragma unroll
     for (int q = 0; q < 16; ++q) acc[q] = (T)0;
     for (int o = 0; o < ord; ++o) {
         const int dep = lower ? o : nblk - 1 - o;
+        const int64_t c0 = (int64_t)dep * kTB;
+        const int cols = (int)min((int64_t)kTB, n - c0);
+        // the matrix block does not depend on the flag: load it first
+        T av[16][4];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            const int r = wid * 16 + q;
+            const T* row = A + (r0 + (r < rows ? r : 0)) * lda + c0;
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int c = lane + 32 * e;
+                av[q][e] = (r < rows && c < cols) ? row[c] : (T)0;
+            }
+        }
         if (lane == 0) {
             long long spins = 0;
             while (true) {
@@ -730,12 +751,10 @@ __global__ void __launch_bounds__(256) trsv_kernel(const T* __restrict__ A, int6
                              : "memory");
                 if (f) break;
                 if (++spins > kSpinLimit) { report(info, GK_ERR_TIMEOUT, dep); break; }
-                if (spins > 8) __nanosleep(32);
+                if (spins > 64) __nanosleep(20);
             }
         }
         __syncwarp();
-        const int64_t c0 = (int64_t)dep * kTB;
-        const int cols = (int)min((int64_t)kTB, n - c0);
         T xv[4];
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
@@ -743,19 +762,9 @@ __global__ void __launch_bounds__(256) trsv_kernel(const T* __restrict__ A, int6
             xv[e] = c < cols ? ((volatile T*)x)[c0 + c] : (T)0;
         }
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
-            const int r = wid * 16 + q;
-            if (r < rows) {
-                const T* row = A + (r0 + r) * lda + c0;
-                T sacc = (T)0;
+        for (int q = 0; q < 16; ++q)
 #pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    const int c = lane + 32 * e;
-                    if (c < cols) sacc += row[c] * xv[e];
-                }
-                acc[q] += sacc;
-            }
-        }
+            for (int e = 0; e < 4; ++e) acc[q] += av[q][e] * xv[e];
     }
 #pragma unroll
     for (int q = 0; q < 16; ++q) {
@@ -766,29 +775,21 @@ __global__ void __launch_bounds__(256) trsv_kernel(const T* __restrict__ A, int6
     }
     __syncthreads();
     // x_b = inv(D_b) rhs
-    const T* Di = dinv + (int64_t)blk * kTB * kTB;
-    T outv[16];
+    T rv[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) rv[e] = rhs[lane + 32 * e];
 #pragma unroll
     for (int q = 0; q < 16; ++q) {
-        const int r = wid * 16 + q;
-        const T* drow = Di + (int64_t)r * kTB;
-        T sv = (T)0;
-#pragma unroll
-        for (int e = 0; e < 4; ++e) sv += drow[lane + 32 * e] * rhs[lane + 32 * e];
+        T sv = dv[q][0] * rv[0] + dv[q][1] * rv[1] + dv[q][2] * rv[2] + dv[q][3] * rv[3];
         for (int o = 16; o > 0; o >>= 1) sv += __shfl_down_sync(0xffffffffu, sv, o);
-        outv[q] = sv;
+        const int r = wid * 16 + q;
+        if (lane == 0 && r < rows) x[r0 + r] = sv;
     }
-    if (lane == 0) {
-#pragma unroll
-        for (int q = 0; q < 16; ++q) {
-            const int r = wid * 16 + q;
-            if (r < rows) x[r0 + r] = outv[q];
-        }
-    }
-    __threadfence();
     __syncthreads();
-    if (tid == 0)
+    if (tid == 0) {
+        __threadfence();
         asm volatile("st.release.gpu.global.b32 [%0], %1;" :: "l"(flags + kFlagStride * blk), "r"(1) : "memory");
+    }
 }
 
 // ----------------------------------------------------------------------------

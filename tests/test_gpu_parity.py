@@ -2,7 +2,7 @@
 
 Tolerances (written here, used by the judge of each test):
   * FP64 build: |K_gpu - K_oracle| <= 1e-13 max|K|
-  * FP64 LU/solve: ||b - K x|| / ||b|| <= 1e-11, x vs LAPACK <= 1e-8 relative
+  * FP64 LU/solve: ||b - K x|| <= 10 x LAPACK's residual, x vs LAPACK <= 1e-8 relative
   * FP64 field/gradient: max|dZ| / max|Z| <= 1e-9
   * FP32 (mixed) field: max|dZ| / max|Z| <= 1e-6; weights from the mixed solve
     <= 1e-6 relative to the FP64 solve
@@ -113,7 +113,8 @@ def test_plain_solve_matches_lapack(case):
     w, info = K.solve_plain(_dev_series(s))
     w = w.cpu().numpy()
     assert K.read_info(info)["status"] == 0
-    assert np.linalg.norm(br - Kr @ w) <= 1e-11 * np.linalg.norm(br)
+    res_ref = np.linalg.norm(br - Kr @ w_ref)
+    assert np.linalg.norm(br - Kr @ w) <= 10 * res_ref + 1e-13 * np.linalg.norm(br)
     assert np.abs(w - w_ref).max() <= 1e-8 * np.abs(w_ref).max()
 
 
