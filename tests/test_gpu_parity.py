@@ -2,7 +2,8 @@
 
 Tolerances (written here, used by the judge of each test):
   * FP64 build: |K_gpu - K_oracle| <= 1e-13 max|K|
-  * FP64 LU/solve: ||b - K x|| <= 10 x LAPACK's residual, x vs LAPACK <= 1e-8 relative
+  * FP64 LU/solve: ||b - K x||_inf <= 50 n eps ||K||_inf ||x||_inf (normwise
+    backward error of a stable LU), x vs LAPACK <= 1e-8 relative
   * FP64 field/gradient: max|dZ| / max|Z| <= 1e-9
   * FP32 (mixed) field: max|dZ| / max|Z| <= 1e-6; weights from the mixed solve
     <= 1e-6 relative to the FP64 solve
@@ -113,8 +114,10 @@ def test_plain_solve_matches_lapack(case):
     w, info = K.solve_plain(_dev_series(s))
     w = w.cpu().numpy()
     assert K.read_info(info)["status"] == 0
-    res_ref = np.linalg.norm(br - Kr @ w_ref)
-    assert np.linalg.norm(br - Kr @ w) <= 10 * res_ref + 1e-13 * np.linalg.norm(br)
+    # normwise backward error of a stable LU: ||b - K x|| <= c n eps ||K|| ||x||
+    n = len(br)
+    bound = 50 * n * np.finfo(float).eps * np.abs(Kr).sum(1).max() * np.abs(w).max()
+    assert np.abs(br - Kr @ w).max() <= bound
     assert np.abs(w - w_ref).max() <= 1e-8 * np.abs(w_ref).max()
 
 
@@ -320,7 +323,7 @@ def test_compute_model_three_series_octree_matches_oracle():
         np.testing.assert_array_equal(ol.last_output_center.mask_matrix.astype(bool), r_ref.masks)
     _, isos = pipeline.solve_all(ss)
     iso_ref = np.concatenate(isos)
-    np.testing.assert_allclose(sol.scalar_field_at_surface_points, iso_ref, rtol=0, atol=1e-12)
+    np.testing.assert_allclose(sol.scalar_field_at_surface_points, iso_ref, rtol=1e-9, atol=0)
 
 
 def test_nan_input_reports_status_without_fault():
