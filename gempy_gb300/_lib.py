@@ -17,6 +17,7 @@ STATUS_NAMES = {0: "OK", 1: "ERR_ARG", 2: "ERR_SIZE", 3: "ERR_CUDA", 4: "ERR_SIN
 GK_F64, GK_F32, GK_FF = 0, 1, 2
 GK_KERNEL_CUBIC, GK_KERNEL_EXPONENTIAL = 0, 1
 GK_MAX_SURFACES = 32
+GK_NOALLOC_MAX_N = 1024
 
 c_int32_p = ctypes.POINTER(ctypes.c_int32)
 c_double_p = ctypes.POINTER(ctypes.c_double)
@@ -67,6 +68,9 @@ SIGNATURES = [
     ("gk_solve_mixed", ctypes.c_int, [ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                       ctypes.c_void_p, ctypes.c_double, ctypes.c_int32, ctypes.c_void_p,
                                       ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]),
+    ("gk_solve_mixed_noalloc", ctypes.c_int, [ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                              ctypes.c_void_p, ctypes.c_double, ctypes.c_int32, ctypes.c_void_p,
+                                              ctypes.c_void_p]),
     ("gk_eval_model_bytes", ctypes.c_size_t, [ctypes.POINTER(GkSystem)]),
     ("gk_eval_prepare", ctypes.c_int, [ctypes.POINTER(GkSystem), ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_void_p]),

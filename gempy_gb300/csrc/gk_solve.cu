@@ -13,6 +13,7 @@
 // device-to-host copy per step).
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "gk_common.cuh"
@@ -366,4 +367,49 @@ extern "C" gk_status gk_solve_mixed(int64_t n, const double* K, int64_t ldk, con
         GK_CUDA_TRY(cudaStreamSynchronize(st));
     }
     return GK_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of gk_solve_mixed.
+//
+// Its scratch is this file-scope device array.  Every GPU that loads the
+// library holds it (8 MiB) until the process exits, and every call shares it:
+// each call rewrites or clears everything it reads before reading it, and two
+// calls that overlap on the GPU (different streams, or without ordering
+// between them) race on it.  Host code cannot use the array's name as a device
+// address; the address is looked up once per device with
+// cudaGetSymbolAddress, by the first call made with that device current.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr size_t kNoAllocBytes = (size_t)8 << 20;
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[kMaxDevices] = {};
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+extern "C" gk_status gk_solve_mixed_noalloc(int64_t n, const double* K, int64_t ldk, const double* b, double* x,
+                                            double tol, int32_t max_iter, gk_info* info, gk_stream stream) {
+    if (n <= 0 || K == nullptr || b == nullptr || x == nullptr || ldk < n || max_iter < 1) return GK_ERR_ARG;
+    if (n > GK_NOALLOC_MAX_N) return GK_ERR_SIZE;
+    if (mixed_bytes(n) > kNoAllocBytes) return GK_ERR_SIZE;
+    int dev = -1;
+    GK_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return GK_ERR_CUDA;
+    void* ptr = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+        if (g_noalloc_ptr[dev] == nullptr) {
+            void* p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess || p == nullptr) {
+                (void)cudaGetLastError();
+                return GK_ERR_CUDA;
+            }
+            g_noalloc_ptr[dev] = p;
+        }
+        ptr = g_noalloc_ptr[dev];
+    }
+    return gk_solve_mixed(n, K, ldk, b, x, tol, max_iter, ptr, kNoAllocBytes, info, stream);
 }

@@ -166,6 +166,27 @@ gk_status gk_solve_mixed(int64_t n, const double* K, int64_t ldk,
                          int32_t max_iter, void* work, size_t work_bytes,
                          gk_info* info, gk_stream stream);
 
+/* Allocation-free form of gk_solve_mixed, with no counterpart in the
+ * reference.  It is for callers that cannot call cudaMalloc -- for example
+ * code running inside a framework that owns the whole device-memory budget
+ * through its own pool or caching allocator and forbids side allocations, or a
+ * host runtime that binds this C ABI but has no way to hand it device
+ * workspace.  The solver's scratch is a file-scope device array of the
+ * library (8 MiB, held on every GPU that loads the library until the process
+ * exits), so only systems with n <= GK_NOALLOC_MAX_N are accepted; larger n
+ * returns GK_ERR_SIZE before any work is queued.  The caller still passes K,
+ * b and x.  The first call made on a device looks up the array's device
+ * address (cudaGetSymbolAddress); make that first call before any stream
+ * capture.  All calls share the one array: calls that overlap on the GPU
+ * race, so serialize them (one stream, or explicit ordering).  Nothing here
+ * calls cudaMalloc, cudaFree or an allocating library routine.  Arguments,
+ * results and ``info`` are as for gk_solve_mixed (``info`` may be NULL). */
+#define GK_NOALLOC_MAX_N 1024
+gk_status gk_solve_mixed_noalloc(int64_t n, const double* K, int64_t ldk,
+                                 const double* b, double* x, double tol,
+                                 int32_t max_iter, gk_info* info,
+                                 gk_stream stream);
+
 /* ---------------- evaluation + segmentation (engine evaluation) ---------- */
 
 /* Packs the solved model (weights ``w`` of length N) into the layout the
