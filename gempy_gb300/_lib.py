@@ -51,6 +51,25 @@ class GkSegment(ctypes.Structure):
                 ("unit_values", ctypes.c_double * (GK_MAX_SURFACES + 1))]
 
 
+class GkBatchItem(ctypes.Structure):
+    _fields_ = [("n_ori", ctypes.c_int32), ("n_sp", ctypes.c_int32), ("n_iface", ctypes.c_int32),
+                ("uni_degree", ctypes.c_int32), ("kernel", ctypes.c_int32), ("n_surf", ctypes.c_int32),
+                ("range", ctypes.c_double), ("c_o", ctypes.c_double), ("i_res", ctypes.c_double),
+                ("gi_res", ctypes.c_double), ("ori_offset", ctypes.c_int64), ("sp_offset", ctypes.c_int64),
+                ("iface_offset", ctypes.c_int64), ("points_per_surface", ctypes.c_int32 * GK_MAX_SURFACES),
+                ("dims", ctypes.c_int32 * 3), ("reserved", ctypes.c_int32), ("origin", ctypes.c_double * 3),
+                ("spacing", ctypes.c_double * 3), ("slope", ctypes.c_double),
+                ("unit_values", ctypes.c_double * (GK_MAX_SURFACES + 1))]
+
+
+class GkBatch(ctypes.Structure):
+    _fields_ = [("n_items", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("items", ctypes.POINTER(GkBatchItem)), ("dip_positions", ctypes.c_void_p),
+                ("dip_gradients", ctypes.c_void_p), ("nugget_grad", ctypes.c_void_p),
+                ("sp_coords", ctypes.c_void_p), ("nugget_sp", ctypes.c_void_p),
+                ("ref_index", ctypes.c_void_p), ("rest_index", ctypes.c_void_p)]
+
+
 # (name, restype, argtypes) of every exported symbol; tests check the header
 # declares exactly these.
 SIGNATURES = [
@@ -86,6 +105,14 @@ SIGNATURES = [
     ("gk_octree_refine", ctypes.c_int, [ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
                                         c_double_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_size_t, ctypes.c_void_p]),
+    ("gk_batch_workspace_bytes", ctypes.c_size_t, [ctypes.POINTER(GkBatch)]),
+    ("gk_batch_points", ctypes.c_int64, [ctypes.POINTER(GkBatch)]),
+    ("gk_batch_plan", ctypes.c_int, [ctypes.POINTER(GkBatch), ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("gk_batch_run", ctypes.c_int, [ctypes.POINTER(GkBatch), ctypes.c_void_p, ctypes.c_size_t, ctypes.c_double,
+                                    ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.c_void_p, ctypes.c_void_p]),
+    ("gk_batch_results", ctypes.c_int, [ctypes.POINTER(GkBatch), ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int32,
+                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     ("gk_version", ctypes.c_char_p, []),
     ("gk_launch_count", ctypes.c_uint64, []),
 ]

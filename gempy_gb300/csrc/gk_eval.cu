@@ -91,19 +91,6 @@ __global__ void ff_maxabs_kernel(const double* __restrict__ a, int n3, double in
     if ((threadIdx.x & 31) == 0) atomicMax(maxbits, __float_as_uint(v));
 }
 
-__device__ __forceinline__ double ff_quantum(const unsigned int* maxbits) {
-    float m = __uint_as_float(*maxbits);
-    if (!(m > 1e-30f)) m = 1.f;
-    int e = (int)ceil(log2((double)m));
-    return ldexp(1.0, e + 4 - 23);
-}
-
-__device__ __forceinline__ void ff_split(double u, double q, float& h, float& l) {
-    double hi = rint(u / q) * q;
-    h = (float)hi;
-    l = (float)(u - hi);
-}
-
 __global__ void pack_ff_kernel(int n_ori, int n_sp, double inv_a, double w_scale_ori, double w_scale_sp,
                                const double* __restrict__ dip, const double* __restrict__ sp,
                                const double* __restrict__ w, const double* __restrict__ alpha,
@@ -392,11 +379,6 @@ drain:
 // ---------------------------------------------------------------------------
 // float-float evaluation (cubic kernel, field only)
 // ---------------------------------------------------------------------------
-struct PointFF {
-    float h[3], l[3];
-    bool exact;
-};
-
 __device__ __forceinline__ void point_coords(const EvalParams& P, int64_t q, double* xd) {
     if (P.kind == 0) {
         const int64_t nyz = (int64_t)P.dims[1] * P.dims[2];
@@ -410,42 +392,6 @@ __device__ __forceinline__ void point_coords(const EvalParams& P, int64_t q, dou
         xd[1] = P.xyz[3 * q + 1];
         xd[2] = P.xyz[3 * q + 2];
     }
-}
-
-__device__ __forceinline__ void ff_point(const double* xd, double inv_a, double q, PointFF& P) {
-    const double lim = ldexp(q, 23);
-    P.exact = true;
-    for (int k = 0; k < 3; ++k) {
-        double u = xd[k] * inv_a;
-        double hi = rint(u / q) * q;
-        P.h[k] = (float)hi;
-        P.l[k] = (float)(u - hi);
-        if (fabs(hi) > lim) P.exact = false;
-    }
-}
-
-// r^2 of d = x - p as float-float; d_k = dh_k + dl_k with dh_k exact when the
-// split is exact, else recovered with a two-sum.
-__device__ __forceinline__ ff ff_dist2(const PointFF& X, const float* ph, const float* pl, float* dh, float* dl) {
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        if (X.exact) {
-            dh[k] = X.h[k] - ph[k];
-            dl[k] = X.l[k] - pl[k];
-        } else {
-            ff t = two_sum(X.h[k], -ph[k]);
-            dh[k] = t.h;
-            dl[k] = t.l + (X.l[k] - pl[k]);
-        }
-    }
-    ff a0 = two_prod(dh[0], dh[0]), a1 = two_prod(dh[1], dh[1]), a2 = two_prod(dh[2], dh[2]);
-    ff s1 = two_sum(a0.h, a1.h);
-    ff s2 = two_sum(s1.h, a2.h);
-    float low = s1.l + s2.l + a0.l + a1.l + a2.l;
-    low = __fmaf_rn(dl[0], 2.f * dh[0] + dl[0], low);
-    low = __fmaf_rn(dl[1], 2.f * dh[1] + dl[1], low);
-    low = __fmaf_rn(dl[2], 2.f * dh[2] + dl[2], low);
-    return fast_two_sum(s2.h, low);
 }
 
 template <int PPT>

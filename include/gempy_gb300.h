@@ -235,6 +235,66 @@ gk_status gk_octree_refine(int64_t n, const double* centres,
                            double* children, int64_t* count, void* work,
                            size_t work_bytes, gk_stream stream);
 
+/* ---------------- batched realisations (many compute_model calls) ------- */
+
+/* One realisation of a batch: a single-series model, its 3-D regular grid
+ * and its segmentation.  Offsets locate its rows in the batch's concatenated
+ * device arrays; ref/rest indices are local to the realisation. */
+typedef struct gk_batch_item {
+    int32_t n_ori, n_sp, n_iface, uni_degree, kernel, n_surf;
+    double range, c_o, i_res, gi_res;
+    int64_t ori_offset;   /* first orientation in the batch arrays          */
+    int64_t sp_offset;    /* first surface point                            */
+    int64_t iface_offset; /* first interface row of ref_index / rest_index  */
+    int32_t points_per_surface[GK_MAX_SURFACES];
+    int32_t dims[3];
+    int32_t reserved;
+    double origin[3], spacing[3];
+    double slope;
+    double unit_values[GK_MAX_SURFACES + 1];
+} gk_batch_item;
+
+typedef struct gk_batch {
+    int32_t n_items;
+    int32_t reserved;
+    const gk_batch_item* items;                     /* HOST array            */
+    const double* dip_positions;                    /* device, n x 3          */
+    const double* dip_gradients;
+    const double* nugget_grad;
+    const double* sp_coords;
+    const double* nugget_sp;
+    const int32_t* ref_index;
+    const int32_t* rest_index;
+} gk_batch;
+
+/* Workspace of a batch (all realisations' matrices, Krylov vectors and
+ * records) and the total number of grid points (output length). */
+size_t gk_batch_workspace_bytes(const gk_batch* batch);
+int64_t gk_batch_points(const gk_batch* batch);
+
+/* Lays the batch out in ``work`` (descriptors, work lists, largest-first
+ * solve order).  Synchronous; call once per batch, outside stream capture. */
+gk_status gk_batch_plan(const gk_batch* batch, void* work, size_t work_bytes,
+                        gk_stream stream);
+
+/* Builds, solves (FP32 LU without pivoting preconditioning FP64 FGMRES, one
+ * CTA per realisation, tolerance ``tol`` on ||b - K x||_2 / ||b||_2),
+ * evaluates every realisation's grid in float-float and segments it, with
+ * four persistent launches and no host synchronisation, so the sequence can
+ * be captured in a CUDA graph and replayed on new inputs of the same layout.
+ * Outputs are concatenated in item order; ``infos`` has one entry per item
+ * (may be NULL).  Cubic kernel only. */
+gk_status gk_batch_run(const gk_batch* batch, void* work, size_t work_bytes,
+                       double tol, int32_t max_iter, double* field,
+                       double* values, int32_t* ids, gk_info* infos,
+                       gk_stream stream);
+
+/* Copies one realisation's weights (N) and isovalues (stack order) out of the
+ * workspace into device buffers (either may be NULL). */
+gk_status gk_batch_results(const gk_batch* batch, const void* work,
+                           size_t work_bytes, int32_t item, double* weights,
+                           double* isovalues, gk_stream stream);
+
 /* Library version string (HOST). */
 const char* gk_version(void);
 
