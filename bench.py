@@ -179,6 +179,8 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid", type=int, default=256)
+    ap.add_argument("--no-extra", action="store_true", help="skip the batch and octree sections")
+    ap.add_argument("--batch-realisations", type=int, default=512)
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -362,12 +364,121 @@ def main():
                      "work": f"{fl_pt} algorithmic flops/point x {n_pts} points per launch",
                      "eval_ms": ev_mixed},
     }
+    if not args.no_extra:
+        line["batch"] = batch_section(n_real=args.batch_realisations)
+        line["octree"] = octree_section()
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(m)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def batch_section(n_real=512, res=64, plain=True):
+    """Config 4: ``n_real`` uneven realisations, each on its own res^3 grid, in
+    one captured CUDA graph (mixed form), against the plain FP64 form run per
+    realisation with the single-system kernels."""
+    import torch
+    from gempy_gb300 import kernels as K
+    from gempy_gb300 import synthetic
+    from gempy_gb300.batch import BatchRunner
+    models = [synthetic.realisation(i, resolution=(res,) * 3) for i in range(n_real)]
+    br = BatchRunner(models)
+    br.capture()
+    stream = torch.cuda.current_stream()
+    for _ in range(2):
+        br.replay()
+    torch.cuda.synchronize()
+    evs = []
+    for _ in range(3):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        br.replay()
+        b.record(stream)
+        torch.cuda.synchronize()
+        evs.append(a.elapsed_time(b))
+    ms = float(np.median(evs))
+    infos = br.infos_host()
+    out = {"realisations": n_real, "grid": f"{res}^3 each", "points": br.n_points,
+           "N_max": int(max(3 * m.n_orientations + m.n_points - 4 + 3 for m in models)),
+           "ms": ms, "grid_points_per_s": br.n_points / (ms * 1e-3), "solves_per_s": n_real / (ms * 1e-3),
+           "launches_per_replay": 4, "captured_in_cuda_graph": True,
+           "solver": {"converged": int((infos["status"] == 0).sum()),
+                      "max_residual": float(infos["residual"].max()),
+                      "max_iterations": int(infos["iterations"].max())}}
+    if plain:
+        field_b = br.field.clone()
+        ids_b = br.ids.clone()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        t0.record(stream)
+        err, mism = 0.0, 0
+        fields = []
+        for i, m in enumerate(models):
+            ii, dd, ko = m.interpolation_input, m.data_descriptor, m.options.kernel_options
+            ds = K.DeviceSeries(ii.orientations.dip_positions, ii.orientations.dip_gradients,
+                                ii.orientations.nugget_effect_grad, ii.surface_points.sp_coords,
+                                ii.surface_points.nugget_effect_scalar,
+                                dd.tensors_structure.number_of_points_per_surface, range=ko.range, c_o=ko.c_o,
+                                uni_degree=ko.uni_degree)
+            w, _ = K.solve_plain(ds)
+            model = K.prepare(ds, w)
+            iso_t, _, _, _ = K.evaluate(ds, model, K.Points(xyz=ds.ref_points), K.GK_F64)
+            iso = iso_t.cpu().numpy()
+            order = np.argsort(-iso, kind="stable")
+            seg = K.make_segment(iso[order], ii.unit_values, m.options.sigmoid_slope)
+            f, _, _, ids = K.evaluate(ds, model, K.Points.regular(ii.grid.dense_grid), K.GK_F64, seg=seg,
+                                      want_ids=True)
+            fields.append((f, ids, iso))
+        t1.record(stream)
+        torch.cuda.synchronize()
+        ms_p = t0.elapsed_time(t1)
+        for i, (f, ids, iso) in enumerate(fields):
+            sl = br.item_slice(i)
+            fb = field_b[sl]
+            err = max(err, float((fb - f).abs().max() / f.abs().max()))
+            band = max(10.0 / models[i].options.sigmoid_slope, 4e-6 * float(f.abs().max()))
+            it = torch.as_tensor(iso, device=f.device)
+            outside = ((f[:, None] - it[None, :]).abs() > band).all(dim=1)
+            mism += int(((ids_b[sl] != ids) & outside).sum())
+        out["plain_fp64"] = {"ms": ms_p, "grid_points_per_s": br.n_points / (ms_p * 1e-3),
+                             "solves_per_s": n_real / (ms_p * 1e-3),
+                             "note": "single-system FP64 kernels, one realisation after another"}
+        out["speedup_vs_plain_fp64"] = ms_p / ms
+        out["errors_vs_fp64"] = {"field_rel_max": err, "ids_mismatch_outside_band": mism}
+    return out
+
+
+def octree_section():
+    """Config 2: three folded series, quadratic drift, 7 octree levels, through
+    compute_model (host inputs), plain FP64 and mixed."""
+    import torch
+    import gempy_gb300 as gg
+    from gempy_gb300 import synthetic
+    m = synthetic.folded_series(octree_levels=7)
+    out = {"workload": "3 series x 2 folded surfaces, 200 points, 60 orientations, quadratic drift, "
+                       "7 octree levels (128^3 effective)"}
+    for name, dt in (("plain_fp64", "float64"), ("mixed", "float32")):
+        cfg = gg.EngineConfig(dtype=dt)
+        gg.compute_model(m.interpolation_input, m.options, m.data_descriptor, config=cfg)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        reps = 3
+        for _ in range(reps):
+            sol = gg.compute_model(m.interpolation_input, m.options, m.data_descriptor, config=cfg)
+        torch.cuda.synchronize()
+        dt_s = (time.perf_counter() - t0) / reps
+        npts = sum(len(l.grid_centers) for l in sol.octrees_output)
+        out[name] = {"ms": 1e3 * dt_s, "octree_points": npts, "points_per_s": npts / dt_s,
+                     "levels": [len(l.grid_centers) for l in sol.octrees_output]}
+        out.setdefault("_ids", {})[name] = sol.octrees_output[-1].last_output_center.ids_block
+    a, b = out.pop("_ids").values()
+    out["ids_identical_last_level"] = bool(np.array_equal(a, b))
+    out["speedup_vs_plain_fp64"] = out["plain_fp64"]["ms"] / out["mixed"]["ms"]
+    return out
 
 
 def cpu_baseline(m, sample=4096):
