@@ -18,6 +18,8 @@ GK_F64, GK_F32, GK_FF = 0, 1, 2
 GK_KERNEL_CUBIC, GK_KERNEL_EXPONENTIAL = 0, 1
 GK_MAX_SURFACES = 32
 GK_NOALLOC_MAX_N = 1024
+GK_TUNE_EVAL_FF, GK_TUNE_EVAL_F32, GK_TUNE_BATCH_EVAL = 0, 1, 2
+TUNABLES = {"eval_ff": GK_TUNE_EVAL_FF, "eval_f32": GK_TUNE_EVAL_F32, "batch_eval": GK_TUNE_BATCH_EVAL}
 
 c_int32_p = ctypes.POINTER(ctypes.c_int32)
 c_double_p = ctypes.POINTER(ctypes.c_double)
@@ -113,6 +115,10 @@ SIGNATURES = [
                                     ctypes.c_void_p, ctypes.c_void_p]),
     ("gk_batch_results", ctypes.c_int, [ctypes.POINTER(GkBatch), ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int32,
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    ("gk_tune_variants", ctypes.c_int32, []),
+    ("gk_tune_describe", ctypes.c_int, [ctypes.c_int32, c_int32_p, c_int32_p]),
+    ("gk_tune_set", ctypes.c_int, [ctypes.c_int32, ctypes.c_int32]),
+    ("gk_tune_get", ctypes.c_int32, [ctypes.c_int32]),
     ("gk_version", ctypes.c_char_p, []),
     ("gk_launch_count", ctypes.c_uint64, []),
 ]

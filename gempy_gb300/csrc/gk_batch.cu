@@ -25,6 +25,7 @@
 
 #include "gk_ff.cuh"
 #include "gk_kriging.cuh"
+#include "gk_tune.h"
 
 namespace gk {
 
@@ -591,8 +592,7 @@ __global__ void __launch_bounds__(256) batch_prepare_kernel(const BatchDesc* __r
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-constexpr int kStage = 32 * 1024;
-constexpr int kPPT = 4;
+constexpr int kChunkPoints = 1024;  // points per (system, chunk) item, whatever the variant
 constexpr long long kWaitSpin = 4LL * 1000 * 1000;
 
 struct Cursor {
@@ -600,9 +600,12 @@ struct Cursor {
     int t;       // tile within the item
 };
 
+template <int kPPT, int kStage>
 __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchDesc* __restrict__ D, int n_sys,
                                                          const int64_t* __restrict__ chunk_prefix, double* field,
                                                          double* values, int32_t* ids, int* err) {
+    static_assert(kChunkPoints % (256 * kPPT) == 0, "chunk is a whole number of passes");
+    constexpr int kPasses = kChunkPoints / (256 * kPPT);
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t mbar[2];
     __shared__ int s_fail;
@@ -631,17 +634,19 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchDesc* __rest
             const int64_t item = blockIdx.x + pc.k * gridDim.x;
             const int s = find_system(chunk_prefix, n_sys, item);
             const int nt = tiles_of(s);
-            if (pc.t >= nt) { pc.k++; pc.t = 0; continue; }
+            // every pass over the item's points consumes all of its tiles once
+            if (pc.t >= nt * kPasses) { pc.k++; pc.t = 0; continue; }
+            const int tt = pc.t % nt;
             const BatchDesc& d = D[s];
             const int to = (d.n_ori + rec_ori - 1) / rec_ori;
             const void* src;
             uint32_t bytes;
-            if (pc.t < to) {
-                int r0 = pc.t * rec_ori, nr = min(rec_ori, d.n_ori - r0);
+            if (tt < to) {
+                int r0 = tt * rec_ori, nr = min(rec_ori, d.n_ori - r0);
                 src = d.rec + 16 * (int64_t)r0;
                 bytes = (uint32_t)(nr * 64);
             } else {
-                int r0 = (pc.t - to) * rec_sp, nr = min(rec_sp, d.n_sp - r0);
+                int r0 = (tt - to) * rec_sp, nr = min(rec_sp, d.n_sp - r0);
                 src = d.rec + 16 * (int64_t)d.n_ori + 8 * (int64_t)r0;
                 bytes = (uint32_t)(nr * 32);
             }
@@ -672,12 +677,13 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchDesc* __rest
         const int nt = tiles_of(s);
         const int to = (d.n_ori + rec_ori - 1) / rec_ori;
         const int nyz = d.dims[1] * d.dims[2];
+        for (int pass = 0; pass < kPasses; ++pass) {
         PointFF X[kPPT];
         int64_t pid[kPPT];
         double Z[kPPT];
 #pragma unroll
         for (int p = 0; p < kPPT; ++p) {
-            pid[p] = c * (256 * kPPT) + tid + p * 256;
+            pid[p] = c * kChunkPoints + pass * (256 * kPPT) + tid + p * 256;
             const int64_t qd = pid[p] < d.n_points ? pid[p] : d.n_points - 1;
             const int64_t ix = qd / nyz, rem = qd - ix * nyz;
             const int64_t iy = rem / d.dims[2], iz = rem - iy * d.dims[2];
@@ -803,6 +809,7 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchDesc* __rest
             if (values) values[o] = v;
             if (ids) ids[o] = (int32_t)rint(v);
         }
+        }  // pass
     }
 }
 
@@ -953,7 +960,7 @@ extern "C" gk_status gk_batch_plan(const gk_batch* b, void* work, size_t work_by
         out_off += d.n_points;
         d.tile_side = (d.N + 31) / 32;
         tiles[i + 1] = tiles[i] + (int64_t)d.tile_side * d.tile_side;
-        chunks[i + 1] = chunks[i] + (d.n_points + 256 * kPPT - 1) / (256 * kPPT);
+        chunks[i + 1] = chunks[i] + (d.n_points + kChunkPoints - 1) / kChunkPoints;
         d.tile_begin = tiles[i];
         d.chunk_begin = chunks[i];
         order[i] = i;
@@ -968,6 +975,20 @@ extern "C" gk_status gk_batch_plan(const gk_batch* b, void* work, size_t work_by
     GK_CUDA_TRY(cudaMemcpyAsync(base + L.order, order.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, s));
     GK_CUDA_TRY(cudaMemcpyAsync(base + L.descs, descs.data(), n * sizeof(BatchDesc), cudaMemcpyHostToDevice, s));
     GK_CUDA_TRY(cudaStreamSynchronize(s));  // host vectors go out of scope
+    return GK_OK;
+}
+
+template <int PPT, int STAGE>
+static gk_status launch_batch_eval(const BatchDesc* D, int n, const int64_t* chunk_prefix, double* field,
+                                   double* values, int32_t* ids, int* err, int sms, cudaStream_t s) {
+    auto k = batch_eval_kernel<PPT, STAGE>;
+    const size_t smem = 2 * (size_t)STAGE;
+    GK_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int occ = 0;
+    GK_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, 256, smem));
+    if (occ < 1) occ = 1;
+    k<<<sms * occ, 256, smem, s>>>(D, n, chunk_prefix, field, values, ids, err);
+    GK_LAUNCH_CHECK();
     return GK_OK;
 }
 
@@ -996,15 +1017,18 @@ extern "C" gk_status gk_batch_run(const gk_batch* b, void* work, size_t work_byt
     GK_LAUNCH_CHECK();
     batch_prepare_kernel<<<(unsigned)n, 256, 0, s>>>(D, (int)n);
     GK_LAUNCH_CHECK();
-    const size_t smem = 2 * (size_t)kStage;
-    GK_CUDA_TRY(cudaFuncSetAttribute(batch_eval_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int occ = 0;
-    GK_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_eval_kernel, 256, smem));
-    if (occ < 1) occ = 1;
-    batch_eval_kernel<<<sms * occ, 256, smem, s>>>(D, (int)n, (const int64_t*)(base + chunk_prefix), field, values,
-                                                   ids, counters + 2);
-    GK_LAUNCH_CHECK();
-    return GK_OK;
+    const TuneVariant v = tune_variant(GK_TUNE_BATCH_EVAL);
+    if (v.ppt == 4 && v.stage_kb == 32)
+        return launch_batch_eval<4, 32 * 1024>(D, (int)n, (const int64_t*)(base + chunk_prefix), field, values, ids,
+                                               counters + 2, sms, s);
+    if (v.ppt == 2 && v.stage_kb == 32)
+        return launch_batch_eval<2, 32 * 1024>(D, (int)n, (const int64_t*)(base + chunk_prefix), field, values, ids,
+                                               counters + 2, sms, s);
+    if (v.ppt == 4)
+        return launch_batch_eval<4, 16 * 1024>(D, (int)n, (const int64_t*)(base + chunk_prefix), field, values, ids,
+                                               counters + 2, sms, s);
+    return launch_batch_eval<2, 16 * 1024>(D, (int)n, (const int64_t*)(base + chunk_prefix), field, values, ids,
+                                           counters + 2, sms, s);
 }
 
 extern "C" gk_status gk_batch_results(const gk_batch* b, const void* work, size_t work_bytes, int32_t item,

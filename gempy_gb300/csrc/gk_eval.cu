@@ -16,6 +16,7 @@
 
 #include "gk_common.cuh"
 #include "gk_ff.cuh"
+#include "gk_tune.h"
 
 namespace gk {
 
@@ -645,8 +646,8 @@ extern "C" gk_status gk_eval_prepare(const gk_system* s, const double* w, void* 
 }
 
 template <typename T, int PPT, bool GRAD>
-static gk_status launch_eval(EvalParams& P, cudaStream_t st) {
-    const int stage_bytes = 32 * 1024;
+static gk_status launch_eval(EvalParams& P, cudaStream_t st, int stage_kb = 32) {
+    const int stage_bytes = stage_kb * 1024;
     P.stage_bytes = stage_bytes;
     P.rec_ori = stage_bytes / (8 * sizeof(T));
     P.rec_sp = stage_bytes / (4 * sizeof(T));
@@ -673,8 +674,8 @@ static gk_status launch_eval(EvalParams& P, cudaStream_t st) {
 }
 
 template <int PPT>
-static gk_status launch_eval_ff(EvalParams& P, const double* meta, cudaStream_t st) {
-    const int stage_bytes = 32 * 1024;
+static gk_status launch_eval_ff(EvalParams& P, const double* meta, cudaStream_t st, int stage_kb) {
+    const int stage_bytes = stage_kb * 1024;
     P.stage_bytes = stage_bytes;
     P.rec_ori = stage_bytes / (16 * sizeof(float));
     P.rec_sp = stage_bytes / (8 * sizeof(float));
@@ -748,13 +749,18 @@ extern "C" gk_status gk_eval(const gk_system* s, const void* model, const gk_poi
     if (prec == GK_F32) {
         P.ori = m + L.ori32;
         P.sp = m + L.sp32;
-        return grad ? launch_eval<float, 2, true>(P, cs) : launch_eval<float, 2, false>(P, cs);
+        if (grad) return launch_eval<float, 2, true>(P, cs);
+        const TuneVariant v = tune_variant(GK_TUNE_EVAL_F32);
+        return v.ppt == 2 ? launch_eval<float, 2, false>(P, cs, v.stage_kb)
+                          : launch_eval<float, 4, false>(P, cs, v.stage_kb);
     }
     if (prec == GK_FF) {
         if (grad != nullptr || s->kernel != GK_KERNEL_CUBIC) return GK_ERR_ARG;
         P.ori = m + L.ffori;
         P.sp = m + L.ffsp;
-        return launch_eval_ff<4>(P, (const double*)(m + L.ffmeta), cs);
+        const TuneVariant v = tune_variant(GK_TUNE_EVAL_FF);
+        return v.ppt == 2 ? launch_eval_ff<2>(P, (const double*)(m + L.ffmeta), cs, v.stage_kb)
+                          : launch_eval_ff<4>(P, (const double*)(m + L.ffmeta), cs, v.stage_kb);
     }
     return GK_ERR_ARG;
 }

@@ -18,6 +18,8 @@ INFO_DTYPE = np.dtype([("status", "<i4"), ("where", "<i4"), ("iterations", "<i4"
 
 
 def _stream():
+    from . import autotune
+    autotune.ensure_applied()
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 

@@ -295,6 +295,25 @@ gk_status gk_batch_results(const gk_batch* batch, const void* work,
                            size_t work_bytes, int32_t item, double* weights,
                            double* isovalues, gk_stream stream);
 
+/* ---------------- tile-shape autotuning -------------------------------- */
+
+/* Kernel families whose tile shape (grid points per thread, bytes per
+ * shared-memory record stage) is chosen at run time.  The table is process
+ * state on the host; gempy_gb300/autotune.py times every variant on the GPU
+ * and persists the fastest per GPU model.  Defaults: variant 0. */
+typedef enum gk_tunable {
+    GK_TUNE_EVAL_FF = 0,     /* gk_eval, GK_FF                  */
+    GK_TUNE_EVAL_F32 = 1,    /* gk_eval, GK_F32 without gradient */
+    GK_TUNE_BATCH_EVAL = 2,  /* gk_batch_run evaluation          */
+    GK_TUNE_COUNT = 3
+} gk_tunable;
+
+int32_t gk_tune_variants(void);
+gk_status gk_tune_describe(int32_t variant, int32_t* points_per_thread,
+                           int32_t* stage_kb);
+gk_status gk_tune_set(int32_t tunable, int32_t variant);
+int32_t gk_tune_get(int32_t tunable);
+
 /* Library version string (HOST). */
 const char* gk_version(void);
 

@@ -67,3 +67,15 @@ def test_invalid_arguments_rejected_before_any_launch(lib):
     assert lib.gk_build(ctypes.byref(s), 0, None, 0, None, None) == _lib.GK_ERR_ARG
     assert lib.gk_lu_factor(0, -1, None, 0, None, None, 0, None, None) == _lib.GK_ERR_ARG
     assert lib.gk_solve_mixed(0, None, 0, None, None, 1e-10, 10, None, 0, None, None) == _lib.GK_ERR_ARG
+
+
+def test_tuning_tables_are_well_formed():
+    import glob
+    import json
+    for p in glob.glob(os.path.join(ROOT, "gempy_gb300", "tuning", "*.json")):
+        t = json.load(open(p))
+        assert "gpu" in t and "choices" in t
+        for name, ch in t["choices"].items():
+            assert name in _lib.TUNABLES
+            assert 0 <= int(ch["variant"]) < 4
+            assert ch["points_per_thread"] in (2, 4) and ch["stage_kb"] in (16, 32)

@@ -85,3 +85,59 @@ def test_batch_graph_replay_is_bitwise_equal_to_eager():
         torch.cuda.synchronize()
         assert torch.equal(br.field, f0)
         assert torch.equal(br.ids, i0)
+
+
+def test_every_tile_variant_gives_the_same_field():
+    """All autotuner variants of the float-float, FP32 and batched field
+    kernels agree (tile boundaries only change the FP64 summation order)."""
+    from gempy_gb300 import _lib, autotune
+    from gempy_gb300 import kernels as K
+    from gempy_gb300.batch import BatchRunner
+    from gempy_gb300 import synthetic
+    lib = _lib.load()
+    m = synthetic.precision(resolution=(20, 18, 22))
+    (s,) = oracle_series_list(m)
+    w = kriging.solve(*kriging.build_system(s))
+    ds = K.DeviceSeries(s.dip_positions, s.dip_gradients, s.nugget_grad, s.sp_coords, s.nugget_sp,
+                        s.points_per_surface, range=s.range, c_o=s.c_o, uni_degree=s.uni_degree)
+    model = K.prepare(ds, torch.as_tensor(w, device="cuda"))
+    pts = K.Points.regular(m.interpolation_input.grid.dense_grid)
+    br = BatchRunner(_models(4))
+    saved = {t: lib.gk_tune_get(t) for t in range(3)}
+    try:
+        for prec, fam in ((K.GK_FF, _lib.GK_TUNE_EVAL_FF), (K.GK_F32, _lib.GK_TUNE_EVAL_F32)):
+            ref = None
+            for v in autotune.variants():
+                lib.gk_tune_set(fam, v["variant"])
+                f, _, _, _ = K.evaluate(ds, model, pts, prec)
+                f = f.cpu().numpy()
+                if ref is None:
+                    ref = f
+                tol = 1e-12 if prec == K.GK_FF else 1e-6
+                assert np.abs(f - ref).max() <= tol * np.abs(ref).max(), (prec, v)
+        ref = None
+        for v in autotune.variants():
+            lib.gk_tune_set(_lib.GK_TUNE_BATCH_EVAL, v["variant"])
+            br.run()
+            torch.cuda.synchronize()
+            f = br.field.cpu().numpy()
+            if ref is None:
+                ref = f
+            assert np.abs(f - ref).max() <= 1e-12 * np.abs(ref).max(), v
+    finally:
+        for t, v in saved.items():
+            lib.gk_tune_set(t, max(v, 0))
+
+
+def test_autotuner_picks_and_installs_a_variant():
+    from gempy_gb300 import _lib, autotune
+    lib = _lib.load()
+    saved = lib.gk_tune_get(_lib.GK_TUNE_EVAL_FF)
+    try:
+        table = autotune.tune(families=("eval_ff",), persist=False, reps=1)
+        ch = table["choices"]["eval_ff"]
+        assert lib.gk_tune_get(_lib.GK_TUNE_EVAL_FF) == ch["variant"]
+        assert len(ch["all_ms"]) == lib.gk_tune_variants()
+        assert ch["ms"] == min(ch["all_ms"].values()) or abs(ch["ms"] - min(ch["all_ms"].values())) < 1e-3
+    finally:
+        lib.gk_tune_set(_lib.GK_TUNE_EVAL_FF, max(saved, 0))
