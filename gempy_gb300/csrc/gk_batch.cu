@@ -25,6 +25,7 @@
 
 #include "gk_ff.cuh"
 #include "gk_kriging.cuh"
+#include "gk_cta.cuh"
 #include "gk_tune.h"
 
 namespace gk {
@@ -130,7 +131,6 @@ __global__ void __launch_bounds__(256) batch_build_kernel(const BatchDesc* __res
 // solve: one CTA per system
 // ---------------------------------------------------------------------------
 constexpr int kSolveThreads = 512;
-constexpr int kLNB = 32;
 
 template <typename T>
 __device__ __forceinline__ T block_sum(T v, T* red) {
@@ -161,165 +161,6 @@ __device__ void cta_gemv64(const double* K, int ld, int N, const double* x, cons
         if (lane == 0) y[row] = b ? b[row] - s : s;
     }
     __syncthreads();
-}
-
-// In-CTA blocked LU without pivoting of A (N x ld, FP32); returns false on a
-// zero / non-finite pivot.
-__device__ bool cta_lu_nopiv(float* A, int ld, int N, float (*Ds)[kLNB + 1], int* s_bad) {
-    const int tid = threadIdx.x, nt = blockDim.x;
-    if (tid == 0) *s_bad = 0;
-    __syncthreads();
-    for (int k = 0; k < N; k += kLNB) {
-        const int kb = min(kLNB, N - k);
-        for (int idx = tid; idx < kLNB * kLNB; idx += nt) {
-            int r = idx / kLNB, c = idx % kLNB;
-            Ds[r][c] = (r < kb && c < kb) ? A[(int64_t)(k + r) * ld + k + c] : 0.f;
-        }
-        __syncthreads();
-        for (int j = 0; j < kb; ++j) {
-            const float pv = Ds[j][j];
-            if (!(pv == pv) || pv == 0.f || !(fabsf(pv) < INFINITY)) {
-                if (tid == 0) *s_bad = 1;
-            }
-            __syncthreads();
-            if (*s_bad) return false;
-            const float inv = 1.f / pv;
-            for (int i = j + 1 + tid; i < kb; i += nt) Ds[i][j] *= inv;
-            __syncthreads();
-            const int w = kb - j - 1;
-            for (int idx = tid; idx < w * w; idx += nt) {
-                const int i = j + 1 + idx / w, c = j + 1 + idx % w;
-                Ds[i][c] -= Ds[i][j] * Ds[j][c];
-            }
-            __syncthreads();
-        }
-        for (int idx = tid; idx < kb * kb; idx += nt) {
-            int r = idx / kb, c = idx % kb;
-            A[(int64_t)(k + r) * ld + k + c] = Ds[r][c];
-        }
-        const int m = N - k - kb;
-        if (m > 0) {
-            // U12 = L11^-1 A12 (thread per column) and L21 = A21 U11^-1 (thread per row)
-            for (int c = tid; c < m; c += nt) {
-                float xv[kLNB];
-                const int64_t col = k + kb + c;
-#pragma unroll
-                for (int i = 0; i < kLNB; ++i) xv[i] = i < kb ? A[(int64_t)(k + i) * ld + col] : 0.f;
-#pragma unroll
-                for (int i = 1; i < kLNB; ++i) {
-                    float s = xv[i];
-#pragma unroll
-                    for (int q = 0; q < i; ++q) s -= Ds[i][q] * xv[q];
-                    xv[i] = s;
-                }
-#pragma unroll
-                for (int i = 0; i < kLNB; ++i)
-                    if (i < kb) A[(int64_t)(k + i) * ld + col] = xv[i];
-            }
-            for (int rr = tid; rr < m; rr += nt) {
-                float xv[kLNB];
-                float* row = A + (int64_t)(k + kb + rr) * ld + k;
-#pragma unroll
-                for (int j = 0; j < kLNB; ++j) xv[j] = j < kb ? row[j] : 0.f;
-#pragma unroll
-                for (int j = 0; j < kLNB; ++j) {
-                    if (j < kb) {
-                        float s = xv[j];
-#pragma unroll
-                        for (int q = 0; q < j; ++q) s -= xv[q] * Ds[q][j];
-                        xv[j] = s / Ds[j][j];
-                    }
-                }
-#pragma unroll
-                for (int j = 0; j < kLNB; ++j)
-                    if (j < kb) row[j] = xv[j];
-            }
-            __syncthreads();
-            // A22 -= L21 U12, 4 x 4 micro-tiles
-            const int mb = (m + 3) / 4;
-            for (int t = tid; t < mb * mb; t += nt) {
-                const int bi = t / mb, bj = t % mb;
-                float acc[4][4] = {};
-                for (int p = 0; p < kb; ++p) {
-                    float lv[4], uv[4];
-#pragma unroll
-                    for (int a = 0; a < 4; ++a) {
-                        const int rr = 4 * bi + a;
-                        lv[a] = rr < m ? A[(int64_t)(k + kb + rr) * ld + k + p] : 0.f;
-                    }
-#pragma unroll
-                    for (int c = 0; c < 4; ++c) {
-                        const int cc = 4 * bj + c;
-                        uv[c] = cc < m ? A[(int64_t)(k + p) * ld + k + kb + cc] : 0.f;
-                    }
-#pragma unroll
-                    for (int a = 0; a < 4; ++a)
-#pragma unroll
-                        for (int c = 0; c < 4; ++c) acc[a][c] = fmaf(lv[a], uv[c], acc[a][c]);
-                }
-#pragma unroll
-                for (int a = 0; a < 4; ++a) {
-                    const int rr = 4 * bi + a;
-                    if (rr >= m) continue;
-#pragma unroll
-                    for (int c = 0; c < 4; ++c) {
-                        const int cc = 4 * bj + c;
-                        if (cc < m) A[(int64_t)(k + kb + rr) * ld + k + kb + cc] -= acc[a][c];
-                    }
-                }
-            }
-        }
-        __syncthreads();
-    }
-    return true;
-}
-
-// In-CTA triangular solves with the FP32 factors, in place on t (length N):
-// forward (unit L) then backward (U), block column sweeps of kLNB.
-__device__ void cta_lu_solve(const float* A, int ld, int N, float* t, float* xs) {
-    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5;
-    for (int k = 0; k < N; k += kLNB) {
-        const int kb = min(kLNB, N - k);
-        if (wid == 0) {
-            float v = lane < kb ? t[k + lane] : 0.f;
-            for (int c = 0; c < kb; ++c) {
-                const float xc = __shfl_sync(0xffffffffu, v, c);
-                if (lane > c && lane < kb) v -= A[(int64_t)(k + lane) * ld + k + c] * xc;
-            }
-            if (lane < kb) { t[k + lane] = v; xs[lane] = v; }
-        }
-        __syncthreads();
-        for (int r = k + kb + tid; r < N; r += nt) {
-            const float* row = A + (int64_t)r * ld + k;
-            float s = 0.f;
-            for (int c = 0; c < kb; ++c) s += row[c] * xs[c];
-            t[r] -= s;
-        }
-        __syncthreads();
-    }
-    const int nblk = (N + kLNB - 1) / kLNB;
-    for (int bk = nblk - 1; bk >= 0; --bk) {
-        const int k = bk * kLNB;
-        const int kb = min(kLNB, N - k);
-        if (wid == 0) {
-            float v = lane < kb ? t[k + lane] : 0.f;
-            for (int c = kb - 1; c >= 0; --c) {
-                float mine = __shfl_sync(0xffffffffu, v, c);
-                float xc = mine / A[(int64_t)(k + c) * ld + k + c];
-                if (lane == c) v = xc;
-                if (lane < c) v -= A[(int64_t)(k + lane) * ld + k + c] * xc;
-            }
-            if (lane < kb) { t[k + lane] = v; xs[lane] = v; }
-        }
-        __syncthreads();
-        for (int r = tid; r < k; r += nt) {
-            const float* row = A + (int64_t)r * ld + k;
-            float s = 0.f;
-            for (int c = 0; c < kb; ++c) s += row[c] * xs[c];
-            t[r] -= s;
-        }
-        __syncthreads();
-    }
 }
 
 __global__ void __launch_bounds__(kSolveThreads) batch_solve_kernel(const BatchDesc* __restrict__ D, int n_sys,

@@ -22,6 +22,7 @@
 #include <cstdlib>
 
 #include "gk_common.cuh"
+#include "gk_cta.cuh"
 
 namespace gk {
 
@@ -512,14 +513,25 @@ __global__ void __launch_bounds__(256) gemm_update_kernel(T* __restrict__ A, int
 // 128 x 128 tile per CTA, 16 x 16 threads each owning an 8 x 8 block split in
 // four 4 x 4 quadrants, float4 shared-memory reads (A stored k-major), the
 // next k-slice prefetched into registers while the current one is consumed.
-__global__ void __launch_bounds__(256, 2) sgemm_update_kernel(float* __restrict__ A, int64_t lda, int64_t n, int64_t k,
-                                                           int kb) {
+// C[i][j] -= sum_p A[i][k+p] A[k+p][j] for i in [r_lo, r_hi), j in [c_lo, c_hi);
+// with diag_bs > 0 the grid's z index selects the diagonal block
+// [r_lo + z diag_bs, ...) of both ranges (block-diagonal update).
+__global__ void __launch_bounds__(256, 2) sgemm_update_kernel(float* __restrict__ A, int64_t lda, int64_t k, int kb,
+                                                              int64_t r_lo, int64_t r_hi, int64_t c_lo,
+                                                              int64_t c_hi, int diag_bs) {
     constexpr int BM = 128, BN = 128, BK = 16;
     __shared__ __align__(16) float As[2][BK][BM];
     __shared__ __align__(16) float Bs[2][BK][BN];
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-    const int64_t off = k + kb;
-    const int64_t i0 = off + (int64_t)blockIdx.y * BM, j0 = off + (int64_t)blockIdx.x * BN;
+    if (diag_bs > 0) {
+        const int64_t b0 = r_lo + (int64_t)blockIdx.z * diag_bs;
+        r_lo = c_lo = b0;
+        r_hi = c_hi = min(r_hi, b0 + diag_bs);
+    }
+    const int64_t n = r_hi;      // row bound
+    const int64_t ncol = c_hi;   // column bound
+    const int64_t i0 = r_lo + (int64_t)blockIdx.y * BM, j0 = c_lo + (int64_t)blockIdx.x * BN;
+    if (i0 >= r_hi || j0 >= c_hi) return;
     float acc[8][8];
 #pragma unroll
     for (int a = 0; a < 8; ++a)
@@ -546,11 +558,11 @@ __global__ void __launch_bounds__(256, 2) sgemm_update_kernel(float* __restrict_
         for (int h = 0; h < 2; ++h) {
             const int kk = p0 + lb_row + 8 * h;
             const int64_t gj = j0 + lb_col;
-            if (kk < kb && gj + 3 < n) {
+            if (kk < kb && gj + 3 < ncol) {
                 rb[h] = *reinterpret_cast<const float4*>(A + (k + kk) * lda + gj);
             } else {
                 float t[4];
-                for (int e = 0; e < 4; ++e) t[e] = (kk < kb && gj + e < n) ? A[(k + kk) * lda + gj + e] : 0.f;
+                for (int e = 0; e < 4; ++e) t[e] = (kk < kb && gj + e < ncol) ? A[(k + kk) * lda + gj + e] : 0.f;
                 rb[h] = make_float4(t[0], t[1], t[2], t[3]);
             }
         }
@@ -598,7 +610,7 @@ __global__ void __launch_bounds__(256, 2) sgemm_update_kernel(float* __restrict_
         for (int hb = 0; hb < 2; ++hb) {
             const int64_t gj = j0 + hb * 64 + tx * 4;
             float* c = A + gi * lda + gj;
-            if (gj + 3 < n) {
+            if (gj + 3 < ncol) {
                 float4 v = *reinterpret_cast<float4*>(c);
                 v.x -= acc[a][4 * hb + 0];
                 v.y -= acc[a][4 * hb + 1];
@@ -607,7 +619,7 @@ __global__ void __launch_bounds__(256, 2) sgemm_update_kernel(float* __restrict_
                 *reinterpret_cast<float4*>(c) = v;
             } else {
                 for (int e = 0; e < 4; ++e)
-                    if (gj + e < n) c[e] -= acc[a][4 * hb + e];
+                    if (gj + e < ncol) c[e] -= acc[a][4 * hb + e];
             }
         }
     }
@@ -981,7 +993,7 @@ static gk_status lu_factor(int64_t n, T* A, int64_t lda, int32_t* ipiv, void* wo
             dim3 grid((unsigned)((rest + BN - 1) / BN), (unsigned)((rest + BM - 1) / BM));
             if (sizeof(T) == 4 && ((k + kb) % 4) == 0 && (lda % 4) == 0 &&
                 ((uintptr_t)A % 16) == 0) {
-                sgemm_update_kernel<<<grid, 256, 0, st>>>((float*)A, lda, n, k, kb);
+                sgemm_update_kernel<<<grid, 256, 0, st>>>((float*)A, lda, k, kb, k + kb, n, k + kb, n, 0);
             } else {
                 gemm_update_kernel<T, BM, BN, 16><<<grid, 256, 0, st>>>(A, lda, n, k, kb);
             }
@@ -1025,7 +1037,7 @@ static gk_status lu_factor_nopiv(int64_t n, T* A, int64_t lda, int32_t* ipiv, vo
             constexpr int BN = BM;
             dim3 grid((unsigned)((rest + BN - 1) / BN), (unsigned)((rest + BM - 1) / BM));
             if (sizeof(T) == 4 && ((k + kb) % 4) == 0 && (lda % 4) == 0 && ((uintptr_t)A % 16) == 0) {
-                sgemm_update_kernel<<<grid, 256, 0, st>>>((float*)A, lda, n, k, kb);
+                sgemm_update_kernel<<<grid, 256, 0, st>>>((float*)A, lda, k, kb, k + kb, n, k + kb, n, 0);
             } else {
                 gemm_update_kernel<T, BM, BN, 16><<<grid, 256, 0, st>>>(A, lda, n, k, kb);
             }
@@ -1076,6 +1088,88 @@ static gk_status lu_solve(int64_t n, const T* LU, int64_t lda, const int32_t* ip
     return GK_OK;
 }
 
+// ----------------------------------------------------------------------------
+// Two-level preconditioner: block-Jacobi on a Schur complement plus a low-rank
+// (landmark) correction.
+//
+// The matrix is symmetrically permuted so that r landmark unknowns come first
+// and the remaining ones follow in spatially contiguous blocks of bs.  A
+// partial LU without pivoting over the first r columns computes
+//     [A_LL A_LR; A_RL A_RR] = [L_LL 0; L_RL I] [U_LL U_LR; 0 S],
+// but of the trailing update S = A_RR - L_RL U_LR only the bs x bs diagonal
+// blocks are formed and LU-factored (block-Jacobi on S).  Applying
+//     M^-1 = [U_LL U_LR; 0 blockdiag(S)]^-1 [L_LL 0; L_RL I]^-1
+// costs two triangular solves of order r, two rectangular products and the
+// block solves.  L_RL U_LR is the low-rank (rank r) part of the operator.
+// ----------------------------------------------------------------------------
+__global__ void __launch_bounds__(512) block_lu_kernel(float* A, int64_t lda, int64_t r, int64_t n, int bs,
+                                                       gk_info* info) {
+    __shared__ float Ds[kLNB][kLNB + 1];
+    __shared__ int s_bad;
+    const int64_t b0 = r + (int64_t)blockIdx.x * bs;
+    const int nb = (int)min((int64_t)bs, n - b0);
+    if (nb <= 0) return;
+    if (!cta_lu_nopiv(A + b0 * lda + b0, (int)lda, nb, Ds, &s_bad)) {
+        if (threadIdx.x == 0) report(info, GK_ERR_SINGULAR, (int)b0);
+    }
+}
+
+__global__ void __launch_bounds__(256) block_solve_kernel(const float* A, int64_t lda, int64_t r, int64_t n, int bs,
+                                                          float* t) {
+    __shared__ float xs[kLNB];
+    const int64_t b0 = r + (int64_t)blockIdx.x * bs;
+    const int nb = (int)min((int64_t)bs, n - b0);
+    if (nb <= 0) return;
+    cta_lu_solve(A + b0 * lda + b0, (int)lda, nb, t + b0, xs);
+}
+
+// y[i] -= sum_j A[i][j] x[j], i in [r_lo, r_hi), j in [c_lo, c_hi); warp per row
+__global__ void rect_gemv_kernel(const float* __restrict__ A, int64_t lda, int64_t r_lo, int64_t r_hi, int64_t c_lo,
+                                 int64_t c_hi, const float* __restrict__ x, float* __restrict__ y) {
+    const int64_t row = r_lo + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (row >= r_hi) return;
+    const float* a = A + row * lda;
+    float s = 0.f;
+    for (int64_t j = c_lo + lane; j < c_hi; j += 32) s = fmaf(a[j], x[j], s);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) y[row] -= s;
+}
+
+__global__ void permute_scale_kernel(const double* __restrict__ K, int64_t ldk, int64_t n,
+                                     const int32_t* __restrict__ perm, const double* __restrict__ d,
+                                     float* __restrict__ A, int64_t lda) {
+    const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (row >= n) return;
+    const int64_t pi = perm[row];
+    const double di = d[pi];
+    const double* k = K + pi * ldk;
+    float* a = A + row * lda;
+    for (int64_t j = lane; j < n; j += 32) {
+        const int64_t pj = perm[j];
+        a[j] = (float)(di * k[pj] * d[pj]);
+    }
+}
+
+__global__ void gather_scale_kernel(const double* __restrict__ v, const int32_t* __restrict__ perm,
+                                    const double* __restrict__ d, int64_t n, float* __restrict__ t) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const int64_t p = perm[i];
+        t[i] = (float)(d[p] * v[p]);
+    }
+}
+
+__global__ void scatter_scale_kernel(const float* __restrict__ t, const int32_t* __restrict__ perm,
+                                     const double* __restrict__ d, int64_t n, double* __restrict__ z) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const int64_t p = perm[i];
+        z[p] = d[p] * (double)t[i];
+    }
+}
+
 }  // namespace gk
 
 using namespace gk;
@@ -1111,6 +1205,90 @@ gk_status gk_internal_lu_solve_f32(int64_t n, const float* LU, int64_t lda, cons
     return lu_solve<float>(n, LU, lda, ipiv, b, work, wb, info, st);
 }
 size_t gk_internal_lu_ws_f32(int64_t n) { return lu_ws_bytes<float>(n); }
+// Two-level setup: A (n x lda, FP32) <- P D K D P^T, partial LU over the first
+// r columns with restricted updates, LU of the Schur diagonal blocks, and the
+// inverses of the 128 x 128 diagonal blocks of L_LL / U_LL for the solves.
+gk_status gk_internal_twolevel_setup(int64_t n, const double* K, int64_t ldk, const int32_t* perm, const double* d,
+                                     int64_t r, int bs, float* A, int64_t lda, int32_t* ipiv, void* work,
+                                     size_t wbytes, gk_info* info, cudaStream_t st) {
+    constexpr int NB = LuCfg<float>::NB;
+    if (n <= 0 || r <= 0 || r >= n || bs <= 0 || (r % NB) != 0 || (bs % 64) != 0 || (lda % 4) != 0 ||
+        ((uintptr_t)A % 16) != 0)
+        return GK_ERR_ARG;
+    if (work == nullptr || wbytes < lu_ws_bytes<float>(n)) return GK_ERR_SIZE;
+    permute_scale_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, st>>>(K, ldk, n, perm, d, A, lda);
+    GK_LAUNCH_CHECK();
+    const int64_t nblk = (n - r + bs - 1) / bs;
+    for (int64_t k = 0; k < r; k += NB) {
+        const int kb = (int)min((int64_t)NB, r - k);
+        diag_lu_kernel<float, NB><<<1, 256, 0, st>>>(A, lda, k, kb, ipiv, info);
+        GK_LAUNCH_CHECK();
+        const int64_t rest = n - k - kb;
+        trsm_right_kernel<float, NB><<<(unsigned)((rest + 63) / 64), 64, 0, st>>>(A, lda, n, k, kb);
+        GK_LAUNCH_CHECK();
+        trsm_kernel<float, NB><<<(unsigned)((rest + 127) / 128), 128, 0, st>>>(A, lda, n, k, kb);
+        GK_LAUNCH_CHECK();
+        const int64_t o = k + kb;
+        if (o < r) {
+            // landmark rows, all columns to the right
+            dim3 ga((unsigned)((n - o + 127) / 128), (unsigned)((r - o + 127) / 128));
+            sgemm_update_kernel<<<ga, 256, 0, st>>>(A, lda, k, kb, o, r, o, n, 0);
+            GK_LAUNCH_CHECK();
+            // remaining rows, landmark columns
+            dim3 gb((unsigned)((r - o + 127) / 128), (unsigned)((n - r + 127) / 128));
+            sgemm_update_kernel<<<gb, 256, 0, st>>>(A, lda, k, kb, r, n, o, r, 0);
+            GK_LAUNCH_CHECK();
+        }
+        // diagonal blocks of the Schur complement
+        dim3 gc((unsigned)((bs + 127) / 128), (unsigned)((bs + 127) / 128), (unsigned)nblk);
+        sgemm_update_kernel<<<gc, 256, 0, st>>>(A, lda, k, kb, r, n, r, n, bs);
+        GK_LAUNCH_CHECK();
+    }
+    block_lu_kernel<<<(unsigned)nblk, 512, 0, st>>>(A, lda, r, n, bs, info);
+    GK_LAUNCH_CHECK();
+    const size_t ysmem = (size_t)kTB * kTB * sizeof(float);
+    GK_CUDA_TRY(cudaFuncSetAttribute(tri_inv_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ysmem));
+    tri_inv_kernel<float><<<(unsigned)((r + kTB - 1) / kTB), kTB, ysmem, st>>>(A, lda, r, lu_ws_dinv<float>(work, r, 0),
+                                                                              lu_ws_dinv<float>(work, r, 1), info);
+    GK_LAUNCH_CHECK();
+    return GK_OK;
+}
+
+// z = M^-1 v (FP64 in/out; FP32 inside).  t: n floats of scratch.
+gk_status gk_internal_twolevel_apply(int64_t n, const float* A, int64_t lda, const int32_t* perm, const double* d,
+                                     int64_t r, int bs, const double* v, double* z, float* t, void* work,
+                                     size_t wbytes, gk_info* info, cudaStream_t st) {
+    const unsigned vb = (unsigned)((n + 255) / 256);
+    gather_scale_kernel<<<vb, 256, 0, st>>>(v, perm, d, n, t);
+    GK_LAUNCH_CHECK();
+    // forward: L_LL w_L = t_L, then t_R -= L_RL w_L
+    int sms = device_sm_count();
+    // flags and diagonal inverses both use the workspace layout of order r
+    char* p = (char*)work + panel_ws_bytes<float, LuCfg<float>::NB>(sms);
+    p += align256((size_t)(r + 1) * sizeof(int32_t)) * 2;
+    const int nblk_r = (int)((r + kTB - 1) / kTB);
+    int* flags = (int*)p;
+    int* counter = flags + (size_t)nblk_r * kFlagStride;
+    GK_CUDA_TRY(cudaMemsetAsync(flags, 0, ((size_t)nblk_r + 1) * kFlagStride * sizeof(int), st));
+    trsv_kernel<float><<<nblk_r, 256, 0, st>>>(A, lda, r, t, lu_ws_dinv<float>(work, r, 0), 1, counter, flags, info);
+    GK_LAUNCH_CHECK();
+    rect_gemv_kernel<<<(unsigned)(((n - r) * 32 + 255) / 256), 256, 0, st>>>(A, lda, r, n, 0, r, t, t);
+    GK_LAUNCH_CHECK();
+    // block-Jacobi on the Schur complement
+    const int64_t nblk = (n - r + bs - 1) / bs;
+    block_solve_kernel<<<(unsigned)nblk, 256, 0, st>>>(A, lda, r, n, bs, t);
+    GK_LAUNCH_CHECK();
+    // backward: t_L -= U_LR x_R, then U_LL x_L = t_L
+    rect_gemv_kernel<<<(unsigned)((r * 32 + 255) / 256), 256, 0, st>>>(A, lda, 0, r, r, n, t, t);
+    GK_LAUNCH_CHECK();
+    GK_CUDA_TRY(cudaMemsetAsync(flags, 0, ((size_t)nblk_r + 1) * kFlagStride * sizeof(int), st));
+    trsv_kernel<float><<<nblk_r, 256, 0, st>>>(A, lda, r, t, lu_ws_dinv<float>(work, r, 1), 0, counter, flags, info);
+    GK_LAUNCH_CHECK();
+    scatter_scale_kernel<<<vb, 256, 0, st>>>(t, perm, d, n, z);
+    GK_LAUNCH_CHECK();
+    return GK_OK;
+}
+
 gk_status gk_internal_lu_factor_nopiv_f32(int64_t n, float* A, int64_t lda, int32_t* ipiv, void* work, size_t wb,
                                           gk_info* info, cudaStream_t st) {
     return lu_factor_nopiv<float>(n, A, lda, ipiv, work, wb, info, st);

@@ -25,6 +25,12 @@ gk_status gk_internal_lu_solve_f32(int64_t n, const float* LU, int64_t lda, cons
 size_t gk_internal_lu_ws_f32(int64_t n);
 gk_status gk_internal_lu_factor_nopiv_f32(int64_t n, float* A, int64_t lda, int32_t* ipiv, void* work, size_t wb,
                                           gk_info* info, cudaStream_t st);
+gk_status gk_internal_twolevel_setup(int64_t n, const double* K, int64_t ldk, const int32_t* perm, const double* d,
+                                     int64_t r, int bs, float* A, int64_t lda, int32_t* ipiv, void* work,
+                                     size_t wbytes, gk_info* info, cudaStream_t st);
+gk_status gk_internal_twolevel_apply(int64_t n, const float* A, int64_t lda, const int32_t* perm, const double* d,
+                                     int64_t r, int bs, const double* v, double* z, float* t, void* work,
+                                     size_t wbytes, gk_info* info, cudaStream_t st);
 
 namespace gk {
 
@@ -200,6 +206,11 @@ struct Solver {
     gk_info* info;
     cudaStream_t st;
     unsigned vb, rb;
+    // preconditioner: 0 = FP32 LU of the equilibrated K, 1 = two-level
+    int mode = 0;
+    const int32_t* perm = nullptr;
+    int64_t r = 0;
+    int bs = 0;
 
     // dot products h[0..ncol) = V[0..ncol)^T v  (accumulate: h += ...)
     gk_status dots(const double* V, int ncol, const double* v, double* h, int accumulate) {
@@ -217,8 +228,11 @@ struct Solver {
         out = sqrt(out);
         return GK_OK;
     }
-    // z = D LU32^-1 D v
+    // z = D LU32^-1 D v, or the two-level preconditioner
     gk_status precond(const double* v, double* z) {
+        if (mode == 1)
+            return gk_internal_twolevel_apply(n, w.K32, ld32, perm, w.d, r, bs, v, z, w.t32, w.luw, w.luw_bytes,
+                                              info, st);
         scale_to_f32_kernel<<<vb, 256, 0, st>>>(v, w.d, n, w.t32);
         GK_LAUNCH_CHECK();
         gk_status s = gk_internal_lu_solve_f32(n, w.K32, ld32, w.ipiv, w.t32, w.luw, w.luw_bytes, info, st);
@@ -231,48 +245,23 @@ struct Solver {
 
 }  // namespace
 
-extern "C" gk_status gk_solve_mixed(int64_t n, const double* K, int64_t ldk, const double* b, double* x, double tol,
-                                    int32_t max_iter, void* work, size_t work_bytes, gk_info* info,
-                                    gk_stream stream) {
-    cudaStream_t st = (cudaStream_t)stream;
-    if (n <= 0 || K == nullptr || b == nullptr || x == nullptr || ldk < n || max_iter < 1) return GK_ERR_ARG;
-    if (work == nullptr || work_bytes < mixed_bytes(n)) return GK_ERR_SIZE;
-    Solver S;
-    S.n = n; S.K = K; S.ldk = ldk; S.w = carve(work, n); S.ld32 = ld32_of(n); S.st = st;
-    if (info == nullptr) info = S.w.iinfo;
-    S.info = info;
-    S.vb = (unsigned)((n + 255) / 256);
-    S.rb = (unsigned)((n * 32 + 255) / 256);
+// Restarted FGMRES(kRestart) in FP64 with right preconditioning S.precond;
+// convergence tested on the host between Arnoldi steps.
+static gk_status fgmres(Solver& S, const double* b, double* x, double tol, int max_iter, int& status, int& its,
+                        double& rel) {
     MixedWork& w = S.w;
-    GK_CUDA_TRY(cudaMemsetAsync(info, 0, sizeof(gk_info), st));
-    equil_kernel<<<S.rb, 256, 0, st>>>(K, ldk, n, w.d);
-    GK_LAUNCH_CHECK();
-    dim3 cg((unsigned)((n + 255) / 256), (unsigned)(n < 4096 ? n : 4096));
-    convert_kernel<<<cg, 256, 0, st>>>(K, ldk, n, w.d, w.K32, S.ld32);
-    GK_LAUNCH_CHECK();
-    // FP32 LU of the equilibrated matrix: first without pivoting (no inter-CTA
-    // pivot exchange); on a zero / non-finite pivot, again with partial pivoting.
-    gk_status s = gk_internal_lu_factor_nopiv_f32(n, w.K32, S.ld32, w.ipiv, w.luw, w.luw_bytes, info, st);
-    if (s != GK_OK) return s;
-    int pivoted = 0;
-    {
-        int32_t fst = 0;
-        GK_CUDA_TRY(cudaMemcpyAsync(&fst, &info->status, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-        GK_CUDA_TRY(cudaStreamSynchronize(st));
-        if (fst != 0) {
-            convert_kernel<<<cg, 256, 0, st>>>(K, ldk, n, w.d, w.K32, S.ld32);
-            GK_LAUNCH_CHECK();
-            s = gk_internal_lu_factor_f32(n, w.K32, S.ld32, w.ipiv, w.luw, w.luw_bytes, info, st);
-            if (s != GK_OK) return s;
-            pivoted = 1;
-        }
-    }
-
+    const int64_t n = S.n;
+    const double* K = S.K;
+    const int64_t ldk = S.ldk;
+    cudaStream_t st = S.st;
+    gk_status s;
     double bnorm = 0.0;
     if ((s = S.norm2(b, bnorm)) != GK_OK) return s;
     GK_CUDA_TRY(cudaMemsetAsync(x, 0, n * sizeof(double), st));
-    int status = GK_ERR_NOT_CONVERGED, its = 0;
-    double rel = 1.0, prev_true = INFINITY;
+    status = GK_ERR_NOT_CONVERGED;
+    its = 0;
+    rel = 1.0;
+    double prev_true = INFINITY;
     if (!(bnorm > 0.0)) {
         status = bnorm == 0.0 ? GK_OK : GK_ERR_NONFINITE;
         rel = 0.0;
@@ -355,6 +344,49 @@ extern "C" gk_status gk_solve_mixed(int64_t n, const double* K, int64_t ldk, con
         rel = beta / bnorm;
         if (rel <= tol) status = GK_OK;
     }
+    return GK_OK;
+}
+
+extern "C" gk_status gk_solve_mixed(int64_t n, const double* K, int64_t ldk, const double* b, double* x, double tol,
+                                    int32_t max_iter, void* work, size_t work_bytes, gk_info* info,
+                                    gk_stream stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (n <= 0 || K == nullptr || b == nullptr || x == nullptr || ldk < n || max_iter < 1) return GK_ERR_ARG;
+    if (work == nullptr || work_bytes < mixed_bytes(n)) return GK_ERR_SIZE;
+    Solver S;
+    S.n = n; S.K = K; S.ldk = ldk; S.w = carve(work, n); S.ld32 = ld32_of(n); S.st = st;
+    if (info == nullptr) info = S.w.iinfo;
+    S.info = info;
+    S.vb = (unsigned)((n + 255) / 256);
+    S.rb = (unsigned)((n * 32 + 255) / 256);
+    MixedWork& w = S.w;
+    GK_CUDA_TRY(cudaMemsetAsync(info, 0, sizeof(gk_info), st));
+    equil_kernel<<<S.rb, 256, 0, st>>>(K, ldk, n, w.d);
+    GK_LAUNCH_CHECK();
+    dim3 cg((unsigned)((n + 255) / 256), (unsigned)(n < 4096 ? n : 4096));
+    convert_kernel<<<cg, 256, 0, st>>>(K, ldk, n, w.d, w.K32, S.ld32);
+    GK_LAUNCH_CHECK();
+    // FP32 LU of the equilibrated matrix: first without pivoting (no inter-CTA
+    // pivot exchange); on a zero / non-finite pivot, again with partial pivoting.
+    gk_status s = gk_internal_lu_factor_nopiv_f32(n, w.K32, S.ld32, w.ipiv, w.luw, w.luw_bytes, info, st);
+    if (s != GK_OK) return s;
+    int pivoted = 0;
+    {
+        int32_t fst = 0;
+        GK_CUDA_TRY(cudaMemcpyAsync(&fst, &info->status, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+        GK_CUDA_TRY(cudaStreamSynchronize(st));
+        if (fst != 0) {
+            convert_kernel<<<cg, 256, 0, st>>>(K, ldk, n, w.d, w.K32, S.ld32);
+            GK_LAUNCH_CHECK();
+            s = gk_internal_lu_factor_f32(n, w.K32, S.ld32, w.ipiv, w.luw, w.luw_bytes, info, st);
+            if (s != GK_OK) return s;
+            pivoted = 1;
+        }
+    }
+
+    int status = GK_ERR_NOT_CONVERGED, its = 0;
+    double rel = 1.0;
+    if ((s = fgmres(S, b, x, tol, max_iter, status, its, rel)) != GK_OK) return s;
     {
         gk_info hi;
         GK_CUDA_TRY(cudaMemcpyAsync(&hi, info, sizeof(gk_info), cudaMemcpyDeviceToHost, st));
@@ -366,6 +398,58 @@ extern "C" gk_status gk_solve_mixed(int64_t n, const double* K, int64_t ldk, con
         GK_CUDA_TRY(cudaMemcpyAsync(info, &hi, sizeof(gk_info), cudaMemcpyHostToDevice, st));
         GK_CUDA_TRY(cudaStreamSynchronize(st));
     }
+    return GK_OK;
+}
+
+// ---------------------------------------------------------------------------
+// FGMRES with the two-level (block-Jacobi + low-rank) preconditioner
+// ---------------------------------------------------------------------------
+extern "C" size_t gk_solve_twolevel_workspace_bytes(int64_t n) { return n > 0 ? mixed_bytes(n) : 0; }
+
+extern "C" gk_status gk_solve_twolevel(int64_t n, const double* K, int64_t ldk, const double* b, double* x,
+                                       const int32_t* perm, int64_t r, int32_t bs, double tol, int32_t max_iter,
+                                       void* work, size_t work_bytes, gk_info* info, gk_stream stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (n <= 0 || K == nullptr || b == nullptr || x == nullptr || perm == nullptr || ldk < n || max_iter < 1)
+        return GK_ERR_ARG;
+    if (r <= 0 || r >= n || (r % 64) != 0 || bs <= 0 || (bs % 64) != 0) return GK_ERR_ARG;
+    if (work == nullptr || work_bytes < mixed_bytes(n)) return GK_ERR_SIZE;
+    Solver S;
+    S.n = n; S.K = K; S.ldk = ldk; S.w = carve(work, n); S.ld32 = ld32_of(n); S.st = st;
+    if (info == nullptr) info = S.w.iinfo;
+    S.info = info;
+    S.vb = (unsigned)((n + 255) / 256);
+    S.rb = (unsigned)((n * 32 + 255) / 256);
+    S.mode = 1;
+    S.perm = perm;
+    S.r = r;
+    S.bs = bs;
+    MixedWork& w = S.w;
+    GK_CUDA_TRY(cudaMemsetAsync(info, 0, sizeof(gk_info), st));
+    equil_kernel<<<S.rb, 256, 0, st>>>(K, ldk, n, w.d);
+    GK_LAUNCH_CHECK();
+    gk_status s = gk_internal_twolevel_setup(n, K, ldk, perm, w.d, r, bs, w.K32, S.ld32, w.ipiv, w.luw, w.luw_bytes,
+                                             info, st);
+    if (s != GK_OK) return s;
+    int32_t fst = 0;
+    GK_CUDA_TRY(cudaMemcpyAsync(&fst, &info->status, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    GK_CUDA_TRY(cudaStreamSynchronize(st));
+    int status = GK_ERR_NOT_CONVERGED, its = 0;
+    double rel = 1.0;
+    if (fst == 0) {
+        if ((s = fgmres(S, b, x, tol, max_iter, status, its, rel)) != GK_OK) return s;
+    } else {
+        status = fst;
+    }
+    gk_info hi;
+    GK_CUDA_TRY(cudaMemcpyAsync(&hi, info, sizeof(gk_info), cudaMemcpyDeviceToHost, st));
+    GK_CUDA_TRY(cudaStreamSynchronize(st));
+    if (hi.status == 0 && status != GK_OK) hi.status = status;
+    hi.iterations = its;
+    hi.pivoted = 0;
+    hi.residual = rel;
+    GK_CUDA_TRY(cudaMemcpyAsync(info, &hi, sizeof(gk_info), cudaMemcpyHostToDevice, st));
+    GK_CUDA_TRY(cudaStreamSynchronize(st));
     return GK_OK;
 }
 

@@ -176,6 +176,65 @@ def solve_mixed(series: DeviceSeries, tol=1e-12, max_iter=30, K=None, b=None):
     return x, info
 
 
+def unknown_positions(series: DeviceSeries):
+    """Position of every unknown: orientation position for gradient rows, rest
+    point for interface rows (drift rows: the centroid)."""
+    xo = series.dip_positions.cpu().numpy()
+    sp = series.sp_coords.cpu().numpy()
+    rest = series.rest_index.cpu().numpy()
+    nd = series.N - 3 * len(xo) - len(rest)
+    pos = np.concatenate([np.tile(xo, (3, 1)), sp[rest], np.repeat(sp.mean(0, keepdims=True), nd, 0)])
+    return pos, nd
+
+
+def morton_codes(p):
+    p = np.asarray(p, dtype=np.float64)
+    q = ((p - p.min(0)) / (np.ptp(p, 0) + 1e-300) * 1023).astype(np.int64)
+    code = np.zeros(len(p), dtype=np.int64)
+    for bit in range(10):
+        for d in range(3):
+            code |= ((q[:, d] >> bit) & 1) << (3 * bit + d)
+    return code
+
+
+def twolevel_permutation(series: DeviceSeries, n_landmarks, seed=0):
+    """(perm, r): r = landmark count rounded up to a multiple of 64 (uniformly
+    sampled covariance unknowns plus every drift unknown) placed first, the
+    other unknowns after them in Morton (Z-curve) order of their positions."""
+    pos, nd = unknown_positions(series)
+    N = len(pos)
+    nc = N - nd
+    r = int(min(max(64, -(-(int(n_landmarks) + nd) // 64) * 64), (N - 1) // 64 * 64))
+    rng = np.random.default_rng(seed)
+    land = np.sort(rng.choice(nc, r - nd, replace=False))
+    mask = np.ones(N, dtype=bool)
+    mask[land] = False
+    mask[nc:] = False
+    rest = np.nonzero(mask)[0]
+    rest = rest[np.argsort(morton_codes(pos[rest]), kind="stable")]
+    perm = np.concatenate([land, np.arange(nc, N), rest]).astype(np.int32)
+    return perm, r
+
+
+def solve_twolevel(series: DeviceSeries, n_landmarks=1024, block=512, tol=1e-8, max_iter=2000, K=None, b=None,
+                   seed=0):
+    """FGMRES with the two-level (block-Jacobi + low-rank) preconditioner."""
+    lib = _lib.load()
+    if K is None:
+        K, b = build(series, GK_F64)
+    n = K.shape[0]
+    perm, r = twolevel_permutation(series, n_landmarks, seed)
+    pt = torch.as_tensor(perm).to(K.device)
+    wb = lib.gk_solve_twolevel_workspace_bytes(n)
+    work = torch.empty(wb, dtype=torch.uint8, device=K.device)
+    x = torch.empty(n, dtype=torch.float64, device=K.device)
+    info = new_info(K.device)
+    check("gk_solve_twolevel", lib.gk_solve_twolevel(n, _ptr(K), K.stride(0), _ptr(b), _ptr(x), _ptr(pt), r,
+                                                     int(block), float(tol), int(max_iter), _ptr(work), wb,
+                                                     _ptr(info), _stream()))
+    return x, info, r
+
+
 def prepare(series: DeviceSeries, w):
     lib = _lib.load()
     nb = lib.gk_eval_model_bytes(ctypes.byref(series.sys))

@@ -166,6 +166,25 @@ gk_status gk_solve_mixed(int64_t n, const double* K, int64_t ldk,
                          int32_t max_iter, void* work, size_t work_bytes,
                          gk_info* info, gk_stream stream);
 
+/* FGMRES on the FP64 system K x = b preconditioned by a two-level
+ * "block-Jacobi plus low-rank" operator, for systems too large for an LU
+ * preconditioner (no reference counterpart beyond the FP64 solve it
+ * replaces).  ``perm`` (device, n entries) lists the unknowns in the new order:
+ * first ``r`` landmark unknowns (r a multiple of 64; the drift unknowns must be
+ * among them), then the others in spatially contiguous blocks of ``bs`` (a
+ * multiple of 64).  Setup, all FP32 on the equilibrated, permuted matrix: LU
+ * without pivoting of the landmark block, the landmark rows/columns
+ * (the rank-r coupling), and LU of the bs x bs diagonal blocks of the Schur
+ * complement.  The Krylov iteration is FP64 on the FP64 K, to
+ * ||b - K x||_2 <= tol ||b||_2 or ``max_iter`` steps; ``info`` reports status,
+ * iterations and the final residual.  Workspace as gk_solve_mixed. */
+size_t gk_solve_twolevel_workspace_bytes(int64_t n);
+gk_status gk_solve_twolevel(int64_t n, const double* K, int64_t ldk,
+                            const double* b, double* x, const int32_t* perm,
+                            int64_t r, int32_t bs, double tol, int32_t max_iter,
+                            void* work, size_t work_bytes, gk_info* info,
+                            gk_stream stream);
+
 /* Allocation-free form of gk_solve_mixed, with no counterpart in the
  * reference.  It is for callers that cannot call cudaMalloc -- for example
  * code running inside a framework that owns the whole device-memory budget

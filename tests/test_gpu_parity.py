@@ -385,3 +385,27 @@ def test_mixed_solve_without_pivoting_on_kriging_matrix():
     x, info = _mixed_solve_raw(Kr, br)
     assert info["pivoted"] == 0
     assert np.linalg.norm(br - Kr @ x) <= 1e-11 * np.linalg.norm(br)
+
+
+@pytest.mark.parametrize("n_land,block", [(256, 64), (512, 128), (1024, 256)])
+def test_twolevel_fgmres_judged_by_fp64_lu(n_land, block):
+    """Block-Jacobi + low-rank preconditioned FGMRES reaches 1e-8; the FP64 LU
+    (plain form) judges the solution."""
+    from gempy_gb300 import kernels as K
+    from gempy_gb300 import synthetic
+    m = synthetic.learned(n_points=1500, n_orient=400, n_surf=5)
+    (s,) = oracle_series_list(m)
+    ds = _dev_series(s)
+    Kt, bt = K.build(ds, K.GK_F64)
+    x, info, r = K.solve_twolevel(ds, n_landmarks=n_land, block=block, tol=1e-8, K=Kt, b=bt)
+    inf = K.read_info(info)
+    assert inf["status"] == 0, inf
+    assert inf["residual"] <= 1e-8
+    w_lu, _ = K.solve_plain(ds)
+    x, w_lu = x.cpu().numpy(), w_lu.cpu().numpy()
+    Kr, br = kriging.build_system(s)
+    assert np.linalg.norm(br - Kr @ x) <= 1.01e-8 * np.linalg.norm(br)
+    # the judge: fields from both weight vectors agree
+    pts = np.random.default_rng(0).uniform(-0.45, 0.45, (2000, 3))
+    z_tl, z_lu = kriging.evaluate(s, x, pts), kriging.evaluate(s, w_lu, pts)
+    assert np.abs(z_tl - z_lu).max() <= 1e-4 * np.abs(z_lu).max()
