@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(kSolveThreads) batch_solve_kernel(const BatchD
                 rel = beta / bn;
                 if (!(rel == rel)) { status = GK_ERR_NONFINITE; break; }
                 if (rel <= tol) { status = GK_OK; break; }
-                if (rel > 0.5 * prev) break;
+                if (rel > 0.98 * prev) break;
                 prev = rel;
                 for (int i = tid; i < N; i += nt) d.V[i] = d.r[i] / beta;
                 if (tid == 0) { for (int q = 0; q <= kBatchRestart; ++q) g[q] = 0.0; g[0] = beta; }

@@ -37,7 +37,7 @@ namespace gk {
 static size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
 static int64_t ld32_of(int64_t n) { return (n + 63) / 64 * 64; }
 
-constexpr int kRestart = 30;
+constexpr int kRestart = 50;
 constexpr int kDotBlocks = 128;
 
 struct MixedWork {
@@ -277,7 +277,8 @@ static gk_status fgmres(Solver& S, const double* b, double* x, double tol, int m
         rel = beta / bnorm;
         if (!std::isfinite(rel)) { status = GK_ERR_NONFINITE; break; }
         if (rel <= tol) { status = GK_OK; break; }
-        if (rel > 0.5 * prev_true) break;  // restart made no progress: stagnated at the FP64 floor
+        // a whole restart cycle gained less than 2%: stagnated (FP64 floor or a weak preconditioner)
+        if (rel > 0.98 * prev_true) break;
         prev_true = rel;
         scale_kernel<<<S.vb, 256, 0, st>>>(w.r, 1.0 / beta, n, w.V);
         GK_LAUNCH_CHECK();

@@ -155,7 +155,7 @@ gk_status gk_lu_solve(gk_prec prec, int64_t n, const void* LU, int64_t lda,
  * (the equilibrated covariance block is SPD with unit diagonal; the drift
  * block comes last), or with partial pivoting if a pivot is zero or
  * non-finite -- and preconditions an
- * FP64 restarted FGMRES(30) whose residuals r = b - K x use the FP64 K, until
+ * FP64 restarted FGMRES(50) whose residuals r = b - K x use the FP64 K, until
  * ||r||_2 <= tol ||b||_2, stagnation, or ``max_iter`` Krylov steps.  ``work``
  * holds the FP32 factors and the Krylov vectors
  * (gk_solve_mixed_workspace_bytes); ``info`` receives the status, the
