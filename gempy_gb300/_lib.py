@@ -72,6 +72,22 @@ class GkBatch(ctypes.Structure):
                 ("ref_index", ctypes.c_void_p), ("rest_index", ctypes.c_void_p)]
 
 
+GK_MLP_HIDDEN = 256
+GK_MLP_MAX_IN = 64
+GK_MLP_MAX_OUT = 16
+GK_MLP_MAX_BATCH = 1 << 22
+GK_SYSTEM_FEATURES = 16
+
+
+class GkMlp(ctypes.Structure):
+    _fields_ = [("in_dim", ctypes.c_int32), ("out_dim", ctypes.c_int32), ("params", ctypes.c_void_p)]
+
+
+class GkAdam(ctypes.Structure):
+    _fields_ = [("lr", ctypes.c_float), ("beta1", ctypes.c_float), ("beta2", ctypes.c_float),
+                ("eps", ctypes.c_float), ("weight_decay", ctypes.c_float)]
+
+
 # (name, restype, argtypes) of every exported symbol; tests check the header
 # declares exactly these.
 SIGNATURES = [
@@ -92,11 +108,11 @@ SIGNATURES = [
     ("gk_solve_mixed_noalloc", ctypes.c_int, [ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                               ctypes.c_void_p, ctypes.c_double, ctypes.c_int32, ctypes.c_void_p,
                                               ctypes.c_void_p]),
-    ("gk_solve_twolevel_workspace_bytes", ctypes.c_size_t, [ctypes.c_int64]),
+    ("gk_solve_twolevel_workspace_bytes", ctypes.c_size_t, [ctypes.c_int64, ctypes.c_int]),
     ("gk_solve_twolevel", ctypes.c_int, [ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32,
-                                         ctypes.c_double, ctypes.c_int32, ctypes.c_void_p, ctypes.c_size_t,
-                                         ctypes.c_void_p, ctypes.c_void_p]),
+                                         ctypes.c_int, ctypes.c_double, ctypes.c_int32, ctypes.c_void_p,
+                                         ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]),
     ("gk_eval_model_bytes", ctypes.c_size_t, [ctypes.POINTER(GkSystem)]),
     ("gk_eval_prepare", ctypes.c_int, [ctypes.POINTER(GkSystem), ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_void_p]),
@@ -124,6 +140,18 @@ SIGNATURES = [
     ("gk_tune_describe", ctypes.c_int, [ctypes.c_int32, c_int32_p, c_int32_p]),
     ("gk_tune_set", ctypes.c_int, [ctypes.c_int32, ctypes.c_int32]),
     ("gk_tune_get", ctypes.c_int32, [ctypes.c_int32]),
+    ("gk_mlp_param_count", ctypes.c_int64, [ctypes.c_int32, ctypes.c_int32]),
+    ("gk_mlp_workspace_bytes", ctypes.c_size_t, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int64]),
+    ("gk_mlp_fwd", ctypes.c_int, [ctypes.POINTER(GkMlp), ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+                                  ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("gk_mlp_bwd", ctypes.c_int, [ctypes.POINTER(GkMlp), ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("gk_mlp_mse", ctypes.c_int, [ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    ("gk_mlp_adam", ctypes.c_int, [ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(GkAdam), ctypes.c_int32,
+                                   ctypes.c_void_p]),
+    ("gk_system_features", ctypes.c_int, [ctypes.POINTER(GkSystem), ctypes.c_void_p, ctypes.c_void_p]),
     ("gk_version", ctypes.c_char_p, []),
     ("gk_launch_count", ctypes.c_uint64, []),
 ]

@@ -1,6 +1,6 @@
 // In-CTA dense kernels shared by the batched solver (gk_batch.cu) and the
 // two-level preconditioner (gk_lu.cu): blocked LU without pivoting of an
-// FP32 matrix in global memory by one CTA, and the matching triangular solves.
+// FP32 or FP64 matrix in global memory by one CTA, and the matching triangular solves.
 #pragma once
 
 #include "gk_common.cuh"
@@ -9,9 +9,15 @@ namespace gk {
 
 constexpr int kLNB = 32;
 
-// In-CTA blocked LU without pivoting of A (N x ld, FP32); returns false on a
+template <typename T> __device__ __forceinline__ T cta_fma(T a, T b, T c);
+template <> __device__ __forceinline__ float cta_fma(float a, float b, float c) { return fmaf(a, b, c); }
+template <> __device__ __forceinline__ double cta_fma(double a, double b, double c) { return fma(a, b, c); }
+template <typename T> __device__ __forceinline__ T cta_abs(T x) { return x < (T)0 ? -x : x; }
+
+// In-CTA blocked LU without pivoting of A (N x ld, FP32 or FP64); returns false on a
 // zero / non-finite pivot.
-static __device__ bool cta_lu_nopiv(float* A, int ld, int N, float (*Ds)[kLNB + 1], int* s_bad) {
+template <typename T>
+static __device__ bool cta_lu_nopiv(T* A, int ld, int N, T (*Ds)[kLNB + 1], int* s_bad) {
     const int tid = threadIdx.x, nt = blockDim.x;
     if (tid == 0) *s_bad = 0;
     __syncthreads();
@@ -19,17 +25,17 @@ static __device__ bool cta_lu_nopiv(float* A, int ld, int N, float (*Ds)[kLNB + 
         const int kb = min(kLNB, N - k);
         for (int idx = tid; idx < kLNB * kLNB; idx += nt) {
             int r = idx / kLNB, c = idx % kLNB;
-            Ds[r][c] = (r < kb && c < kb) ? A[(int64_t)(k + r) * ld + k + c] : 0.f;
+            Ds[r][c] = (r < kb && c < kb) ? A[(int64_t)(k + r) * ld + k + c] : (T)0;
         }
         __syncthreads();
         for (int j = 0; j < kb; ++j) {
-            const float pv = Ds[j][j];
-            if (!(pv == pv) || pv == 0.f || !(fabsf(pv) < INFINITY)) {
+            const T pv = Ds[j][j];
+            if (!(pv == pv) || pv == (T)0 || !(cta_abs(pv) < (T)INFINITY)) {
                 if (tid == 0) *s_bad = 1;
             }
             __syncthreads();
             if (*s_bad) return false;
-            const float inv = 1.f / pv;
+            const T inv = (T)1 / pv;
             for (int i = j + 1 + tid; i < kb; i += nt) Ds[i][j] *= inv;
             __syncthreads();
             const int w = kb - j - 1;
@@ -47,13 +53,13 @@ static __device__ bool cta_lu_nopiv(float* A, int ld, int N, float (*Ds)[kLNB + 
         if (m > 0) {
             // U12 = L11^-1 A12 (thread per column) and L21 = A21 U11^-1 (thread per row)
             for (int c = tid; c < m; c += nt) {
-                float xv[kLNB];
+                T xv[kLNB];
                 const int64_t col = k + kb + c;
 #pragma unroll
-                for (int i = 0; i < kLNB; ++i) xv[i] = i < kb ? A[(int64_t)(k + i) * ld + col] : 0.f;
+                for (int i = 0; i < kLNB; ++i) xv[i] = i < kb ? A[(int64_t)(k + i) * ld + col] : (T)0;
 #pragma unroll
                 for (int i = 1; i < kLNB; ++i) {
-                    float s = xv[i];
+                    T s = xv[i];
 #pragma unroll
                     for (int q = 0; q < i; ++q) s -= Ds[i][q] * xv[q];
                     xv[i] = s;
@@ -63,14 +69,14 @@ static __device__ bool cta_lu_nopiv(float* A, int ld, int N, float (*Ds)[kLNB + 
                     if (i < kb) A[(int64_t)(k + i) * ld + col] = xv[i];
             }
             for (int rr = tid; rr < m; rr += nt) {
-                float xv[kLNB];
-                float* row = A + (int64_t)(k + kb + rr) * ld + k;
+                T xv[kLNB];
+                T* row = A + (int64_t)(k + kb + rr) * ld + k;
 #pragma unroll
-                for (int j = 0; j < kLNB; ++j) xv[j] = j < kb ? row[j] : 0.f;
+                for (int j = 0; j < kLNB; ++j) xv[j] = j < kb ? row[j] : (T)0;
 #pragma unroll
                 for (int j = 0; j < kLNB; ++j) {
                     if (j < kb) {
-                        float s = xv[j];
+                        T s = xv[j];
 #pragma unroll
                         for (int q = 0; q < j; ++q) s -= xv[q] * Ds[q][j];
                         xv[j] = s / Ds[j][j];
@@ -85,23 +91,23 @@ static __device__ bool cta_lu_nopiv(float* A, int ld, int N, float (*Ds)[kLNB + 
             const int mb = (m + 3) / 4;
             for (int t = tid; t < mb * mb; t += nt) {
                 const int bi = t / mb, bj = t % mb;
-                float acc[4][4] = {};
+                T acc[4][4] = {};
                 for (int p = 0; p < kb; ++p) {
-                    float lv[4], uv[4];
+                    T lv[4], uv[4];
 #pragma unroll
                     for (int a = 0; a < 4; ++a) {
                         const int rr = 4 * bi + a;
-                        lv[a] = rr < m ? A[(int64_t)(k + kb + rr) * ld + k + p] : 0.f;
+                        lv[a] = rr < m ? A[(int64_t)(k + kb + rr) * ld + k + p] : (T)0;
                     }
 #pragma unroll
                     for (int c = 0; c < 4; ++c) {
                         const int cc = 4 * bj + c;
-                        uv[c] = cc < m ? A[(int64_t)(k + p) * ld + k + kb + cc] : 0.f;
+                        uv[c] = cc < m ? A[(int64_t)(k + p) * ld + k + kb + cc] : (T)0;
                     }
 #pragma unroll
                     for (int a = 0; a < 4; ++a)
 #pragma unroll
-                        for (int c = 0; c < 4; ++c) acc[a][c] = fmaf(lv[a], uv[c], acc[a][c]);
+                        for (int c = 0; c < 4; ++c) acc[a][c] = cta_fma(lv[a], uv[c], acc[a][c]);
                 }
 #pragma unroll
                 for (int a = 0; a < 4; ++a) {
@@ -120,24 +126,25 @@ static __device__ bool cta_lu_nopiv(float* A, int ld, int N, float (*Ds)[kLNB + 
     return true;
 }
 
-// In-CTA triangular solves with the FP32 factors, in place on t (length N):
+// In-CTA triangular solves with the factors, in place on t (length N):
 // forward (unit L) then backward (U), block column sweeps of kLNB.
-static __device__ void cta_lu_solve(const float* A, int ld, int N, float* t, float* xs) {
+template <typename T>
+static __device__ void cta_lu_solve(const T* A, int ld, int N, T* t, T* xs) {
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5;
     for (int k = 0; k < N; k += kLNB) {
         const int kb = min(kLNB, N - k);
         if (wid == 0) {
-            float v = lane < kb ? t[k + lane] : 0.f;
+            T v = lane < kb ? t[k + lane] : (T)0;
             for (int c = 0; c < kb; ++c) {
-                const float xc = __shfl_sync(0xffffffffu, v, c);
+                const T xc = __shfl_sync(0xffffffffu, v, c);
                 if (lane > c && lane < kb) v -= A[(int64_t)(k + lane) * ld + k + c] * xc;
             }
             if (lane < kb) { t[k + lane] = v; xs[lane] = v; }
         }
         __syncthreads();
         for (int r = k + kb + tid; r < N; r += nt) {
-            const float* row = A + (int64_t)r * ld + k;
-            float s = 0.f;
+            const T* row = A + (int64_t)r * ld + k;
+            T s = (T)0;
             for (int c = 0; c < kb; ++c) s += row[c] * xs[c];
             t[r] -= s;
         }
@@ -148,10 +155,10 @@ static __device__ void cta_lu_solve(const float* A, int ld, int N, float* t, flo
         const int k = bk * kLNB;
         const int kb = min(kLNB, N - k);
         if (wid == 0) {
-            float v = lane < kb ? t[k + lane] : 0.f;
+            T v = lane < kb ? t[k + lane] : (T)0;
             for (int c = kb - 1; c >= 0; --c) {
-                float mine = __shfl_sync(0xffffffffu, v, c);
-                float xc = mine / A[(int64_t)(k + c) * ld + k + c];
+                T mine = __shfl_sync(0xffffffffu, v, c);
+                T xc = mine / A[(int64_t)(k + c) * ld + k + c];
                 if (lane == c) v = xc;
                 if (lane < c) v -= A[(int64_t)(k + lane) * ld + k + c] * xc;
             }
@@ -159,8 +166,8 @@ static __device__ void cta_lu_solve(const float* A, int ld, int N, float* t, flo
         }
         __syncthreads();
         for (int r = tid; r < k; r += nt) {
-            const float* row = A + (int64_t)r * ld + k;
-            float s = 0.f;
+            const T* row = A + (int64_t)r * ld + k;
+            T s = (T)0;
             for (int c = 0; c < kb; ++c) s += row[c] * xs[c];
             t[r] -= s;
         }

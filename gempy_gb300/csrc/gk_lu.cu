@@ -509,6 +509,68 @@ __global__ void __launch_bounds__(256) gemm_update_kernel(T* __restrict__ A, int
     }
 }
 
+// Restricted form of gemm_update_kernel for the two-level setup (any T):
+// C[i][j] -= sum_p A[i][k+p] A[k+p][j] for i in [r_lo, r_hi), j in [c_lo, c_hi);
+// with diag_bs > 0 the grid's z index selects the diagonal block
+// [r_lo + z diag_bs, ...) of both ranges.
+template <typename T, int BM, int BN, int BK>
+__global__ void __launch_bounds__(256) gemm_range_kernel(T* __restrict__ A, int64_t lda, int64_t k, int kb,
+                                                         int64_t r_lo, int64_t r_hi, int64_t c_lo, int64_t c_hi,
+                                                         int diag_bs) {
+    constexpr int TM = BM / 16, TN = BN / 16;
+    __shared__ T As[BK][BM + 1];
+    __shared__ T Bs[BK][BN];
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    if (diag_bs > 0) {
+        const int64_t b0 = r_lo + (int64_t)blockIdx.z * diag_bs;
+        r_lo = c_lo = b0;
+        r_hi = c_hi = min(r_hi, b0 + diag_bs);
+    }
+    const int64_t i0 = r_lo + (int64_t)blockIdx.y * BM, j0 = c_lo + (int64_t)blockIdx.x * BN;
+    if (i0 >= r_hi || j0 >= c_hi) return;
+    T acc[TM][TN];
+#pragma unroll
+    for (int a = 0; a < TM; ++a)
+#pragma unroll
+        for (int b = 0; b < TN; ++b) acc[a][b] = (T)0;
+    for (int p0 = 0; p0 < kb; p0 += BK) {
+        for (int idx = threadIdx.x; idx < BM * BK; idx += 256) {
+            int m = idx / BK, p = idx % BK;
+            int64_t gi = i0 + m;
+            As[p][m] = (gi < r_hi && p0 + p < kb) ? A[gi * lda + k + p0 + p] : (T)0;
+        }
+        for (int idx = threadIdx.x; idx < BK * BN; idx += 256) {
+            int p = idx / BN, c = idx % BN;
+            int64_t gj = j0 + c;
+            Bs[p][c] = (gj < c_hi && p0 + p < kb) ? A[(k + p0 + p) * lda + gj] : (T)0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int p = 0; p < BK; ++p) {
+            T av[TM], bv[TN];
+#pragma unroll
+            for (int a = 0; a < TM; ++a) av[a] = As[p][ty + 16 * a];
+#pragma unroll
+            for (int b = 0; b < TN; ++b) bv[b] = Bs[p][tx + 16 * b];
+#pragma unroll
+            for (int a = 0; a < TM; ++a)
+#pragma unroll
+                for (int b = 0; b < TN; ++b) acc[a][b] += av[a] * bv[b];
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int a = 0; a < TM; ++a) {
+        int64_t gi = i0 + ty + 16 * a;
+        if (gi >= r_hi) continue;
+#pragma unroll
+        for (int b = 0; b < TN; ++b) {
+            int64_t gj = j0 + tx + 16 * b;
+            if (gj < c_hi) A[gi * lda + gj] -= acc[a][b];
+        }
+    }
+}
+
 // FP32 trailing update for aligned panels (offsets and lda multiples of 4):
 // 128 x 128 tile per CTA, 16 x 16 threads each owning an 8 x 8 block split in
 // four 4 x 4 quadrants, float4 shared-memory reads (A stored k-major), the
@@ -1102,9 +1164,15 @@ static gk_status lu_solve(int64_t n, const T* LU, int64_t lda, const int32_t* ip
 // costs two triangular solves of order r, two rectangular products and the
 // block solves.  L_RL U_LR is the low-rank (rank r) part of the operator.
 // ----------------------------------------------------------------------------
-__global__ void __launch_bounds__(512) block_lu_kernel(float* A, int64_t lda, int64_t r, int64_t n, int bs,
+// FP64 blocks use 256 threads so the per-thread 32-entry row buffers of
+// cta_lu_nopiv stay in registers.
+template <typename T>
+constexpr int block_lu_threads() { return sizeof(T) == 8 ? 256 : 512; }
+
+template <typename T>
+__global__ void __launch_bounds__(block_lu_threads<T>()) block_lu_kernel(T* A, int64_t lda, int64_t r, int64_t n, int bs,
                                                        gk_info* info) {
-    __shared__ float Ds[kLNB][kLNB + 1];
+    __shared__ T Ds[kLNB][kLNB + 1];
     __shared__ int s_bad;
     const int64_t b0 = r + (int64_t)blockIdx.x * bs;
     const int nb = (int)min((int64_t)bs, n - b0);
@@ -1114,9 +1182,10 @@ __global__ void __launch_bounds__(512) block_lu_kernel(float* A, int64_t lda, in
     }
 }
 
-__global__ void __launch_bounds__(256) block_solve_kernel(const float* A, int64_t lda, int64_t r, int64_t n, int bs,
-                                                          float* t) {
-    __shared__ float xs[kLNB];
+template <typename T>
+__global__ void __launch_bounds__(256) block_solve_kernel(const T* A, int64_t lda, int64_t r, int64_t n, int bs,
+                                                          T* t) {
+    __shared__ T xs[kLNB];
     const int64_t b0 = r + (int64_t)blockIdx.x * bs;
     const int nb = (int)min((int64_t)bs, n - b0);
     if (nb <= 0) return;
@@ -1124,44 +1193,48 @@ __global__ void __launch_bounds__(256) block_solve_kernel(const float* A, int64_
 }
 
 // y[i] -= sum_j A[i][j] x[j], i in [r_lo, r_hi), j in [c_lo, c_hi); warp per row
-__global__ void rect_gemv_kernel(const float* __restrict__ A, int64_t lda, int64_t r_lo, int64_t r_hi, int64_t c_lo,
-                                 int64_t c_hi, const float* __restrict__ x, float* __restrict__ y) {
+template <typename T>
+__global__ void rect_gemv_kernel(const T* __restrict__ A, int64_t lda, int64_t r_lo, int64_t r_hi, int64_t c_lo,
+                                 int64_t c_hi, const T* __restrict__ x, T* __restrict__ y) {
     const int64_t row = r_lo + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (row >= r_hi) return;
-    const float* a = A + row * lda;
-    float s = 0.f;
-    for (int64_t j = c_lo + lane; j < c_hi; j += 32) s = fmaf(a[j], x[j], s);
+    const T* a = A + row * lda;
+    T s = (T)0;
+    for (int64_t j = c_lo + lane; j < c_hi; j += 32) s = cta_fma(a[j], x[j], s);
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
     if (lane == 0) y[row] -= s;
 }
 
+template <typename T>
 __global__ void permute_scale_kernel(const double* __restrict__ K, int64_t ldk, int64_t n,
                                      const int32_t* __restrict__ perm, const double* __restrict__ d,
-                                     float* __restrict__ A, int64_t lda) {
+                                     T* __restrict__ A, int64_t lda) {
     const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (row >= n) return;
     const int64_t pi = perm[row];
     const double di = d[pi];
     const double* k = K + pi * ldk;
-    float* a = A + row * lda;
+    T* a = A + row * lda;
     for (int64_t j = lane; j < n; j += 32) {
         const int64_t pj = perm[j];
-        a[j] = (float)(di * k[pj] * d[pj]);
+        a[j] = (T)(di * k[pj] * d[pj]);
     }
 }
 
+template <typename T>
 __global__ void gather_scale_kernel(const double* __restrict__ v, const int32_t* __restrict__ perm,
-                                    const double* __restrict__ d, int64_t n, float* __restrict__ t) {
+                                    const double* __restrict__ d, int64_t n, T* __restrict__ t) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
         const int64_t p = perm[i];
-        t[i] = (float)(d[p] * v[p]);
+        t[i] = (T)(d[p] * v[p]);
     }
 }
 
-__global__ void scatter_scale_kernel(const float* __restrict__ t, const int32_t* __restrict__ perm,
+template <typename T>
+__global__ void scatter_scale_kernel(const T* __restrict__ t, const int32_t* __restrict__ perm,
                                      const double* __restrict__ d, int64_t n, double* __restrict__ z) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
@@ -1205,86 +1278,105 @@ gk_status gk_internal_lu_solve_f32(int64_t n, const float* LU, int64_t lda, cons
     return lu_solve<float>(n, LU, lda, ipiv, b, work, wb, info, st);
 }
 size_t gk_internal_lu_ws_f32(int64_t n) { return lu_ws_bytes<float>(n); }
-// Two-level setup: A (n x lda, FP32) <- P D K D P^T, partial LU over the first
+// Two-level setup: A (n x lda, FP32 or FP64) <- P D K D P^T, partial LU over the first
 // r columns with restricted updates, LU of the Schur diagonal blocks, and the
 // inverses of the 128 x 128 diagonal blocks of L_LL / U_LL for the solves.
-gk_status gk_internal_twolevel_setup(int64_t n, const double* K, int64_t ldk, const int32_t* perm, const double* d,
-                                     int64_t r, int bs, float* A, int64_t lda, int32_t* ipiv, void* work,
+template <typename T>
+static gk_status twolevel_setup(int64_t n, const double* K, int64_t ldk, const int32_t* perm, const double* d,
+                                     int64_t r, int bs, T* A, int64_t lda, int32_t* ipiv, void* work,
                                      size_t wbytes, gk_info* info, cudaStream_t st) {
-    constexpr int NB = LuCfg<float>::NB;
-    if (n <= 0 || r <= 0 || r >= n || bs <= 0 || (r % NB) != 0 || (bs % 64) != 0 || (lda % 4) != 0 ||
+    constexpr int NB = LuCfg<T>::NB;
+    if (n <= 0 || r <= 0 || r >= n || bs <= 0 || (r % 64) != 0 || (bs % 64) != 0 || (lda % 4) != 0 ||
         ((uintptr_t)A % 16) != 0)
         return GK_ERR_ARG;
-    if (work == nullptr || wbytes < lu_ws_bytes<float>(n)) return GK_ERR_SIZE;
-    permute_scale_kernel<<<(unsigned)((n * 32 + 255) / 256), 256, 0, st>>>(K, ldk, n, perm, d, A, lda);
+    if (work == nullptr || wbytes < lu_ws_bytes<T>(n)) return GK_ERR_SIZE;
+    permute_scale_kernel<T><<<(unsigned)((n * 32 + 255) / 256), 256, 0, st>>>(K, ldk, n, perm, d, A, lda);
     GK_LAUNCH_CHECK();
     const int64_t nblk = (n - r + bs - 1) / bs;
     for (int64_t k = 0; k < r; k += NB) {
         const int kb = (int)min((int64_t)NB, r - k);
-        diag_lu_kernel<float, NB><<<1, 256, 0, st>>>(A, lda, k, kb, ipiv, info);
+        diag_lu_kernel<T, NB><<<1, 256, 0, st>>>(A, lda, k, kb, ipiv, info);
         GK_LAUNCH_CHECK();
         const int64_t rest = n - k - kb;
-        trsm_right_kernel<float, NB><<<(unsigned)((rest + 63) / 64), 64, 0, st>>>(A, lda, n, k, kb);
+        trsm_right_kernel<T, NB><<<(unsigned)((rest + 63) / 64), 64, 0, st>>>(A, lda, n, k, kb);
         GK_LAUNCH_CHECK();
-        trsm_kernel<float, NB><<<(unsigned)((rest + 127) / 128), 128, 0, st>>>(A, lda, n, k, kb);
+        trsm_kernel<T, NB><<<(unsigned)((rest + 127) / 128), 128, 0, st>>>(A, lda, n, k, kb);
         GK_LAUNCH_CHECK();
         const int64_t o = k + kb;
+        if (sizeof(T) == 8) {
+            double* Ad = (double*)A;
+            constexpr int BT = 64;
+            if (o < r) {
+                dim3 ga((unsigned)((n - o + BT - 1) / BT), (unsigned)((r - o + BT - 1) / BT));
+                gemm_range_kernel<double, BT, BT, 16><<<ga, 256, 0, st>>>(Ad, lda, k, kb, o, r, o, n, 0);
+                GK_LAUNCH_CHECK();
+                dim3 gb((unsigned)((r - o + BT - 1) / BT), (unsigned)((n - r + BT - 1) / BT));
+                gemm_range_kernel<double, BT, BT, 16><<<gb, 256, 0, st>>>(Ad, lda, k, kb, r, n, o, r, 0);
+                GK_LAUNCH_CHECK();
+            }
+            dim3 gc((unsigned)((bs + BT - 1) / BT), (unsigned)((bs + BT - 1) / BT), (unsigned)nblk);
+            gemm_range_kernel<double, BT, BT, 16><<<gc, 256, 0, st>>>(Ad, lda, k, kb, r, n, r, n, bs);
+            GK_LAUNCH_CHECK();
+            continue;
+        }
+        float* Af = (float*)A;
         if (o < r) {
             // landmark rows, all columns to the right
             dim3 ga((unsigned)((n - o + 127) / 128), (unsigned)((r - o + 127) / 128));
-            sgemm_update_kernel<<<ga, 256, 0, st>>>(A, lda, k, kb, o, r, o, n, 0);
+            sgemm_update_kernel<<<ga, 256, 0, st>>>(Af, lda, k, kb, o, r, o, n, 0);
             GK_LAUNCH_CHECK();
             // remaining rows, landmark columns
             dim3 gb((unsigned)((r - o + 127) / 128), (unsigned)((n - r + 127) / 128));
-            sgemm_update_kernel<<<gb, 256, 0, st>>>(A, lda, k, kb, r, n, o, r, 0);
+            sgemm_update_kernel<<<gb, 256, 0, st>>>(Af, lda, k, kb, r, n, o, r, 0);
             GK_LAUNCH_CHECK();
         }
         // diagonal blocks of the Schur complement
         dim3 gc((unsigned)((bs + 127) / 128), (unsigned)((bs + 127) / 128), (unsigned)nblk);
-        sgemm_update_kernel<<<gc, 256, 0, st>>>(A, lda, k, kb, r, n, r, n, bs);
+        sgemm_update_kernel<<<gc, 256, 0, st>>>(Af, lda, k, kb, r, n, r, n, bs);
         GK_LAUNCH_CHECK();
     }
-    block_lu_kernel<<<(unsigned)nblk, 512, 0, st>>>(A, lda, r, n, bs, info);
+    block_lu_kernel<T><<<(unsigned)nblk, block_lu_threads<T>(), 0, st>>>(A, lda, r, n, bs, info);
     GK_LAUNCH_CHECK();
-    const size_t ysmem = (size_t)kTB * kTB * sizeof(float);
-    GK_CUDA_TRY(cudaFuncSetAttribute(tri_inv_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ysmem));
-    tri_inv_kernel<float><<<(unsigned)((r + kTB - 1) / kTB), kTB, ysmem, st>>>(A, lda, r, lu_ws_dinv<float>(work, r, 0),
-                                                                              lu_ws_dinv<float>(work, r, 1), info);
+    const size_t ysmem = (size_t)kTB * kTB * sizeof(T);
+    GK_CUDA_TRY(cudaFuncSetAttribute(tri_inv_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ysmem));
+    tri_inv_kernel<T><<<(unsigned)((r + kTB - 1) / kTB), kTB, ysmem, st>>>(A, lda, r, lu_ws_dinv<T>(work, r, 0),
+                                                                          lu_ws_dinv<T>(work, r, 1), info);
     GK_LAUNCH_CHECK();
     return GK_OK;
 }
 
-// z = M^-1 v (FP64 in/out; FP32 inside).  t: n floats of scratch.
-gk_status gk_internal_twolevel_apply(int64_t n, const float* A, int64_t lda, const int32_t* perm, const double* d,
-                                     int64_t r, int bs, const double* v, double* z, float* t, void* work,
+// z = M^-1 v (FP64 in/out; T inside).  t: n values of scratch.
+template <typename T>
+static gk_status twolevel_apply(int64_t n, const T* A, int64_t lda, const int32_t* perm, const double* d,
+                                     int64_t r, int bs, const double* v, double* z, T* t, void* work,
                                      size_t wbytes, gk_info* info, cudaStream_t st) {
     const unsigned vb = (unsigned)((n + 255) / 256);
-    gather_scale_kernel<<<vb, 256, 0, st>>>(v, perm, d, n, t);
+    gather_scale_kernel<T><<<vb, 256, 0, st>>>(v, perm, d, n, t);
     GK_LAUNCH_CHECK();
     // forward: L_LL w_L = t_L, then t_R -= L_RL w_L
     int sms = device_sm_count();
     // flags and diagonal inverses both use the workspace layout of order r
-    char* p = (char*)work + panel_ws_bytes<float, LuCfg<float>::NB>(sms);
+    char* p = (char*)work + panel_ws_bytes<T, LuCfg<T>::NB>(sms);
     p += align256((size_t)(r + 1) * sizeof(int32_t)) * 2;
     const int nblk_r = (int)((r + kTB - 1) / kTB);
     int* flags = (int*)p;
     int* counter = flags + (size_t)nblk_r * kFlagStride;
     GK_CUDA_TRY(cudaMemsetAsync(flags, 0, ((size_t)nblk_r + 1) * kFlagStride * sizeof(int), st));
-    trsv_kernel<float><<<nblk_r, 256, 0, st>>>(A, lda, r, t, lu_ws_dinv<float>(work, r, 0), 1, counter, flags, info);
+    trsv_kernel<T><<<nblk_r, 256, 0, st>>>(A, lda, r, t, lu_ws_dinv<T>(work, r, 0), 1, counter, flags, info);
     GK_LAUNCH_CHECK();
-    rect_gemv_kernel<<<(unsigned)(((n - r) * 32 + 255) / 256), 256, 0, st>>>(A, lda, r, n, 0, r, t, t);
+    rect_gemv_kernel<T><<<(unsigned)(((n - r) * 32 + 255) / 256), 256, 0, st>>>(A, lda, r, n, 0, r, t, t);
     GK_LAUNCH_CHECK();
     // block-Jacobi on the Schur complement
     const int64_t nblk = (n - r + bs - 1) / bs;
-    block_solve_kernel<<<(unsigned)nblk, 256, 0, st>>>(A, lda, r, n, bs, t);
+    block_solve_kernel<T><<<(unsigned)nblk, 256, 0, st>>>(A, lda, r, n, bs, t);
     GK_LAUNCH_CHECK();
     // backward: t_L -= U_LR x_R, then U_LL x_L = t_L
-    rect_gemv_kernel<<<(unsigned)((r * 32 + 255) / 256), 256, 0, st>>>(A, lda, 0, r, r, n, t, t);
+    rect_gemv_kernel<T><<<(unsigned)((r * 32 + 255) / 256), 256, 0, st>>>(A, lda, 0, r, r, n, t, t);
     GK_LAUNCH_CHECK();
     GK_CUDA_TRY(cudaMemsetAsync(flags, 0, ((size_t)nblk_r + 1) * kFlagStride * sizeof(int), st));
-    trsv_kernel<float><<<nblk_r, 256, 0, st>>>(A, lda, r, t, lu_ws_dinv<float>(work, r, 1), 0, counter, flags, info);
+    trsv_kernel<T><<<nblk_r, 256, 0, st>>>(A, lda, r, t, lu_ws_dinv<T>(work, r, 1), 0, counter, flags, info);
     GK_LAUNCH_CHECK();
-    scatter_scale_kernel<<<vb, 256, 0, st>>>(t, perm, d, n, z);
+    scatter_scale_kernel<T><<<vb, 256, 0, st>>>(t, perm, d, n, z);
     GK_LAUNCH_CHECK();
     return GK_OK;
 }
@@ -1293,3 +1385,25 @@ gk_status gk_internal_lu_factor_nopiv_f32(int64_t n, float* A, int64_t lda, int3
                                           gk_info* info, cudaStream_t st) {
     return lu_factor_nopiv<float>(n, A, lda, ipiv, work, wb, info, st);
 }
+
+gk_status gk_internal_twolevel_setup(int64_t n, const double* K, int64_t ldk, const int32_t* perm, const double* d,
+                                     int64_t r, int bs, float* A, int64_t lda, int32_t* ipiv, void* work,
+                                     size_t wbytes, gk_info* info, cudaStream_t st) {
+    return twolevel_setup<float>(n, K, ldk, perm, d, r, bs, A, lda, ipiv, work, wbytes, info, st);
+}
+gk_status gk_internal_twolevel_setup_f64(int64_t n, const double* K, int64_t ldk, const int32_t* perm,
+                                         const double* d, int64_t r, int bs, double* A, int64_t lda, int32_t* ipiv,
+                                         void* work, size_t wbytes, gk_info* info, cudaStream_t st) {
+    return twolevel_setup<double>(n, K, ldk, perm, d, r, bs, A, lda, ipiv, work, wbytes, info, st);
+}
+gk_status gk_internal_twolevel_apply(int64_t n, const float* A, int64_t lda, const int32_t* perm, const double* d,
+                                     int64_t r, int bs, const double* v, double* z, float* t, void* work,
+                                     size_t wbytes, gk_info* info, cudaStream_t st) {
+    return twolevel_apply<float>(n, A, lda, perm, d, r, bs, v, z, t, work, wbytes, info, st);
+}
+gk_status gk_internal_twolevel_apply_f64(int64_t n, const double* A, int64_t lda, const int32_t* perm,
+                                         const double* d, int64_t r, int bs, const double* v, double* z, double* t,
+                                         void* work, size_t wbytes, gk_info* info, cudaStream_t st) {
+    return twolevel_apply<double>(n, A, lda, perm, d, r, bs, v, z, t, work, wbytes, info, st);
+}
+size_t gk_internal_lu_ws_f64(int64_t n) { return lu_ws_bytes<double>(n); }

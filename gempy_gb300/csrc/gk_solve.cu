@@ -23,6 +23,13 @@ gk_status gk_internal_lu_factor_f32(int64_t n, float* A, int64_t lda, int32_t* i
 gk_status gk_internal_lu_solve_f32(int64_t n, const float* LU, int64_t lda, const int32_t* ipiv, float* b, void* work,
                                    size_t wb, gk_info* info, cudaStream_t st);
 size_t gk_internal_lu_ws_f32(int64_t n);
+size_t gk_internal_lu_ws_f64(int64_t n);
+gk_status gk_internal_twolevel_setup_f64(int64_t n, const double* K, int64_t ldk, const int32_t* perm,
+                                         const double* d, int64_t r, int bs, double* A, int64_t lda, int32_t* ipiv,
+                                         void* work, size_t wbytes, gk_info* info, cudaStream_t st);
+gk_status gk_internal_twolevel_apply_f64(int64_t n, const double* A, int64_t lda, const int32_t* perm,
+                                         const double* d, int64_t r, int bs, const double* v, double* z, double* t,
+                                         void* work, size_t wbytes, gk_info* info, cudaStream_t st);
 gk_status gk_internal_lu_factor_nopiv_f32(int64_t n, float* A, int64_t lda, int32_t* ipiv, void* work, size_t wb,
                                           gk_info* info, cudaStream_t st);
 gk_status gk_internal_twolevel_setup(int64_t n, const double* K, int64_t ldk, const int32_t* perm, const double* d,
@@ -37,17 +44,20 @@ namespace gk {
 static size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
 static int64_t ld32_of(int64_t n) { return (n + 63) / 64 * 64; }
 
-constexpr int kRestart = 50;
+constexpr int kRestart = 50;           // LU-preconditioned FGMRES
+constexpr int kRestartTwoLevel = 200;  // two-level: many more outlying eigenvalues to resolve
 constexpr int kDotBlocks = 128;
 
 struct MixedWork {
-    float* K32;
+    float* K32;     // preconditioner matrix (FP32 layout) ...
+    double* K64;    // ... or the same region as FP64 (two-level, FP64 storage)
     int32_t* ipiv;
     void* luw;
     size_t luw_bytes;
     double* d;      // equilibration
     double* r;      // residual / work vector
-    float* t32;     // FP32 vector for the preconditioner
+    float* t32;     // preconditioner vector (FP32) ...
+    double* t64;    // ... or FP64, same region
     double* V;      // (m+1) x n Krylov basis (vector-major)
     double* Z;      // m x n preconditioned directions
     double* w;      // n
@@ -57,31 +67,33 @@ struct MixedWork {
     gk_info* iinfo; // status word used when the caller passes none
 };
 
-static size_t mixed_bytes(int64_t n) {
+// es: bytes per element of the preconditioner's matrix and vector (4 or 8);
+// m: restart length (Krylov basis size).
+static size_t mixed_bytes(int64_t n, int es = 4, int m = kRestart) {
     int64_t ld = ld32_of(n);
-    return al((size_t)n * ld * sizeof(float)) + al(n * sizeof(int32_t)) + al(gk_internal_lu_ws_f32(n)) +
-           2 * al(n * sizeof(double)) + al(n * sizeof(float)) + al((size_t)(kRestart + 1) * n * sizeof(double)) +
-           al((size_t)kRestart * n * sizeof(double)) + al(n * sizeof(double)) +
-           al((size_t)kDotBlocks * (kRestart + 1) * sizeof(double)) + 2 * al((kRestart + 1) * sizeof(double)) +
-           al(sizeof(gk_info));
+    const size_t luws = es == 8 ? gk_internal_lu_ws_f64(n) : gk_internal_lu_ws_f32(n);
+    return al((size_t)n * ld * es) + al(n * sizeof(int32_t)) + al(luws) + 2 * al(n * sizeof(double)) +
+           al((size_t)n * es) + al((size_t)(m + 1) * n * sizeof(double)) + al((size_t)m * n * sizeof(double)) +
+           al(n * sizeof(double)) + al((size_t)kDotBlocks * (m + 1) * sizeof(double)) +
+           2 * al((m + 1) * sizeof(double)) + al(sizeof(gk_info));
 }
 
-static MixedWork carve(void* base, int64_t n) {
+static MixedWork carve(void* base, int64_t n, int es = 4, int m = kRestart) {
     MixedWork w;
     char* p = (char*)base;
     int64_t ld = ld32_of(n);
-    w.K32 = (float*)p; p += al((size_t)n * ld * sizeof(float));
+    w.K32 = (float*)p; w.K64 = (double*)p; p += al((size_t)n * ld * es);
     w.ipiv = (int32_t*)p; p += al(n * sizeof(int32_t));
-    w.luw = p; w.luw_bytes = al(gk_internal_lu_ws_f32(n)); p += w.luw_bytes;
+    w.luw = p; w.luw_bytes = al(es == 8 ? gk_internal_lu_ws_f64(n) : gk_internal_lu_ws_f32(n)); p += w.luw_bytes;
     w.d = (double*)p; p += al(n * sizeof(double));
     w.r = (double*)p; p += al(n * sizeof(double));
-    w.t32 = (float*)p; p += al(n * sizeof(float));
-    w.V = (double*)p; p += al((size_t)(kRestart + 1) * n * sizeof(double));
-    w.Z = (double*)p; p += al((size_t)kRestart * n * sizeof(double));
+    w.t32 = (float*)p; w.t64 = (double*)p; p += al((size_t)n * es);
+    w.V = (double*)p; p += al((size_t)(m + 1) * n * sizeof(double));
+    w.Z = (double*)p; p += al((size_t)m * n * sizeof(double));
     w.w = (double*)p; p += al(n * sizeof(double));
-    w.part = (double*)p; p += al((size_t)kDotBlocks * (kRestart + 1) * sizeof(double));
-    w.h = (double*)p; p += al((kRestart + 1) * sizeof(double));
-    w.y = (double*)p; p += al((kRestart + 1) * sizeof(double));
+    w.part = (double*)p; p += al((size_t)kDotBlocks * (m + 1) * sizeof(double));
+    w.h = (double*)p; p += al((m + 1) * sizeof(double));
+    w.y = (double*)p; p += al((m + 1) * sizeof(double));
     w.iinfo = (gk_info*)p;
     return w;
 }
@@ -120,32 +132,26 @@ __global__ void gemv_kernel(const double* __restrict__ K, int64_t ldk, int64_t n
     if (lane == 0) y[row] = b ? b[row] - s : s;
 }
 
-// partial dots part[blk][c] = sum_{i in blk} V[c][i] * w[i], c < ncol
+// partial dots part[blk][c] = sum_{i in blk} V[c][i] * w[i], c < ncol; one
+// warp per column, each block over its own contiguous index range.
 __global__ void dots_partial_kernel(const double* __restrict__ V, int64_t n, int ncol, const double* __restrict__ w,
                                     double* __restrict__ part) {
-    __shared__ double red[8];
     const int64_t per = (n + gridDim.x - 1) / gridDim.x;
     const int64_t i0 = (int64_t)blockIdx.x * per, i1 = min(n, i0 + per);
-    for (int c = 0; c < ncol; ++c) {
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int c = threadIdx.x >> 5; c < ncol; c += nw) {
         const double* v = V + (int64_t)c * n;
         double s = 0.0;
-        for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) s = fma(v[i], w[i], s);
+        for (int64_t i = i0 + lane; i < i1; i += 32) s = fma(v[i], w[i], s);
         for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double t = 0.0;
-            for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
-            part[(int64_t)blockIdx.x * ncol + c] = t;
-        }
-        __syncthreads();
+        if (lane == 0) part[(int64_t)blockIdx.x * ncol + c] = s;
     }
 }
 
 // h[c] = sum_blk part[blk][c] (fixed order: deterministic); acc: h += result
 __global__ void dots_final_kernel(const double* __restrict__ part, int nblk, int ncol, double* __restrict__ h,
                                   int accumulate) {
-    int c = threadIdx.x;
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncol) return;
     double t = 0.0;
     for (int b = 0; b < nblk; ++b) t += part[(int64_t)b * ncol + c];
@@ -207,23 +213,25 @@ struct Solver {
     cudaStream_t st;
     unsigned vb, rb;
     // preconditioner: 0 = FP32 LU of the equilibrated K, 1 = two-level
+    // (FP32 storage), 2 = two-level (FP64 storage)
     int mode = 0;
     const int32_t* perm = nullptr;
     int64_t r = 0;
     int bs = 0;
+    int m = kRestart;  // restart length; the workspace holds m + 1 basis vectors
 
     // dot products h[0..ncol) = V[0..ncol)^T v  (accumulate: h += ...)
     gk_status dots(const double* V, int ncol, const double* v, double* h, int accumulate) {
         dots_partial_kernel<<<kDotBlocks, 256, 0, st>>>(V, n, ncol, v, w.part);
         GK_LAUNCH_CHECK();
-        dots_final_kernel<<<1, 64, 0, st>>>(w.part, kDotBlocks, ncol, h, accumulate);
+        dots_final_kernel<<<(unsigned)((ncol + 63) / 64), 64, 0, st>>>(w.part, kDotBlocks, ncol, h, accumulate);
         GK_LAUNCH_CHECK();
         return GK_OK;
     }
     gk_status norm2(const double* v, double& out) {
-        gk_status s = dots(v, 1, v, w.h + kRestart, 0);
+        gk_status s = dots(v, 1, v, w.h + m, 0);
         if (s != GK_OK) return s;
-        GK_CUDA_TRY(cudaMemcpyAsync(&out, w.h + kRestart, sizeof(double), cudaMemcpyDeviceToHost, st));
+        GK_CUDA_TRY(cudaMemcpyAsync(&out, w.h + m, sizeof(double), cudaMemcpyDeviceToHost, st));
         GK_CUDA_TRY(cudaStreamSynchronize(st));
         out = sqrt(out);
         return GK_OK;
@@ -233,6 +241,9 @@ struct Solver {
         if (mode == 1)
             return gk_internal_twolevel_apply(n, w.K32, ld32, perm, w.d, r, bs, v, z, w.t32, w.luw, w.luw_bytes,
                                               info, st);
+        if (mode == 2)
+            return gk_internal_twolevel_apply_f64(n, w.K64, ld32, perm, w.d, r, bs, v, z, w.t64, w.luw,
+                                                  w.luw_bytes, info, st);
         scale_to_f32_kernel<<<vb, 256, 0, st>>>(v, w.d, n, w.t32);
         GK_LAUNCH_CHECK();
         gk_status s = gk_internal_lu_solve_f32(n, w.K32, ld32, w.ipiv, w.t32, w.luw, w.luw_bytes, info, st);
@@ -245,7 +256,7 @@ struct Solver {
 
 }  // namespace
 
-// Restarted FGMRES(kRestart) in FP64 with right preconditioning S.precond;
+// Restarted FGMRES(S.m) in FP64 with right preconditioning S.precond;
 // convergence tested on the host between Arnoldi steps.
 static gk_status fgmres(Solver& S, const double* b, double* x, double tol, int max_iter, int& status, int& its,
                         double& rel) {
@@ -266,7 +277,7 @@ static gk_status fgmres(Solver& S, const double* b, double* x, double tol, int m
         status = bnorm == 0.0 ? GK_OK : GK_ERR_NONFINITE;
         rel = 0.0;
     }
-    const int m = kRestart;
+    const int m = S.m;
     std::vector<double> H((m + 1) * m), cs(m), sn(m), g(m + 1), hcol(m + 2), y(m);
     while (status == GK_ERR_NOT_CONVERGED && its < max_iter) {
         // true residual r = b - K x
@@ -405,23 +416,30 @@ extern "C" gk_status gk_solve_mixed(int64_t n, const double* K, int64_t ldk, con
 // ---------------------------------------------------------------------------
 // FGMRES with the two-level (block-Jacobi + low-rank) preconditioner
 // ---------------------------------------------------------------------------
-extern "C" size_t gk_solve_twolevel_workspace_bytes(int64_t n) { return n > 0 ? mixed_bytes(n) : 0; }
+extern "C" size_t gk_solve_twolevel_workspace_bytes(int64_t n, gk_prec prec) {
+    if (n <= 0 || (prec != GK_F32 && prec != GK_F64)) return 0;
+    return mixed_bytes(n, prec == GK_F64 ? 8 : 4, kRestartTwoLevel);
+}
 
 extern "C" gk_status gk_solve_twolevel(int64_t n, const double* K, int64_t ldk, const double* b, double* x,
-                                       const int32_t* perm, int64_t r, int32_t bs, double tol, int32_t max_iter,
-                                       void* work, size_t work_bytes, gk_info* info, gk_stream stream) {
+                                       const int32_t* perm, int64_t r, int32_t bs, gk_prec prec, double tol,
+                                       int32_t max_iter, void* work, size_t work_bytes, gk_info* info,
+                                       gk_stream stream) {
     cudaStream_t st = (cudaStream_t)stream;
     if (n <= 0 || K == nullptr || b == nullptr || x == nullptr || perm == nullptr || ldk < n || max_iter < 1)
         return GK_ERR_ARG;
     if (r <= 0 || r >= n || (r % 64) != 0 || bs <= 0 || (bs % 64) != 0) return GK_ERR_ARG;
-    if (work == nullptr || work_bytes < mixed_bytes(n)) return GK_ERR_SIZE;
+    if (prec != GK_F32 && prec != GK_F64) return GK_ERR_ARG;
+    const int es = prec == GK_F64 ? 8 : 4;
+    if (work == nullptr || work_bytes < mixed_bytes(n, es, kRestartTwoLevel)) return GK_ERR_SIZE;
     Solver S;
-    S.n = n; S.K = K; S.ldk = ldk; S.w = carve(work, n); S.ld32 = ld32_of(n); S.st = st;
+    S.n = n; S.K = K; S.ldk = ldk; S.w = carve(work, n, es, kRestartTwoLevel); S.ld32 = ld32_of(n); S.st = st;
+    S.m = kRestartTwoLevel;
     if (info == nullptr) info = S.w.iinfo;
     S.info = info;
     S.vb = (unsigned)((n + 255) / 256);
     S.rb = (unsigned)((n * 32 + 255) / 256);
-    S.mode = 1;
+    S.mode = prec == GK_F64 ? 2 : 1;
     S.perm = perm;
     S.r = r;
     S.bs = bs;
@@ -429,8 +447,11 @@ extern "C" gk_status gk_solve_twolevel(int64_t n, const double* K, int64_t ldk, 
     GK_CUDA_TRY(cudaMemsetAsync(info, 0, sizeof(gk_info), st));
     equil_kernel<<<S.rb, 256, 0, st>>>(K, ldk, n, w.d);
     GK_LAUNCH_CHECK();
-    gk_status s = gk_internal_twolevel_setup(n, K, ldk, perm, w.d, r, bs, w.K32, S.ld32, w.ipiv, w.luw, w.luw_bytes,
-                                             info, st);
+    gk_status s = prec == GK_F64
+                      ? gk_internal_twolevel_setup_f64(n, K, ldk, perm, w.d, r, bs, w.K64, S.ld32, w.ipiv, w.luw,
+                                                       w.luw_bytes, info, st)
+                      : gk_internal_twolevel_setup(n, K, ldk, perm, w.d, r, bs, w.K32, S.ld32, w.ipiv, w.luw,
+                                                   w.luw_bytes, info, st);
     if (s != GK_OK) return s;
     int32_t fst = 0;
     GK_CUDA_TRY(cudaMemcpyAsync(&fst, &info->status, sizeof(int32_t), cudaMemcpyDeviceToHost, st));

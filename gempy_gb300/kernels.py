@@ -197,16 +197,31 @@ def morton_codes(p):
     return code
 
 
-def twolevel_permutation(series: DeviceSeries, n_landmarks, seed=0):
-    """(perm, r): r = landmark count rounded up to a multiple of 64 (uniformly
-    sampled covariance unknowns plus every drift unknown) placed first, the
-    other unknowns after them in Morton (Z-curve) order of their positions."""
+LANDMARK_POLICIES = ("random", "stratified")
+
+
+def twolevel_permutation(series: DeviceSeries, n_landmarks, seed=0, policy="random"):
+    """(perm, r): r = landmark count rounded up to a multiple of 64 (covariance
+    unknowns plus every drift unknown) placed first, the other unknowns after
+    them in Morton (Z-curve) order of their positions.  ``policy`` picks the
+    covariance landmarks: "random" samples them uniformly, "stratified" takes
+    every k-th unknown along the Morton curve (an even spatial spread) from a
+    seeded offset."""
+    if policy not in LANDMARK_POLICIES:
+        raise ValueError(f"unknown landmark policy {policy!r}")
     pos, nd = unknown_positions(series)
     N = len(pos)
     nc = N - nd
     r = int(min(max(64, -(-(int(n_landmarks) + nd) // 64) * 64), (N - 1) // 64 * 64))
     rng = np.random.default_rng(seed)
-    land = np.sort(rng.choice(nc, r - nd, replace=False))
+    nl = r - nd
+    if policy == "random":
+        land = np.sort(rng.choice(nc, nl, replace=False))
+    else:
+        order = np.argsort(morton_codes(pos[:nc]), kind="stable")
+        step = nc / nl
+        idx = np.minimum((rng.uniform(0, step) + step * np.arange(nl)).astype(np.int64), nc - 1)
+        land = np.sort(order[idx])
     mask = np.ones(N, dtype=bool)
     mask[land] = False
     mask[nc:] = False
@@ -217,20 +232,22 @@ def twolevel_permutation(series: DeviceSeries, n_landmarks, seed=0):
 
 
 def solve_twolevel(series: DeviceSeries, n_landmarks=1024, block=512, tol=1e-8, max_iter=2000, K=None, b=None,
-                   seed=0):
-    """FGMRES with the two-level (block-Jacobi + low-rank) preconditioner."""
+                   seed=0, policy="random", prec=None):
+    """FGMRES with the two-level (block-Jacobi + low-rank) preconditioner;
+    ``prec`` (GK_F32 / GK_F64, default GK_F64) is the preconditioner's storage."""
     lib = _lib.load()
+    prec = GK_F64 if prec is None else int(prec)
     if K is None:
         K, b = build(series, GK_F64)
     n = K.shape[0]
-    perm, r = twolevel_permutation(series, n_landmarks, seed)
+    perm, r = twolevel_permutation(series, n_landmarks, seed, policy)
     pt = torch.as_tensor(perm).to(K.device)
-    wb = lib.gk_solve_twolevel_workspace_bytes(n)
+    wb = lib.gk_solve_twolevel_workspace_bytes(n, prec)
     work = torch.empty(wb, dtype=torch.uint8, device=K.device)
     x = torch.empty(n, dtype=torch.float64, device=K.device)
     info = new_info(K.device)
     check("gk_solve_twolevel", lib.gk_solve_twolevel(n, _ptr(K), K.stride(0), _ptr(b), _ptr(x), _ptr(pt), r,
-                                                     int(block), float(tol), int(max_iter), _ptr(work), wb,
+                                                     int(block), prec, float(tol), int(max_iter), _ptr(work), wb,
                                                      _ptr(info), _stream()))
     return x, info, r
 

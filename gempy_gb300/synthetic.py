@@ -184,7 +184,8 @@ def realisation(index, n_surf=4, resolution=(64, 64, 64), base_seed=0):
                      dense_res=resolution, meta=meta)
 
 
-def learned(seed=0, n_points=20000, n_orient=6000, n_surf=10):
+def learned(seed=0, n_points=20000, n_orient=6000, n_surf=10, range_m=np.sqrt(3) * 1000.0, nug_sp=None,
+            nug_ori=None):
     """Large multi-fold system (N ~ 38k) of the learned-preconditioner config."""
     rng = np.random.default_rng(1234 + seed)
     k = rng.uniform(1, 3, (3, 2)) * 2 * np.pi / 1000.0
@@ -214,4 +215,21 @@ def learned(seed=0, n_points=20000, n_orient=6000, n_surf=10):
     g /= np.linalg.norm(g, axis=1, keepdims=True)
     meta = {"_ori_per_series": [base]}
     return _assemble("learned", surfaces, [base], [g], [n_surf], [StackRelationType.BASEMENT], 1,
-                     dense_res=(8, 8, 8), meta=meta)
+                     nug_sp=nug_sp, nug_ori=nug_ori, dense_res=(8, 8, 8), meta=meta, range_m=range_m)
+
+
+def training_system(index, base_seed=0, n_min=1000, n_max=16000):
+    """One system of the preconditioner-selection training distribution:
+    random multi-fold geometry as ``learned`` with 1k-16k surface points
+    (log-uniform), 10-40 % as many orientations, 3-12 surfaces, range
+    0.5-1.5 x the default and surface-point nuggets 1e-7..1e-4 (log-uniform)."""
+    rng = np.random.default_rng(7_000_003 + base_seed * 100_003 + index)
+    n_p = int(np.exp(rng.uniform(np.log(n_min), np.log(n_max))))
+    n_o = max(8, int(n_p * rng.uniform(0.1, 0.4)))
+    n_s = int(rng.integers(3, 13))
+    rm = np.sqrt(3) * 1000.0 * rng.uniform(0.5, 1.5)
+    nug = float(np.exp(rng.uniform(np.log(1e-7), np.log(1e-4))))
+    m = learned(seed=100_000 + base_seed * 100_003 + index, n_points=n_p, n_orient=n_o, n_surf=n_s, range_m=rm,
+                nug_sp=nug)
+    m.meta.update(dict(n_points=n_p, n_orient=n_o, n_surf=n_s, range_m=rm, nug_sp=nug))
+    return m

@@ -172,18 +172,21 @@ gk_status gk_solve_mixed(int64_t n, const double* K, int64_t ldk,
  * replaces).  ``perm`` (device, n entries) lists the unknowns in the new order:
  * first ``r`` landmark unknowns (r a multiple of 64; the drift unknowns must be
  * among them), then the others in spatially contiguous blocks of ``bs`` (a
- * multiple of 64).  Setup, all FP32 on the equilibrated, permuted matrix: LU
- * without pivoting of the landmark block, the landmark rows/columns
- * (the rank-r coupling), and LU of the bs x bs diagonal blocks of the Schur
- * complement.  The Krylov iteration is FP64 on the FP64 K, to
- * ||b - K x||_2 <= tol ||b||_2 or ``max_iter`` steps; ``info`` reports status,
- * iterations and the final residual.  Workspace as gk_solve_mixed. */
-size_t gk_solve_twolevel_workspace_bytes(int64_t n);
+ * multiple of 64).  Setup, in ``prec`` (GK_F32 or GK_F64) on the
+ * equilibrated, permuted matrix: LU without pivoting of the landmark block,
+ * the landmark rows/columns (the rank-r coupling), and LU of the bs x bs
+ * diagonal blocks of the Schur complement.  GK_F32 halves the setup's memory
+ * traffic but only preconditions systems with kappa(K) eps32 well below 1;
+ * GK_F64 covers the densely sampled, nugget-dominated systems beyond that.
+ * The Krylov iteration is FP64 on the FP64 K, to ||b - K x||_2 <= tol ||b||_2
+ * or ``max_iter`` steps; ``info`` reports status, iterations and the final
+ * residual. */
+size_t gk_solve_twolevel_workspace_bytes(int64_t n, gk_prec prec);
 gk_status gk_solve_twolevel(int64_t n, const double* K, int64_t ldk,
                             const double* b, double* x, const int32_t* perm,
-                            int64_t r, int32_t bs, double tol, int32_t max_iter,
-                            void* work, size_t work_bytes, gk_info* info,
-                            gk_stream stream);
+                            int64_t r, int32_t bs, gk_prec prec, double tol,
+                            int32_t max_iter, void* work, size_t work_bytes,
+                            gk_info* info, gk_stream stream);
 
 /* Allocation-free form of gk_solve_mixed, with no counterpart in the
  * reference.  It is for callers that cannot call cudaMalloc -- for example
@@ -332,6 +335,67 @@ gk_status gk_tune_describe(int32_t variant, int32_t* points_per_thread,
                            int32_t* stage_kb);
 gk_status gk_tune_set(int32_t tunable, int32_t variant);
 int32_t gk_tune_get(int32_t tunable);
+
+/* ---------------- learned preconditioner selection --------------------- */
+
+/* The network that picks the two-level preconditioner of gk_solve_twolevel
+ * (landmark count r, block size bs, landmark policy) for a system from its
+ * geometry.  No reference counterpart: the reference solves every system
+ * with the dense FP64 direct solve (``kernel_solver: 1``), which stays the
+ * fallback and the judge of every learned-path solution.
+ *
+ * A 3-layer perceptron in_dim -> 256 -> 256 -> out_dim with ReLU between
+ * layers, BF16 weights and FP32 accumulation.  ``params`` holds the weights
+ * as BF16 bit patterns: per layer a row-major n_out x (n_in + 1) matrix whose
+ * last column is the bias, layers in order (gk_mlp_param_count values). */
+#define GK_MLP_HIDDEN 256
+#define GK_MLP_MAX_IN 64
+#define GK_MLP_MAX_OUT 16
+#define GK_MLP_MAX_BATCH (1 << 22)
+#define GK_SYSTEM_FEATURES 16
+
+typedef struct gk_mlp {
+    int32_t in_dim;          /* 1 .. GK_MLP_MAX_IN   */
+    int32_t out_dim;         /* 1 .. GK_MLP_MAX_OUT  */
+    const uint16_t* params;  /* device, BF16 bits    */
+} gk_mlp;
+
+typedef struct gk_adam {
+    float lr, beta1, beta2, eps, weight_decay;
+} gk_adam;
+
+/* Number of parameters (-1 for bad dimensions). */
+int64_t gk_mlp_param_count(int32_t in_dim, int32_t out_dim);
+/* Workspace of gk_mlp_fwd / gk_mlp_bwd for ``batch`` samples (0 if invalid). */
+size_t gk_mlp_workspace_bytes(int32_t in_dim, int32_t out_dim, int64_t batch);
+/* y (batch x out_dim, FP32) = net(x) for x (batch x in_dim, FP32, row-major).
+ * Saves the hidden activations in ``work`` for gk_mlp_bwd. */
+gk_status gk_mlp_fwd(const gk_mlp* net, int64_t batch, const float* x,
+                     float* y, void* work, size_t work_bytes,
+                     gk_stream stream);
+/* grad (gk_mlp_param_count FP32, overwritten, parameter layout) = the
+ * gradient of sum(dy * y) with respect to the parameters, for the x and the
+ * activations of the preceding gk_mlp_fwd on the same ``work``.  The sample
+ * sum runs in fixed chunks added in a fixed order: bitwise reproducible. */
+gk_status gk_mlp_bwd(const gk_mlp* net, int64_t batch, const float* x,
+                     const float* dy, float* grad, void* work,
+                     size_t work_bytes, gk_stream stream);
+/* Weighted mean-squared error loss = sum_i w_i |y_i - t_i|^2 / sum_i w_i
+ * (w may be NULL: all ones) into loss[0], and its gradient dy (may be NULL). */
+gk_status gk_mlp_mse(int64_t batch, int32_t out_dim, const float* y,
+                     const float* target, const float* weight, float* dy,
+                     float* loss, gk_stream stream);
+/* One AdamW step (bias-corrected moments; decoupled weight decay) on the
+ * FP32 master parameters, then params = master rounded to BF16 (nearest
+ * even).  ``step`` counts from 1. */
+gk_status gk_mlp_adam(int64_t n, float* master, uint16_t* params,
+                      const float* grad, float* m, float* v,
+                      const gk_adam* hp, int32_t step, gk_stream stream);
+/* Geometry descriptor of a system: GK_SYSTEM_FEATURES floats (device) --
+ * sizes, position extents and spread relative to the range, orientation
+ * alignment, nugget levels, drift degree, point spacing, surface count. */
+gk_status gk_system_features(const gk_system* s, float* features,
+                             gk_stream stream);
 
 /* Library version string (HOST). */
 const char* gk_version(void);

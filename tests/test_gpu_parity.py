@@ -387,8 +387,10 @@ def test_mixed_solve_without_pivoting_on_kriging_matrix():
     assert np.linalg.norm(br - Kr @ x) <= 1e-11 * np.linalg.norm(br)
 
 
-@pytest.mark.parametrize("n_land,block", [(256, 64), (512, 128), (1024, 256)])
-def test_twolevel_fgmres_judged_by_fp64_lu(n_land, block):
+@pytest.mark.parametrize("n_land,block,prec,policy", [(256, 64, 1, "random"), (512, 128, 1, "stratified"),
+                                                      (1024, 256, 1, "random"), (256, 64, 0, "stratified"),
+                                                      (1024, 256, 0, "random")])
+def test_twolevel_fgmres_judged_by_fp64_lu(n_land, block, prec, policy):
     """Block-Jacobi + low-rank preconditioned FGMRES reaches 1e-8; the FP64 LU
     (plain form) judges the solution."""
     from gempy_gb300 import kernels as K
@@ -397,7 +399,8 @@ def test_twolevel_fgmres_judged_by_fp64_lu(n_land, block):
     (s,) = oracle_series_list(m)
     ds = _dev_series(s)
     Kt, bt = K.build(ds, K.GK_F64)
-    x, info, r = K.solve_twolevel(ds, n_landmarks=n_land, block=block, tol=1e-8, K=Kt, b=bt)
+    x, info, r = K.solve_twolevel(ds, n_landmarks=n_land, block=block, tol=1e-8, K=Kt, b=bt, prec=prec,
+                                  policy=policy)
     inf = K.read_info(info)
     assert inf["status"] == 0, inf
     assert inf["residual"] <= 1e-8
