@@ -181,9 +181,19 @@ def main():
     ap.add_argument("--grid", type=int, default=256)
     ap.add_argument("--no-extra", action="store_true", help="skip the batch and octree sections")
     ap.add_argument("--batch-realisations", type=int, default=512)
+    ap.add_argument("--only-learned", action="store_true",
+                    help="run only the config-5 section (learned two-level solve vs FP64 LU) and print it")
+    ap.add_argument("--learned-points", type=int, default=20000,
+                    help="surface points of the config-5 system (orientations: 30 %%)")
+    ap.add_argument("--learned-config", default=None,
+                    help="landmarks,block,policy,f32|f64: use this two-level configuration instead of the network's")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
+    if args.only_learned:
+        print(json.dumps({"learned": learned_section(args.learned_points, args.learned_config)}, default=float),
+              flush=True)
+        return
 
     import torch
     import torch.distributed as dist
@@ -409,6 +419,7 @@ def main():
     if not args.no_extra:
         line["batch"] = batch_section(n_real=args.batch_realisations)
         line["octree"] = octree_section()
+        line["learned"] = learned_section(args.learned_points, args.learned_config)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(m)
     if rank == 0:
@@ -521,6 +532,79 @@ def octree_section():
     out["ids_identical_last_level"] = bool(np.array_equal(a, b))
     out["speedup_vs_plain_fp64"] = out["plain_fp64"]["ms"] / out["mixed"]["ms"]
     return out
+
+
+def learned_section(n_points=20000, force_config=None):
+    """Config 5: one 20000-point / 6000-orientation multi-fold system
+    (N = 37993; ``n_points`` scales it down for profiling).  Plain FP64 form (build + blocked LU + solves) against the
+    learned form (network picks the two-level configuration, FGMRES to 1e-8,
+    FP64 LU fallback), with the fixed default configuration as the ablation;
+    the LU solution judges the scalar field.  Also times the network kernels."""
+    import torch
+    from gempy_gb300 import kernels as K
+    from gempy_gb300 import learned, synthetic
+    forced = None
+    if force_config:
+        r_, bs_, pol_, pr_ = force_config.split(",")
+        forced = learned.PrecondConfig(int(r_), int(bs_), pol_, K.GK_F64 if pr_ == "f64" else K.GK_F32)
+    elif not os.path.exists(learned.DEFAULT_MODEL):
+        return {"unavailable": "no trained model in the package"}
+    model = None if forced else learned.CostModel.load()
+    m = synthetic.learned(n_points=n_points, n_orient=int(0.3 * n_points))
+    s = learned.series_of(m)
+
+    def clock(fn):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return r, time.perf_counter() - t
+
+    (Kt, bt), t_build = clock(lambda: K.build(s, K.GK_F64))
+    N = int(Kt.shape[0])
+    (x_lu, _), t_lu = clock(lambda: learned.solve_plain_K(Kt, bt))
+    pts = learned.judge_points(s)
+    f_lu = learned.field_at(s, x_lu, pts)
+    res, t_learned = clock(lambda: learned.solve_learned(s, model, Kt, bt, tol=1e-8, config=forced))
+    err = learned.field_error(s, res.x, f_lu, pts)
+    (xd, infd), t_def = clock(lambda: learned.solve_with(s, learned.DEFAULT_CONFIG, Kt, bt, 1e-8))
+    def_ok = int(infd["status"]) == 0
+    t_def_total = t_def if def_ok else t_def + t_lu
+    # network kernels: inference over a large batch and one training step
+    if model is None:
+        model = learned.CostModel(learned.Mlp(), np.zeros(learned.IN_DIM), np.ones(learned.IN_DIM),
+                                  np.zeros(learned.OUT_DIM), np.ones(learned.OUT_DIM), {"untrained": True})
+    B = 65536
+    x = torch.randn(B, learned.IN_DIM, device="cuda")
+    for _ in range(3):
+        model.mlp.forward(x)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    reps = 10
+    for _ in range(reps):
+        model.mlp.forward(x)
+    ev1.record()
+    torch.cuda.synchronize()
+    fwd_ms = ev0.elapsed_time(ev1) / reps
+    flops = 2.0 * B * (256 * (learned.IN_DIM + 1) + 256 * 257 + learned.OUT_DIM * 257)
+    return {
+        "workload": f"{n_points} surface points, {int(0.3 * n_points)} orientations, 10 folded surfaces, "
+                    "linear drift",
+        "N": N,
+        "build_s": t_build,
+        "plain_fp64_lu_s": t_lu,
+        "learned": {"s": t_learned, "config": None if res.config is None else vars(res.config),
+                    "iterations": res.iterations, "residual": res.residual, "fallback_to_lu": res.fallback,
+                    "choose_ms": 1e3 * res.seconds_choose, "field_rel_err_vs_lu": err},
+        "default_config": {"s": t_def_total, "config": vars(learned.DEFAULT_CONFIG), "converged": def_ok,
+                           "iterations": int(infd["iterations"])},
+        "solves_per_s": {"plain_fp64": 1.0 / t_lu, "learned": 1.0 / t_learned,
+                         "default_config": 1.0 / t_def_total},
+        "speedup_vs_plain_fp64": t_lu / t_learned,
+        "gain_vs_default_config": t_def_total / t_learned,
+        "network": {"samples_per_forward": B, "forward_ms": fwd_ms, "forward_tflops": flops / (fwd_ms * 1e-3) / 1e12,
+                    "training": model.meta},
+    }
 
 
 def cpu_baseline(m, sample=4096):

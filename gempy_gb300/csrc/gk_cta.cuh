@@ -134,10 +134,16 @@ static __device__ void cta_lu_solve(const T* A, int ld, int N, T* t, T* xs) {
     for (int k = 0; k < N; k += kLNB) {
         const int kb = min(kLNB, N - k);
         if (wid == 0) {
+            // the lane's row of the diagonal block, loaded before the serial sweep
+            T arow[kLNB];
+            const T* ar = A + (int64_t)(k + (lane < kb ? lane : 0)) * ld + k;
+#pragma unroll
+            for (int c = 0; c < kLNB; ++c) arow[c] = c < kb ? ar[c] : (T)0;
             T v = lane < kb ? t[k + lane] : (T)0;
-            for (int c = 0; c < kb; ++c) {
+#pragma unroll
+            for (int c = 0; c < kLNB; ++c) {
                 const T xc = __shfl_sync(0xffffffffu, v, c);
-                if (lane > c && lane < kb) v -= A[(int64_t)(k + lane) * ld + k + c] * xc;
+                if (lane > c && lane < kb) v -= arow[c] * xc;
             }
             if (lane < kb) { t[k + lane] = v; xs[lane] = v; }
         }
@@ -155,12 +161,20 @@ static __device__ void cta_lu_solve(const T* A, int ld, int N, T* t, T* xs) {
         const int k = bk * kLNB;
         const int kb = min(kLNB, N - k);
         if (wid == 0) {
+            T arow[kLNB];
+            const T* ar = A + (int64_t)(k + (lane < kb ? lane : 0)) * ld + k;
+#pragma unroll
+            for (int c = 0; c < kLNB; ++c) arow[c] = c < kb ? ar[c] : (T)0;
             T v = lane < kb ? t[k + lane] : (T)0;
-            for (int c = kb - 1; c >= 0; --c) {
-                T mine = __shfl_sync(0xffffffffu, v, c);
-                T xc = mine / A[(int64_t)(k + c) * ld + k + c];
-                if (lane == c) v = xc;
-                if (lane < c) v -= A[(int64_t)(k + lane) * ld + k + c] * xc;
+#pragma unroll
+            for (int c = kLNB - 1; c >= 0; --c) {
+                if (c < kb) {  // warp-uniform
+                    const T mine = __shfl_sync(0xffffffffu, v, c);
+                    const T dcc = __shfl_sync(0xffffffffu, arow[c], c);
+                    const T xc = mine / dcc;
+                    if (lane == c) v = xc;
+                    if (lane < c) v -= arow[c] * xc;
+                }
             }
             if (lane < kb) { t[k + lane] = v; xs[lane] = v; }
         }

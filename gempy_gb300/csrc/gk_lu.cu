@@ -1192,19 +1192,76 @@ __global__ void __launch_bounds__(256) block_solve_kernel(const T* A, int64_t ld
     cta_lu_solve(A + b0 * lda + b0, (int)lda, nb, t + b0, xs);
 }
 
-// y[i] -= sum_j A[i][j] x[j], i in [r_lo, r_hi), j in [c_lo, c_hi); warp per row
+// y[i] -= sum_j A[i][j] x[j], i in [r_lo, r_hi), j in [c_lo, c_hi).  One warp
+// per kRectRows consecutive rows, so each x element is loaded once for all of
+// them; 16-byte loads of A when the row segments are 16-byte aligned.
+constexpr int kRectRows = 4;
+
+template <typename T> struct Vec16;
+template <> struct Vec16<float> {
+    static constexpr int W = 4;
+    __device__ static void load(const float* p, float* o) {
+        const float4 v = *reinterpret_cast<const float4*>(p);
+        o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+    }
+};
+template <> struct Vec16<double> {
+    static constexpr int W = 2;
+    __device__ static void load(const double* p, double* o) {
+        const double2 v = *reinterpret_cast<const double2*>(p);
+        o[0] = v.x; o[1] = v.y;
+    }
+};
+
 template <typename T>
-__global__ void rect_gemv_kernel(const T* __restrict__ A, int64_t lda, int64_t r_lo, int64_t r_hi, int64_t c_lo,
-                                 int64_t c_hi, const T* __restrict__ x, T* __restrict__ y) {
-    const int64_t row = r_lo + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+__global__ void __launch_bounds__(256) rect_gemv_kernel(const T* __restrict__ A, int64_t lda, int64_t r_lo,
+                                                        int64_t r_hi, int64_t c_lo, int64_t c_hi,
+                                                        const T* __restrict__ x, T* __restrict__ y) {
+    constexpr int W = Vec16<T>::W;
+    const int64_t row0 = r_lo + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kRectRows;
     const int lane = threadIdx.x & 31;
-    if (row >= r_hi) return;
-    const T* a = A + row * lda;
-    T s = (T)0;
-    for (int64_t j = c_lo + lane; j < c_hi; j += 32) s = cta_fma(a[j], x[j], s);
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if (lane == 0) y[row] -= s;
+    if (row0 >= r_hi) return;
+    const int nr = (int)min((int64_t)kRectRows, r_hi - row0);
+    T acc[kRectRows];
+#pragma unroll
+    for (int r = 0; r < kRectRows; ++r) acc[r] = (T)0;
+    int64_t j0 = c_lo;
+    if ((lda % W) == 0 && (c_lo % W) == 0 && ((uintptr_t)A % 16) == 0) {
+        const int64_t nv = (c_hi - c_lo) / W;
+        for (int64_t q = lane; q < nv; q += 32) {
+            const int64_t j = c_lo + q * W;
+            T xv[W];
+#pragma unroll
+            for (int e = 0; e < W; ++e) xv[e] = x[j + e];
+#pragma unroll
+            for (int r = 0; r < kRectRows; ++r) {
+                if (r < nr) {
+                    T av[W];
+                    Vec16<T>::load(A + (row0 + r) * lda + j, av);
+#pragma unroll
+                    for (int e = 0; e < W; ++e) acc[r] = cta_fma(av[e], xv[e], acc[r]);
+                }
+            }
+        }
+        j0 = c_lo + nv * W;
+    }
+    for (int64_t j = j0 + lane; j < c_hi; j += 32) {
+        const T xv = x[j];
+#pragma unroll
+        for (int r = 0; r < kRectRows; ++r)
+            if (r < nr) acc[r] = cta_fma(A[(row0 + r) * lda + j], xv, acc[r]);
+    }
+#pragma unroll
+    for (int r = 0; r < kRectRows; ++r)
+        for (int o = 16; o > 0; o >>= 1) acc[r] += __shfl_down_sync(0xffffffffu, acc[r], o);
+    if (lane == 0) {
+#pragma unroll
+        for (int r = 0; r < kRectRows; ++r)
+            if (r < nr) y[row0 + r] -= acc[r];
+    }
 }
+
+static unsigned rect_blocks(int64_t rows) { return (unsigned)(((rows + kRectRows - 1) / kRectRows * 32 + 255) / 256); }
 
 template <typename T>
 __global__ void permute_scale_kernel(const double* __restrict__ K, int64_t ldk, int64_t n,
@@ -1364,14 +1421,14 @@ static gk_status twolevel_apply(int64_t n, const T* A, int64_t lda, const int32_
     GK_CUDA_TRY(cudaMemsetAsync(flags, 0, ((size_t)nblk_r + 1) * kFlagStride * sizeof(int), st));
     trsv_kernel<T><<<nblk_r, 256, 0, st>>>(A, lda, r, t, lu_ws_dinv<T>(work, r, 0), 1, counter, flags, info);
     GK_LAUNCH_CHECK();
-    rect_gemv_kernel<T><<<(unsigned)(((n - r) * 32 + 255) / 256), 256, 0, st>>>(A, lda, r, n, 0, r, t, t);
+    rect_gemv_kernel<T><<<rect_blocks(n - r), 256, 0, st>>>(A, lda, r, n, 0, r, t, t);
     GK_LAUNCH_CHECK();
     // block-Jacobi on the Schur complement
     const int64_t nblk = (n - r + bs - 1) / bs;
     block_solve_kernel<T><<<(unsigned)nblk, 256, 0, st>>>(A, lda, r, n, bs, t);
     GK_LAUNCH_CHECK();
     // backward: t_L -= U_LR x_R, then U_LL x_L = t_L
-    rect_gemv_kernel<T><<<(unsigned)((r * 32 + 255) / 256), 256, 0, st>>>(A, lda, 0, r, r, n, t, t);
+    rect_gemv_kernel<T><<<rect_blocks(r), 256, 0, st>>>(A, lda, 0, r, r, n, t, t);
     GK_LAUNCH_CHECK();
     GK_CUDA_TRY(cudaMemsetAsync(flags, 0, ((size_t)nblk_r + 1) * kFlagStride * sizeof(int), st));
     trsv_kernel<T><<<nblk_r, 256, 0, st>>>(A, lda, r, t, lu_ws_dinv<T>(work, r, 1), 0, counter, flags, info);

@@ -18,6 +18,7 @@ Flow per call, all arithmetic on the GPU through ``libgempy_gb300.so``:
      octree levels refine voxels whose corner ids differ.
 There is no CPU path: without the CUDA library this raises.
 """
+import os
 import time
 from dataclasses import dataclass, field as dc_field
 from typing import Optional
@@ -39,7 +40,13 @@ class EngineConfig:
     float-float on the FP32 pipe (cubic kernel; other kernels evaluate in
     FP64) with FP64 isovalues.  ``eval_precision`` overrides the evaluation
     arithmetic ("f64", "ff" or "f32"; "f32" is only accurate to ~1e-7 times
-    the cancellation factor sum|w_j k_j| / |Z| of the kriging sum)."""
+    the cancellation factor sum|w_j k_j| / |Z| of the kriging sum).
+
+    In the mixed form, series with at least ``learned_min_n`` unknowns are
+    solved by FGMRES to ``learned_tol`` with the two-level preconditioner the
+    trained network picks (``learned.py``; FP64 LU fallback) when a trained
+    model is available (``learned_model``, default: the packaged one);
+    ``learned_min_n`` = 0 disables this."""
     dtype: str = "float64"
     use_gpu: bool = True
     keep_on_device: bool = False
@@ -47,6 +54,9 @@ class EngineConfig:
     solver_max_iter: int = 60
     eval_precision: Optional[str] = None
     timings: bool = False
+    learned_min_n: int = 16384
+    learned_tol: float = 1e-8
+    learned_model: Optional[str] = None
 
 
 class _Series:
@@ -63,6 +73,27 @@ class _Series:
 
     def set_slope(self, slope):
         self.seg.slope = float(slope)
+
+
+def _load_cost_model(path, device):
+    from . import learned
+    path = path or learned.DEFAULT_MODEL
+    if not os.path.exists(path):
+        return None
+    return learned.CostModel.load(path, device=device)
+
+
+def _solve_learned(dev_s, cost_model, tol):
+    """Network-chosen two-level FGMRES (FP64 LU fallback); (w, gk_info tensor)."""
+    from . import learned
+    r = learned.solve_learned(dev_s, cost_model, tol=tol)
+    rec = np.zeros(1, dtype=K.INFO_DTYPE)
+    rec["status"] = 0 if r.fallback or r.status == 0 else r.status
+    rec["iterations"] = r.iterations
+    rec["where"] = int(r.fallback)  # 1: FGMRES missed the tolerance and the FP64 LU produced w
+    rec["residual"] = r.residual
+    info = torch.as_tensor(np.frombuffer(rec.tobytes(), dtype=np.uint8).copy()).to(dev_s.device)
+    return r.x, info
 
 
 def _split(interpolation_input, options, data_descriptor, device):
@@ -158,8 +189,14 @@ def compute_model(interpolation_input, options, data_descriptor, geophysics_inpu
     # ---- 1-2: per-series solve
     uv = np.asarray(interpolation_input.unit_values, dtype=np.float64)
     series = []
+    cost_model = None
     for dev_s, s_off, n_s, rel in _split(interpolation_input, options, data_descriptor, device):
-        if mixed:
+        if mixed and cfg.learned_min_n > 0 and dev_s.N >= cfg.learned_min_n:
+            if cost_model is None:
+                cost_model = _load_cost_model(cfg.learned_model, device)
+        if mixed and cost_model is not None and dev_s.N >= cfg.learned_min_n:
+            w, info = _solve_learned(dev_s, cost_model, cfg.learned_tol)
+        elif mixed:
             w, info = K.solve_mixed(dev_s, tol=cfg.solver_tol, max_iter=cfg.solver_max_iter)
         else:
             w, info = K.solve_plain(dev_s)

@@ -8,7 +8,9 @@ the block size, the landmark policy and the storage precision.  A small
 network (3 layers, width 256, BF16 weights, FP32 accumulation; CUDA forward,
 backward and AdamW kernels in ``gk_mlp.cu``) maps the system's geometry
 descriptor (``gk_system_features``) plus one candidate configuration to the
-predicted log solve time; the cheapest predicted candidate is used.  The
+predicted log time of the FGMRES run, the probability that it fails, and the
+log time of the LU fallback; the candidate with the least expected cost
+t_run + p_fail t_lu is used.  The
 dense FP64 LU is the fallback (a candidate that does not reach the tolerance
 falls back to it) and the judge (training labels record each candidate's
 error against the LU solution; a run whose FGMRES residual meets the
@@ -31,7 +33,9 @@ from ._lib import GK_F32, GK_F64, GK_SYSTEM_FEATURES, GkAdam, GkMlp, check
 
 CONFIG_FEATURES = 4
 IN_DIM = GK_SYSTEM_FEATURES + CONFIG_FEATURES
-OUT_DIM = 1
+# outputs: log(seconds of the FGMRES run), failure indicator, log(seconds of the FP64 LU fallback)
+OUT_DIM = 3
+MAX_ITER = 1000
 JUDGE_TOL = 1e-6          # relative scalar-field error of an accepted solution vs the FP64 LU's
 DEFAULT_MODEL = os.path.join(os.path.dirname(os.path.abspath(__file__)), "models", "precond_cost.npz")
 
@@ -50,7 +54,7 @@ class PrecondConfig:
 
 
 CANDIDATES = tuple(PrecondConfig(r, bs, pol, pr)
-                   for r in (512, 1024, 2048, 4096, 8192)
+                   for r in (512, 1024, 2048, 4096, 8192, 16384)
                    for bs in (256, 512)
                    for pol in kernels.LANDMARK_POLICIES
                    for pr in (GK_F32, GK_F64))
@@ -199,18 +203,24 @@ class CostModel:
         self.mlp = mlp
         self.x_mean = np.asarray(x_mean, np.float32)
         self.x_std = np.asarray(x_std, np.float32)
-        self.y_mean, self.y_std = float(y_mean), float(y_std)
+        self.y_mean = np.asarray(y_mean, np.float64).reshape(-1)
+        self.y_std = np.asarray(y_std, np.float64).reshape(-1)
         self.meta = meta or {}
 
     def _norm(self, X):
         return (np.asarray(X, np.float32) - self.x_mean) / self.x_std
 
-    def predict_log_seconds(self, sys_feats, configs):
-        """Predicted log(seconds) of each candidate configuration."""
+    def predict(self, sys_feats, configs):
+        """Per candidate: (run seconds, failure probability, LU seconds)."""
         sf = np.asarray(sys_feats, np.float32).reshape(1, -1)
         X = np.concatenate([np.repeat(sf, len(configs), 0), np.stack([c.features() for c in configs])], 1)
-        y = self.mlp.forward(torch.as_tensor(self._norm(X)).to(self.mlp.device))
-        return y[:, 0].cpu().numpy() * self.y_std + self.y_mean
+        y = self.mlp.forward(torch.as_tensor(self._norm(X)).to(self.mlp.device)).cpu().numpy().astype(np.float64)
+        y = y * self.y_std + self.y_mean
+        return np.exp(y[:, 0]), np.clip(y[:, 1], 0.0, 1.0), np.exp(y[:, 2])
+
+    def expected_cost(self, sys_feats, configs):
+        t_run, p_fail, t_lu = self.predict(sys_feats, configs)
+        return t_run + p_fail * t_lu
 
     def choose(self, series, N=None):
         N = series.N if N is None else N
@@ -218,8 +228,7 @@ class CostModel:
         if not cands:
             return None
         feats = system_features(series).cpu().numpy()
-        pred = self.predict_log_seconds(feats, cands)
-        return cands[int(np.argmin(pred))]
+        return cands[int(np.argmin(self.expected_cost(feats, cands)))]
 
     def save(self, path):
         os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
@@ -231,32 +240,38 @@ class CostModel:
     def load(cls, path=DEFAULT_MODEL, device="cuda"):
         z = np.load(path, allow_pickle=False)
         st = {k[4:]: z[k] for k in z.files if k.startswith("mlp_")}
-        return cls(Mlp.from_state(st, device), z["x_mean"], z["x_std"], float(z["y_mean"]), float(z["y_std"]),
+        return cls(Mlp.from_state(st, device), z["x_mean"], z["x_std"], z["y_mean"], z["y_std"],
                    json.loads(str(z["meta"])))
 
 
-def train(dataset, epochs=400, batch=512, lr=2e-3, weight_decay=1e-4, seed=0, model=None, device="cuda",
+def targets(dataset):
+    """Network targets: log run seconds, failure indicator, log LU seconds."""
+    return np.stack([np.log(dataset["t_run"]), 1.0 - dataset["ok"], np.log(dataset["t_lu"])], 1)
+
+
+def train(dataset, epochs=300, batch=256, lr=2e-3, weight_decay=1e-3, seed=0, model=None, device="cuda",
           log_every=0):
     """Fit (or, given ``model``, continue fitting) the cost model on a dataset
-    from ``generate``: inputs = system features + config features, label =
-    log(seconds) of the solve with the LU fallback's time added when the
-    candidate failed.  Returns (model, per-epoch mean losses)."""
+    from ``generate`` with AdamW under a cosine learning-rate schedule.
+    Returns (model, per-epoch mean losses)."""
     X = np.concatenate([dataset["sys_feats"], dataset["cfg_feats"]], 1).astype(np.float32)
-    y = np.log(dataset["cost_s"]).astype(np.float32)
+    Y = targets(dataset)
     if model is None:
         x_mean, x_std = X.mean(0), X.std(0) + 1e-3
-        model = CostModel(Mlp(IN_DIM, OUT_DIM, seed=seed, device=device), x_mean, x_std, y.mean(), y.std() + 1e-6)
+        model = CostModel(Mlp(IN_DIM, OUT_DIM, seed=seed, device=device), x_mean, x_std, Y.mean(0),
+                          Y.std(0) + 1e-6)
     Xn = torch.as_tensor(model._norm(X)).to(device)
-    yn = torch.as_tensor(((y - model.y_mean) / model.y_std)[:, None]).to(device)
+    Yn = torch.as_tensor(((Y - model.y_mean) / model.y_std).astype(np.float32)).to(device)
     rng = np.random.default_rng(seed)
     n = len(X)
     hist = []
     for ep in range(epochs):
+        lr_ep = lr * 0.5 * (1.0 + np.cos(np.pi * ep / max(epochs, 1)))
         order = torch.as_tensor(rng.permutation(n)).to(device)
         losses = []
         for i in range(0, n, batch):
             idx = order[i:i + batch]
-            losses.append(model.mlp.train_step(Xn[idx], yn[idx], lr=lr, weight_decay=weight_decay))
+            losses.append(model.mlp.train_step(Xn[idx], Yn[idx], lr=lr_ep, weight_decay=weight_decay))
         hist.append(float(torch.stack(losses).mean()))
         if log_every and ep % log_every == 0:
             print(f"epoch {ep} loss {hist[-1]:.4f}", flush=True)
@@ -277,7 +292,7 @@ class LearnedResult:
     seconds_choose: float
 
 
-def solve_with(series, cfg, K, b, tol=1e-8, max_iter=600, seed=0):
+def solve_with(series, cfg, K, b, tol=1e-8, max_iter=MAX_ITER, seed=0):
     x, info, _ = kernels.solve_twolevel(series, n_landmarks=cfg.landmarks, block=cfg.block, tol=tol,
                                         max_iter=max_iter, K=K, b=b, seed=seed, policy=cfg.policy, prec=cfg.prec)
     return x, kernels.read_info(info)
@@ -289,12 +304,13 @@ def solve_plain_K(K, b):
     return kernels.lu_solve(f, b), kernels.read_info(f.info)
 
 
-def solve_learned(series, model, K=None, b=None, tol=1e-8, max_iter=600):
-    """Solve with the configuration the network picks; FP64 LU if it fails."""
+def solve_learned(series, model, K=None, b=None, tol=1e-8, max_iter=MAX_ITER, config=None):
+    """Solve with the configuration the network picks (or ``config``); FP64
+    LU if FGMRES misses the tolerance."""
     if K is None:
         K, b = kernels.build(series, GK_F64)
     t0 = time.perf_counter()
-    cfg = model.choose(series, K.shape[0])
+    cfg = config if config is not None else model.choose(series, K.shape[0])
     t_choose = time.perf_counter() - t0
     if cfg is None:
         x, inf = solve_plain_K(K, b)
@@ -348,7 +364,7 @@ def field_error(series, w, f_ref, pts):
     return float((f - f_ref).abs().max() / f_ref.abs().max())
 
 
-def label_system(series, configs, tol=1e-8, max_iter=600, K=None, b=None):
+def label_system(series, configs, tol=1e-8, max_iter=MAX_ITER, K=None, b=None):
     """Run every config on one system; the FP64 LU solution is the judge:
     a run counts as solved when FGMRES met the tolerance and its scalar field
     matches the LU solution's within JUDGE_TOL (relative, at judge_points).
@@ -371,14 +387,14 @@ def label_system(series, configs, tol=1e-8, max_iter=600, K=None, b=None):
     return rows, t_lu
 
 
-def generate(n_systems, base_seed=0, configs_per_system=12, tol=1e-8, max_iter=600, n_min=1000, n_max=16000,
+def generate(n_systems, base_seed=0, configs_per_system=12, tol=1e-8, max_iter=MAX_ITER, n_min=1000, n_max=16000,
              seed=0, log=None):
     """Training data: ``n_systems`` systems of ``synthetic.training_system``,
     each labelled on a random subset of the candidates (all of them if
     configs_per_system <= 0)."""
     from . import synthetic
     rng = np.random.default_rng(seed)
-    sys_feats, cfg_feats, cost, records = [], [], [], []
+    sys_feats, cfg_feats, cost, t_run, okl, t_lus, records = [], [], [], [], [], [], []
     for i in range(n_systems):
         m = synthetic.training_system(i, base_seed, n_min, n_max)
         s = series_of(m)
@@ -386,18 +402,29 @@ def generate(n_systems, base_seed=0, configs_per_system=12, tol=1e-8, max_iter=6
         cands = candidates_for(N)
         if configs_per_system > 0 and len(cands) > configs_per_system:
             cands = [cands[j] for j in rng.choice(len(cands), configs_per_system, replace=False)]
-        feats = system_features(s).cpu().numpy()
-        rows, t_lu = label_system(s, cands, tol, max_iter)
+        try:
+            feats = system_features(s).cpu().numpy()
+            rows, t_lu = label_system(s, cands, tol, max_iter)
+        except (RuntimeError, _lib.GkError) as e:  # a failed judge: skip the system, keep going
+            if log:
+                log(f"system {i}: N={N} skipped ({e})")
+            continue
         for r in rows:
             cfg = PrecondConfig(**r["config"])
             sys_feats.append(feats)
             cfg_feats.append(cfg.features())
             cost.append(r["cost_s"])
+            t_run.append(r["seconds"])
+            okl.append(float(r["ok"]))
+            t_lus.append(t_lu)
         records.append(dict(index=i, N=N, lu_seconds=t_lu, meta={k: float(v) for k, v in m.meta.items()},
                             runs=rows))
         if log:
             best = min(rows, key=lambda r: r["cost_s"])
             log(f"system {i}: N={N} lu={t_lu:.3f}s best={best['config']} {best['cost_s']:.3f}s "
                 f"ok={sum(r['ok'] for r in rows)}/{len(rows)}")
+        del s, m
+        torch.cuda.empty_cache()
     return dict(sys_feats=np.asarray(sys_feats, np.float32), cfg_feats=np.asarray(cfg_feats, np.float32),
-                cost_s=np.asarray(cost, np.float64)), records
+                cost_s=np.asarray(cost, np.float64), t_run=np.asarray(t_run, np.float64),
+                ok=np.asarray(okl, np.float64), t_lu=np.asarray(t_lus, np.float64)), records

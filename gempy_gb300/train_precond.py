@@ -39,7 +39,8 @@ def evaluate(model, n_systems, base_seed, n_min, n_max, log=print):
         by = {learned.PrecondConfig(**r["config"]): r for r in rows}
         best = min(rows, key=lambda r: r["cost_s"])
         rec = dict(N=N, lu_seconds=t_lu, pick=by[pick], default=by[learned.DEFAULT_CONFIG], best=best,
-                   rank_of_pick=int(sorted(r["cost_s"] for r in rows).index(by[pick]["cost_s"])))
+                   rank_of_pick=int(sorted(r["cost_s"] for r in rows).index(by[pick]["cost_s"])), runs=rows,
+                   sys_feats=learned.system_features(s).cpu().numpy().tolist())
         out.append(rec)
         log(f"held-out {i}: N={N} lu={t_lu:.3f}s pick={by[pick]['cost_s']:.3f}s (ok={by[pick]['ok']}) "
             f"default={rec['default']['cost_s']:.3f}s best={best['cost_s']:.3f}s")
@@ -51,6 +52,7 @@ def main(argv=None):
     ap.add_argument("--systems", type=int, default=90)
     ap.add_argument("--large", type=int, default=6, help="extra systems with 12k-20k surface points")
     ap.add_argument("--configs", type=int, default=12)
+    ap.add_argument("--large-configs", type=int, default=16)
     ap.add_argument("--epochs", type=int, default=300)
     ap.add_argument("--heldout", type=int, default=6)
     ap.add_argument("--seed", type=int, default=0)
@@ -68,7 +70,7 @@ def main(argv=None):
     else:
         ds1, rec1 = learned.generate(a.systems, base_seed=a.seed, configs_per_system=a.configs, n_min=1000,
                                      n_max=8000, seed=a.seed, log=print)
-        ds2, rec2 = learned.generate(a.large, base_seed=a.seed + 50, configs_per_system=a.configs, n_min=12000,
+        ds2, rec2 = learned.generate(a.large, base_seed=a.seed + 50, configs_per_system=a.large_configs, n_min=12000,
                                      n_max=20000, seed=a.seed + 1, log=print)
         ds = {k: np.concatenate([ds1[k], ds2[k]]) for k in ds1}
         records = rec1 + rec2
@@ -82,7 +84,8 @@ def main(argv=None):
     model = learned.CostModel.load(a.resume) if a.resume else None
     torch.cuda.synchronize()
     t1 = time.perf_counter()
-    model, hist = learned.train(ds, epochs=a.epochs, batch=256, lr=2e-3, seed=a.seed, model=model, log_every=50)
+    model, hist = learned.train(ds, epochs=a.epochs, batch=256, lr=2e-3, weight_decay=1e-3, seed=a.seed, model=model,
+                                log_every=50)
     torch.cuda.synchronize()
     summary["train_seconds"] = time.perf_counter() - t1
     summary["train_steps"] = int(model.mlp.step)

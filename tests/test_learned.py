@@ -63,7 +63,7 @@ def test_config_features_and_candidates():
     from gempy_gb300 import learned
     assert learned.IN_DIM == 20
     c = learned.CANDIDATES
-    assert len(c) == len(set(c)) == 40
+    assert len(c) == len(set(c)) == 48
     f = np.stack([x.features() for x in c])
     assert np.unique(f, axis=0).shape[0] == len(c)
     assert all(x.landmarks <= 3000 for x in learned.candidates_for(6000))
@@ -197,8 +197,9 @@ def test_training_reduces_loss():
     rng = np.random.default_rng(6)
     X = rng.normal(0, 1, (4096, learned.IN_DIM)).astype(np.float32)
     y = (np.sin(X[:, 0]) + 0.5 * X[:, 1] * X[:, 2] - 0.3 * X[:, 3] ** 2).astype(np.float64)
-    ds = dict(sys_feats=X[:, :16], cfg_feats=X[:, 16:], cost_s=np.exp(y))
-    model, hist = learned.train(ds, epochs=60, batch=256, lr=2e-3, seed=0)
+    ds = dict(sys_feats=X[:, :16], cfg_feats=X[:, 16:], t_run=np.exp(y), ok=(X[:, 5] > 0).astype(float),
+              t_lu=np.exp(0.5 * X[:, 6]))
+    model, hist = learned.train(ds, epochs=60, batch=256, lr=2e-3, weight_decay=1e-4, seed=0)
     assert hist[-1] < 0.1 * hist[0], hist[::10]
     # checkpoint round trip, then training resumes from the saved state
     st = model.mlp.state()
