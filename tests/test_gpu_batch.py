@@ -104,6 +104,11 @@ def test_every_tile_variant_gives_the_same_field():
     model = K.prepare(ds, torch.as_tensor(w, device="cuda"))
     pts = K.Points.regular(m.interpolation_input.grid.dense_grid)
     br = BatchRunner(_models(4))
+    # plain FP32 sums are accurate to ~1e-7 x the cancellation factor of the kriging sum
+    f64, _, _, _ = K.evaluate(ds, model, pts, K.GK_F64)
+    zmax = float(f64.abs().max())
+    alpha = kriging.point_coefficients(s, w)
+    cancel = s.c_o * s.gi_res * (np.abs(alpha).sum() + np.abs(w[:3 * s.n_o]).sum() * 14 / s.range) / zmax
     saved = {t: lib.gk_tune_get(t) for t in range(3)}
     try:
         for prec, fam in ((K.GK_FF, _lib.GK_TUNE_EVAL_FF), (K.GK_F32, _lib.GK_TUNE_EVAL_F32)):
@@ -114,7 +119,7 @@ def test_every_tile_variant_gives_the_same_field():
                 f = f.cpu().numpy()
                 if ref is None:
                     ref = f
-                tol = 1e-9 if prec == K.GK_FF else 1e-6   # float-float accuracy / FP32 bound
+                tol = 1e-9 if prec == K.GK_FF else 2e-6 * cancel   # float-float accuracy / FP32 bound
                 assert np.abs(f - ref).max() <= tol * np.abs(ref).max(), (prec, v)
         ref = None
         for v in autotune.variants():
