@@ -77,6 +77,25 @@ def test_training_system_is_deterministic():
     assert 1000 <= a.meta["n_points"] <= 16000
 
 
+def test_packaged_model_is_consistent():
+    """The shipped network: BF16 weights of the right shape, the master copy
+    they round from, and finite predictions through the oracle."""
+    from gempy_gb300 import learned
+    if not os.path.exists(learned.DEFAULT_MODEL):
+        pytest.skip("no trained model in the package")
+    z = np.load(learned.DEFAULT_MODEL)
+    F, O = int(z["mlp_in_dim"]), int(z["mlp_out_dim"])
+    assert (F, O) == (learned.IN_DIM, learned.OUT_DIM)
+    bits = z["mlp_params"].view(np.uint16)
+    assert bits.size == omlp.param_count(F, O)
+    assert np.array_equal(bits, omlp.bf16_bits(z["mlp_master"]))
+    p = omlp.bf16_value(bits).astype(np.float64)
+    X = np.random.default_rng(0).normal(0, 1, (48, F))
+    y, _ = omlp.forward(p, X, F, O)
+    assert np.isfinite(y).all()
+    assert z["x_mean"].shape == (F,) and z["y_mean"].shape == (O,)
+
+
 # ---------------------------------------------------------------- GPU ------
 def _net(F, O, seed):
     from gempy_gb300 import learned
@@ -245,3 +264,28 @@ def test_learned_choice_beats_fixed_configuration():
         t_default += rows[1]["cost_s"]
         assert rows[0]["ok"], rows[0]
     assert t_learned < 0.8 * t_default, (t_learned, t_default)
+
+
+@pytest.mark.gpu
+def test_compute_model_routes_large_series_through_learned_solve():
+    """compute_model (mixed form) with the learned solve enabled for the
+    series gives the plain FP64 form's field within 1e-6 and the same ids
+    outside the isovalue band."""
+    import gempy_gb300 as gg
+    from gempy_gb300 import learned, synthetic
+    if not os.path.exists(learned.DEFAULT_MODEL):
+        pytest.skip("no trained model in the package")
+    m = synthetic.learned(n_points=2500, n_orient=700, n_surf=5)
+    args = (m.interpolation_input, m.options, m.data_descriptor)
+    plain = gg.compute_model(*args, config=gg.EngineConfig(dtype="float64"))
+    lrn = gg.compute_model(*args, config=gg.EngineConfig(dtype="float32", learned_min_n=1000))
+    zp = np.asarray(plain.raw_arrays.scalar_field_matrix)[0]
+    zl = np.asarray(lrn.raw_arrays.scalar_field_matrix)[0]
+    assert np.abs(zl - zp).max() <= 1e-6 * np.abs(zp).max()
+    info = lrn.solver_info[0]
+    assert int(info["status"]) == 0 and int(info["iterations"]) > 0 and int(info["where"]) == 0, info
+    ids_p, ids_l = np.asarray(plain.raw_arrays.lith_block), np.asarray(lrn.raw_arrays.lith_block)
+    iso = np.asarray(plain.scalar_field_at_surface_points)
+    band = 1e-5 * np.abs(zp).max()
+    outside = (np.abs(zp[:, None] - iso[None, :]) > band).all(1)
+    assert np.array_equal(ids_p[outside], ids_l[outside])
