@@ -101,6 +101,8 @@ SIGNATURES = [
     ("gk_lu_solve", ctypes.c_int, [ctypes.c_int, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
                                    ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
                                    ctypes.c_void_p, ctypes.c_void_p]),
+    ("gk_gemv", ctypes.c_int, [ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+                               ctypes.c_void_p]),
     ("gk_solve_mixed_workspace_bytes", ctypes.c_size_t, [ctypes.c_int64]),
     ("gk_solve_mixed", ctypes.c_int, [ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                       ctypes.c_void_p, ctypes.c_double, ctypes.c_int32, ctypes.c_void_p,

@@ -1192,6 +1192,99 @@ __global__ void __launch_bounds__(256) block_solve_kernel(const T* A, int64_t ld
     cta_lu_solve(A + b0 * lda + b0, (int)lda, nb, t + b0, xs);
 }
 
+// Explicit inverses of the Schur diagonal blocks, so that the block-Jacobi
+// step of every application is a matrix-vector product instead of two
+// latency-bound in-CTA triangular sweeps.  The inverse of block b (rows and
+// columns [b0, b0 + nb)) is stored in rows [b0, b0 + nb) of an off-diagonal
+// column range of the Schur part, which the preconditioner never reads: the
+// next block's columns when that block is full, else the previous block's.
+// Used with FP64 storage when at least two blocks are full (every block then
+// has a home): the inverses cost ~40 ms of setup and save ~0.3 ms per FP64
+// application; FP32 configurations converge in too few iterations to gain.
+template <typename T>
+__host__ __device__ inline bool block_inverse_mode(int64_t n, int64_t r, int bs) {
+    return sizeof(T) == 8 && (n - r) / bs >= 2;
+}
+
+__host__ __device__ inline int64_t block_inverse_col(int64_t n, int64_t r, int bs, int64_t b) {
+    const int64_t nfull = (n - r) / bs;
+    const int64_t b0 = r + b * bs;
+    return b + 1 < nfull ? b0 + bs : b0 - bs;
+}
+
+// X = U^-1 L^-1 of the LU (unit L) held in the diagonal block; one CTA per
+// block, one thread per column of X (column-parallel substitutions; the
+// factor entry of a step is the same for the whole warp).
+template <typename T>
+__global__ void __launch_bounds__(256) block_inv_kernel(T* A, int64_t lda, int64_t r, int64_t n, int bs) {
+    const int64_t b = blockIdx.x;
+    const int64_t b0 = r + b * bs;
+    const int nb = (int)min((int64_t)bs, n - b0);
+    if (nb <= 0) return;
+    const T* F = A + b0 * lda + b0;
+    T* X = A + b0 * lda + block_inverse_col(n, r, bs, b);
+    for (int j = threadIdx.x; j < nb; j += blockDim.x) {
+        // L^-1 e_j (lower triangular: rows >= j)
+        for (int i = 0; i < j; ++i) X[(int64_t)i * lda + j] = (T)0;
+        X[(int64_t)j * lda + j] = (T)1;
+        for (int i = j + 1; i < nb; ++i) {
+            const T* Li = F + (int64_t)i * lda;
+            T s = (T)0;
+            for (int k = j; k < i; ++k) s = cta_fma(Li[k], X[(int64_t)k * lda + j], s);
+            X[(int64_t)i * lda + j] = -s;
+        }
+        // U^-1 (in place, rows descending)
+        for (int i = nb - 1; i >= 0; --i) {
+            const T* Ui = F + (int64_t)i * lda;
+            T s = X[(int64_t)i * lda + j];
+            for (int k = i + 1; k < nb; ++k) s = cta_fma(-Ui[k], X[(int64_t)k * lda + j], s);
+            X[(int64_t)i * lda + j] = s / Ui[i];
+        }
+    }
+}
+
+// t_b <- inv(S_b) t_b for every block: t_b is staged in shared memory, then
+// each warp computes kInvRows rows at once (one accumulator per row, so
+// kInvRows independent loads are in flight per lane).
+constexpr int kInvRows = 8;
+
+template <typename T>
+__global__ void __launch_bounds__(512) block_inv_apply_kernel(const T* __restrict__ A, int64_t lda, int64_t r,
+                                                              int64_t n, int bs, T* t) {
+    extern __shared__ unsigned char smem_raw[];
+    T* ts = reinterpret_cast<T*>(smem_raw);
+    const int64_t b = blockIdx.x;
+    const int64_t b0 = r + b * bs;
+    const int nb = (int)min((int64_t)bs, n - b0);
+    if (nb <= 0) return;
+    for (int j = threadIdx.x; j < nb; j += blockDim.x) ts[j] = t[b0 + j];
+    __syncthreads();
+    const T* X = A + b0 * lda + block_inverse_col(n, r, bs, b);
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int i0 = (threadIdx.x >> 5) * kInvRows; i0 < nb; i0 += nw * kInvRows) {
+        T acc[kInvRows];
+#pragma unroll
+        for (int q = 0; q < kInvRows; ++q) acc[q] = (T)0;
+        for (int j = lane; j < nb; j += 32) {
+            const T tj = ts[j];
+#pragma unroll
+            for (int q = 0; q < kInvRows; ++q)
+                if (i0 + q < nb) acc[q] = cta_fma(X[(int64_t)(i0 + q) * lda + j], tj, acc[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < kInvRows; ++q) {
+            T v = acc[q];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            acc[q] = v;
+        }
+        if (lane == 0) {
+#pragma unroll
+            for (int q = 0; q < kInvRows; ++q)
+                if (i0 + q < nb) t[b0 + i0 + q] = acc[q];
+        }
+    }
+}
+
 // y[i] -= sum_j A[i][j] x[j], i in [r_lo, r_hi), j in [c_lo, c_hi).  One warp
 // per kRectRows consecutive rows, so each x element is loaded once for all of
 // them; 16-byte loads of A when the row segments are 16-byte aligned.
@@ -1394,6 +1487,10 @@ static gk_status twolevel_setup(int64_t n, const double* K, int64_t ldk, const i
     }
     block_lu_kernel<T><<<(unsigned)nblk, block_lu_threads<T>(), 0, st>>>(A, lda, r, n, bs, info);
     GK_LAUNCH_CHECK();
+    if (block_inverse_mode<T>(n, r, bs)) {
+        block_inv_kernel<T><<<(unsigned)nblk, 256, 0, st>>>(A, lda, r, n, bs);
+        GK_LAUNCH_CHECK();
+    }
     const size_t ysmem = (size_t)kTB * kTB * sizeof(T);
     GK_CUDA_TRY(cudaFuncSetAttribute(tri_inv_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ysmem));
     tri_inv_kernel<T><<<(unsigned)((r + kTB - 1) / kTB), kTB, ysmem, st>>>(A, lda, r, lu_ws_dinv<T>(work, r, 0),
@@ -1425,7 +1522,11 @@ static gk_status twolevel_apply(int64_t n, const T* A, int64_t lda, const int32_
     GK_LAUNCH_CHECK();
     // block-Jacobi on the Schur complement
     const int64_t nblk = (n - r + bs - 1) / bs;
-    block_solve_kernel<T><<<(unsigned)nblk, 256, 0, st>>>(A, lda, r, n, bs, t);
+    if (block_inverse_mode<T>(n, r, bs)) {
+        block_inv_apply_kernel<T><<<(unsigned)nblk, 512, (size_t)bs * sizeof(T), st>>>(A, lda, r, n, bs, t);
+    } else {
+        block_solve_kernel<T><<<(unsigned)nblk, 256, 0, st>>>(A, lda, r, n, bs, t);
+    }
     GK_LAUNCH_CHECK();
     // backward: t_L -= U_LR x_R, then U_LL x_L = t_L
     rect_gemv_kernel<T><<<rect_blocks(r), 256, 0, st>>>(A, lda, 0, r, r, n, t, t);

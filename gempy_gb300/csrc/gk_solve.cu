@@ -395,6 +395,14 @@ static gk_status fgmres(Solver& S, const double* b, double* x, double tol, int m
     return GK_OK;
 }
 
+extern "C" gk_status gk_gemv(int64_t n, const double* K, int64_t ldk, const double* x, double* y,
+                             gk_stream stream) {
+    if (n <= 0 || K == nullptr || x == nullptr || y == nullptr || ldk < n || x == y) return GK_ERR_ARG;
+    gemv_kernel<<<gemv_blocks(n), 256, 0, (cudaStream_t)stream>>>(K, ldk, n, nullptr, x, y);
+    GK_LAUNCH_CHECK();
+    return GK_OK;
+}
+
 extern "C" gk_status gk_solve_mixed(int64_t n, const double* K, int64_t ldk, const double* b, double* x, double tol,
                                     int32_t max_iter, void* work, size_t work_bytes, gk_info* info,
                                     gk_stream stream) {
@@ -464,7 +472,7 @@ extern "C" gk_status gk_solve_twolevel(int64_t n, const double* K, int64_t ldk, 
     cudaStream_t st = (cudaStream_t)stream;
     if (n <= 0 || K == nullptr || b == nullptr || x == nullptr || perm == nullptr || ldk < n || max_iter < 1)
         return GK_ERR_ARG;
-    if (r <= 0 || r >= n || (r % 64) != 0 || bs <= 0 || (bs % 64) != 0) return GK_ERR_ARG;
+    if (r <= 0 || r >= n || (r % 64) != 0 || bs <= 0 || (bs % 64) != 0 || bs > 4096) return GK_ERR_ARG;
     if (prec != GK_F32 && prec != GK_F64) return GK_ERR_ARG;
     const int es = prec == GK_F64 ? 8 : 4;
     if (work == nullptr || work_bytes < mixed_bytes(n, es, kRestartTwoLevel)) return GK_ERR_SIZE;

@@ -190,7 +190,12 @@ def compute_model(interpolation_input, options, data_descriptor, geophysics_inpu
     uv = np.asarray(interpolation_input.unit_values, dtype=np.float64)
     series = []
     cost_model = None
+    conds = []
     for dev_s, s_off, n_s, rel in _split(interpolation_input, options, data_descriptor, device):
+        if getattr(ko, "compute_condition_number", False):
+            Kc, _ = K.build(dev_s, GK_F64)
+            conds.append(K.condition_number(Kc))
+            del Kc
         if mixed and cfg.learned_min_n > 0 and dev_s.N >= cfg.learned_min_n:
             if cost_model is None:
                 cost_model = _load_cost_model(cfg.learned_model, device)
@@ -213,6 +218,9 @@ def compute_model(interpolation_input, options, data_descriptor, geophysics_inpu
         s = _Series(dev_s, iso, order, uv[s_off:s_off + n_s + 1], rel, w, info)
         s.model = model
         series.append(s)
+    if conds:
+        # the engine reports one number on the options; with several series, the largest
+        ko.condition_number = float(max(conds))
     if cfg.timings:
         torch.cuda.synchronize()
         timings["solve_s"] = time.perf_counter() - t0

@@ -176,6 +176,40 @@ def solve_mixed(series: DeviceSeries, tol=1e-12, max_iter=30, K=None, b=None):
     return x, info
 
 
+def gemv(K, x):
+    """y = K x (FP64, on the GPU)."""
+    lib = _lib.load()
+    n = K.shape[0]
+    x = x.contiguous()
+    y = torch.empty(n, dtype=torch.float64, device=K.device)
+    check("gk_gemv", lib.gk_gemv(n, _ptr(K), K.stride(0), _ptr(x), _ptr(y), _stream()))
+    return y
+
+
+def condition_number(K, factors=None, iters=60, seed=0):
+    """2-norm condition number of the symmetric FP64 matrix K: the largest
+    |eigenvalue| by power iteration on K, the smallest by inverse iteration
+    with the FP64 LU (``factors``, computed from a copy when not given)."""
+    n = K.shape[0]
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    v = torch.randn(n, generator=g, dtype=torch.float64).to(K.device)
+    v /= torch.linalg.vector_norm(v)
+    big = 0.0
+    for _ in range(iters):
+        w = gemv(K, v)
+        big = float(torch.linalg.vector_norm(w))
+        v = w / big
+    f = factors if factors is not None else lu_factor(K, GK_F64, overwrite=False)
+    v = torch.randn(n, generator=g, dtype=torch.float64).to(K.device)
+    v /= torch.linalg.vector_norm(v)
+    inv_small = 0.0
+    for _ in range(iters):
+        w = lu_solve(f, v)
+        inv_small = float(torch.linalg.vector_norm(w))
+        v = w / inv_small
+    return big * inv_small
+
+
 def unknown_positions(series: DeviceSeries):
     """Position of every unknown: orientation position for gradient rows, rest
     point for interface rows (drift rows: the centroid)."""

@@ -149,6 +149,12 @@ gk_status gk_lu_solve(gk_prec prec, int64_t n, const void* LU, int64_t lda,
                       const int32_t* ipiv, void* b, void* work,
                       size_t work_bytes, gk_info* info, gk_stream stream);
 
+/* y = K x for the FP64 matrix (row-major, ld ``ldk``); x and y must not
+ * overlap.  Used with gk_lu_solve for the condition-number estimate the
+ * engine reports when ``KernelOptions.compute_condition_number`` is set. */
+gk_status gk_gemv(int64_t n, const double* K, int64_t ldk, const double* x,
+                  double* y, gk_stream stream);
+
 /* Mixed-precision solve of the FP64 system K x = b (no reference
  * counterpart beyond the FP64 solve it replaces): an FP32 copy of the
  * symmetrically equilibrated K is LU-factored on the GPU -- without pivoting
@@ -172,10 +178,12 @@ gk_status gk_solve_mixed(int64_t n, const double* K, int64_t ldk,
  * replaces).  ``perm`` (device, n entries) lists the unknowns in the new order:
  * first ``r`` landmark unknowns (r a multiple of 64; the drift unknowns must be
  * among them), then the others in spatially contiguous blocks of ``bs`` (a
- * multiple of 64).  Setup, in ``prec`` (GK_F32 or GK_F64) on the
+ * multiple of 64, at most 4096).  Setup, in ``prec`` (GK_F32 or GK_F64) on the
  * equilibrated, permuted matrix: LU without pivoting of the landmark block,
  * the landmark rows/columns (the rank-r coupling), and LU of the bs x bs
- * diagonal blocks of the Schur complement.  GK_F32 halves the setup's memory
+ * diagonal blocks of the Schur complement (with GK_F64, then their explicit
+ * inverses, kept in unused off-diagonal space, when at least two blocks are
+ * full).  GK_F32 halves the setup's memory
  * traffic but only preconditions systems with kappa(K) eps32 well below 1;
  * GK_F64 covers the densely sampled, nugget-dominated systems beyond that.
  * The Krylov iteration is FP64 on the FP64 K, to ||b - K x||_2 <= tol ||b||_2

@@ -412,3 +412,22 @@ def test_twolevel_fgmres_judged_by_fp64_lu(n_land, block, prec, policy):
     pts = np.random.default_rng(0).uniform(-0.45, 0.45, (2000, 3))
     z_tl, z_lu = kriging.evaluate(s, x, pts), kriging.evaluate(s, w_lu, pts)
     assert np.abs(z_tl - z_lu).max() <= 1e-4 * np.abs(z_lu).max()
+
+
+def test_condition_number_matches_oracle():
+    """compute_condition_number: kappa_2(K) estimated on the GPU (power and
+    inverse iteration with the FP64 LU) against numpy's SVD-based cond."""
+    import gempy_gb300 as gg
+    from gempy_gb300 import kernels as K
+    s = _anticline()
+    Kr, _ = kriging.build_system(s)
+    ref = np.linalg.cond(Kr)
+    Kt, _ = K.build(_dev_series(s), K.GK_F64)
+    est = K.condition_number(Kt, iters=300)
+    assert abs(est - ref) <= 0.02 * ref, (est, ref)
+    # through compute_model: the options carry the number afterwards
+    from __graft_entry__ import _anticline_model
+    g, ii, opts, dd, ext = _anticline_model(levels=2, custom=False)
+    opts.kernel_options.compute_condition_number = True
+    gg.compute_model(ii, opts, dd)
+    assert abs(opts.kernel_options.condition_number - ref) <= 0.02 * ref
