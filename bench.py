@@ -414,7 +414,12 @@ def main():
                      "peak_source": f"nominal FP32 SIMT: 152 SMs x 128 lanes x 2 x {sm_mhz:.0f} MHz "
                                     f"(max SM clock from MEASURED_PEAKS.json, {pk['_source']})",
                      "work": f"{fl_pt} algorithmic flops/point x {n_pts} points per launch",
-                     "eval_ms": ev_mixed},
+                     "eval_ms": ev_mixed,
+                     # float-float executes ~168 FP32-pipe instructions per point-record pair (ncu count)
+                     # where the algorithmic count has 20: the pipe view
+                     "fp32_pipe_ops_per_pair": 168, "algorithmic_flops_per_pair": 20,
+                     "fp32_pipe_achieved": achieved_tf * 168 / 20,
+                     "fp32_pipe_frac": achieved_tf * 168 / 20 / fp32_peak},
     }
     if not args.no_extra:
         line["batch"] = batch_section(n_real=args.batch_realisations)
@@ -571,6 +576,25 @@ def learned_section(n_points=20000, force_config=None):
     def_ok = int(infd["status"]) == 0
     t_def_total = t_def if def_ok else t_def + t_lu
     # network kernels: inference over a large batch and one training step
+    # the dominant per-iteration kernel: the FP64 product K v of FGMRES (gk_gemv), CUDA events
+    xv = torch.randn(N, dtype=torch.float64, device="cuda")
+    for _ in range(3):
+        K.gemv(Kt, xv)
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g0.record()
+    for _ in range(10):
+        K.gemv(Kt, xv)
+    g1.record()
+    torch.cuda.synchronize()
+    gemv_ms = g0.elapsed_time(g1) / 10
+    pk = peaks()
+    gemv_gbs = N * N * 8 / (gemv_ms * 1e-3) / 1e9
+    gemv_tf = 2.0 * N * N / (gemv_ms * 1e-3) / 1e12
+    roof = {"kernel": "gk::gemv_kernel (FP64 K v of FGMRES, 4 rows per warp)", "bound": "fp64",
+            "achieved": gemv_tf, "peak": 1.25, "unit": "TFLOP/s", "frac": gemv_tf / 1.25,
+            "peak_source": "nominal GB300 FP64 rate (no measured FP64 peak is available)",
+            "hbm_gbs": gemv_gbs, "hbm_frac_of_measured": gemv_gbs / pk["hbm_gbs"],
+            "work": f"{N}^2 x 8 bytes and 2 x {N}^2 flops per launch", "ms": gemv_ms}
     if model is None:
         model = learned.CostModel(learned.Mlp(), np.zeros(learned.IN_DIM), np.ones(learned.IN_DIM),
                                   np.zeros(learned.OUT_DIM), np.ones(learned.OUT_DIM), {"untrained": True})
@@ -601,6 +625,7 @@ def learned_section(n_points=20000, force_config=None):
         "solves_per_s": {"plain_fp64": 1.0 / t_lu, "learned": 1.0 / t_learned,
                          "default_config": 1.0 / t_def_total},
         "speedup_vs_plain_fp64": t_lu / t_learned,
+        "roofline": roof,
         "gain_vs_default_config": t_def_total / t_learned,
         "network": {"samples_per_forward": B, "forward_ms": fwd_ms, "forward_tflops": flops / (fwd_ms * 1e-3) / 1e12,
                     "training": model.meta},

@@ -571,6 +571,120 @@ __global__ void __launch_bounds__(256) gemm_range_kernel(T* __restrict__ A, int6
     }
 }
 
+// ----------------------------------------------------------------------------
+// Float-float restricted update for the two-level setup (GK_FF): the same
+// C -= L_panel U_panel as gemm_range_kernel<double> on FP64 storage, with the
+// products on the FP32 pipe.  GB300 issues ~2 FP64 FMAs per clock per SM, so
+// FP64 updates run at ~1.2 TFLOP/s; here each panel entry is split once into
+// a float pair (hi + lo, ~48 bits) by split_panel_kernel and every
+// multiply-add is ~12 FP32 operations: the exact product error from an FMA,
+// the cross terms, and a TwoSum into a (hi, lo) accumulator whose low word
+// collects the errors (accuracy ~1e-12 of sum |a b| per update; the FP32 form
+// gives ~1e-6).  Only the epilogue (C -= hi + lo) touches the FP64 pipe.
+// Panels: L rows [o, n) x columns [k, k + kb) as Lh/Ll[i * kFfPanel + p];
+// U rows [k, k + kb) x columns [o, n) as Uh/Ul[p * n + j].
+// ----------------------------------------------------------------------------
+constexpr int kFfPanel = 32;  // == LuCfg<double>::NB
+
+__global__ void split_panel_kernel(const double* __restrict__ A, int64_t lda, int64_t n, int64_t k, int kb,
+                                   int64_t o, float* __restrict__ Lh, float* __restrict__ Ll,
+                                   float* __restrict__ Uh, float* __restrict__ Ul) {
+    const int64_t m = (n - o) * kFfPanel;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < 2 * m; e += (int64_t)gridDim.x * blockDim.x) {
+        const bool upper = e >= m;
+        const int64_t f = upper ? e - m : e;
+        double v = 0.0;
+        int64_t dst;
+        if (!upper) {
+            const int64_t i = o + f / kFfPanel;
+            const int p = (int)(f % kFfPanel);
+            if (p < kb) v = A[i * lda + k + p];
+            dst = i * kFfPanel + p;
+        } else {
+            const int p = (int)(f / (n - o));
+            const int64_t j = o + f % (n - o);
+            if (p < kb) v = A[(k + p) * lda + j];
+            dst = (int64_t)p * n + j;
+        }
+        const float h = (float)v;
+        const float l = (float)(v - (double)h);
+        if (!upper) { Lh[dst] = h; Ll[dst] = l; } else { Uh[dst] = h; Ul[dst] = l; }
+    }
+}
+
+__global__ void __launch_bounds__(256) ffgemm_range_kernel(double* __restrict__ A, int64_t lda, int64_t n, int kb,
+                                                           const float* __restrict__ Lh, const float* __restrict__ Ll,
+                                                           const float* __restrict__ Uh, const float* __restrict__ Ul,
+                                                           int64_t r_lo, int64_t r_hi, int64_t c_lo, int64_t c_hi,
+                                                           int diag_bs) {
+    constexpr int BM = 64, BN = 64, BK = 16, TM = 4, TN = 4;
+    __shared__ float Ash[BK][BM + 1], Asl[BK][BM + 1];
+    __shared__ float Bsh[BK][BN], Bsl[BK][BN];
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    if (diag_bs > 0) {
+        const int64_t b0 = r_lo + (int64_t)blockIdx.z * diag_bs;
+        r_lo = c_lo = b0;
+        r_hi = c_hi = min(r_hi, b0 + diag_bs);
+    }
+    const int64_t i0 = r_lo + (int64_t)blockIdx.y * BM, j0 = c_lo + (int64_t)blockIdx.x * BN;
+    if (i0 >= r_hi || j0 >= c_hi) return;
+    float ah[TM][TN], al[TM][TN];
+#pragma unroll
+    for (int a = 0; a < TM; ++a)
+#pragma unroll
+        for (int b = 0; b < TN; ++b) { ah[a][b] = 0.f; al[a][b] = 0.f; }
+    for (int p0 = 0; p0 < kb; p0 += BK) {
+        for (int idx = threadIdx.x; idx < BM * BK; idx += 256) {
+            const int m = idx / BK, p = idx % BK;
+            const int64_t gi = i0 + m;
+            const bool ok = gi < r_hi && p0 + p < kb;
+            Ash[p][m] = ok ? Lh[gi * kFfPanel + p0 + p] : 0.f;
+            Asl[p][m] = ok ? Ll[gi * kFfPanel + p0 + p] : 0.f;
+        }
+        for (int idx = threadIdx.x; idx < BK * BN; idx += 256) {
+            const int p = idx / BN, c = idx % BN;
+            const int64_t gj = j0 + c;
+            const bool ok = gj < c_hi && p0 + p < kb;
+            Bsh[p][c] = ok ? Uh[(int64_t)(p0 + p) * n + gj] : 0.f;
+            Bsl[p][c] = ok ? Ul[(int64_t)(p0 + p) * n + gj] : 0.f;
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int p = 0; p < BK; ++p) {
+            float xh[TM], xl[TM], yh[TN], yl[TN];
+#pragma unroll
+            for (int a = 0; a < TM; ++a) { xh[a] = Ash[p][ty + 16 * a]; xl[a] = Asl[p][ty + 16 * a]; }
+#pragma unroll
+            for (int b = 0; b < TN; ++b) { yh[b] = Bsh[p][tx + 16 * b]; yl[b] = Bsl[p][tx + 16 * b]; }
+#pragma unroll
+            for (int a = 0; a < TM; ++a)
+#pragma unroll
+                for (int b = 0; b < TN; ++b) {
+                    const float ph = __fmul_rn(xh[a], yh[b]);
+                    float pl = __fmaf_rn(xh[a], yh[b], -ph);
+                    pl = __fmaf_rn(xh[a], yl[b], pl);
+                    pl = __fmaf_rn(xl[a], yh[b], pl);
+                    const float s = __fadd_rn(ah[a][b], ph);
+                    const float v = __fsub_rn(s, ah[a][b]);
+                    const float e = __fadd_rn(__fsub_rn(ah[a][b], __fsub_rn(s, v)), __fsub_rn(ph, v));
+                    ah[a][b] = s;
+                    al[a][b] = __fadd_rn(al[a][b], __fadd_rn(e, pl));
+                }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int a = 0; a < TM; ++a) {
+        const int64_t gi = i0 + ty + 16 * a;
+        if (gi >= r_hi) continue;
+#pragma unroll
+        for (int b = 0; b < TN; ++b) {
+            const int64_t gj = j0 + tx + 16 * b;
+            if (gj < c_hi) A[gi * lda + gj] -= (double)ah[a][b] + (double)al[a][b];
+        }
+    }
+}
+
 // FP32 trailing update for aligned panels (offsets and lda multiples of 4):
 // 128 x 128 tile per CTA, 16 x 16 threads each owning an 8 x 8 block split in
 // four 4 x 4 quadrants, float4 shared-memory reads (A stored k-major), the
@@ -1434,7 +1548,7 @@ size_t gk_internal_lu_ws_f32(int64_t n) { return lu_ws_bytes<float>(n); }
 template <typename T>
 static gk_status twolevel_setup(int64_t n, const double* K, int64_t ldk, const int32_t* perm, const double* d,
                                      int64_t r, int bs, T* A, int64_t lda, int32_t* ipiv, void* work,
-                                     size_t wbytes, gk_info* info, cudaStream_t st) {
+                                     size_t wbytes, gk_info* info, cudaStream_t st, float* ffpanel = nullptr) {
     constexpr int NB = LuCfg<T>::NB;
     if (n <= 0 || r <= 0 || r >= n || bs <= 0 || (r % 64) != 0 || (bs % 64) != 0 || (lda % 4) != 0 ||
         ((uintptr_t)A % 16) != 0)
@@ -1453,6 +1567,28 @@ static gk_status twolevel_setup(int64_t n, const double* K, int64_t ldk, const i
         trsm_kernel<T, NB><<<(unsigned)((rest + 127) / 128), 128, 0, st>>>(A, lda, n, k, kb);
         GK_LAUNCH_CHECK();
         const int64_t o = k + kb;
+        if (sizeof(T) == 8 && ffpanel != nullptr) {
+            double* Ad = (double*)A;
+            constexpr int BT = 64;
+            float* Lh = ffpanel;
+            float* Ll = Lh + n * kFfPanel;
+            float* Uh = Ll + n * kFfPanel;
+            float* Ul = Uh + n * kFfPanel;
+            split_panel_kernel<<<4 * kSMs, 256, 0, st>>>(Ad, lda, n, k, kb, o, Lh, Ll, Uh, Ul);
+            GK_LAUNCH_CHECK();
+            if (o < r) {
+                dim3 ga((unsigned)((n - o + BT - 1) / BT), (unsigned)((r - o + BT - 1) / BT));
+                ffgemm_range_kernel<<<ga, 256, 0, st>>>(Ad, lda, n, kb, Lh, Ll, Uh, Ul, o, r, o, n, 0);
+                GK_LAUNCH_CHECK();
+                dim3 gb((unsigned)((r - o + BT - 1) / BT), (unsigned)((n - r + BT - 1) / BT));
+                ffgemm_range_kernel<<<gb, 256, 0, st>>>(Ad, lda, n, kb, Lh, Ll, Uh, Ul, r, n, o, r, 0);
+                GK_LAUNCH_CHECK();
+            }
+            dim3 gc((unsigned)((bs + BT - 1) / BT), (unsigned)((bs + BT - 1) / BT), (unsigned)nblk);
+            ffgemm_range_kernel<<<gc, 256, 0, st>>>(Ad, lda, n, kb, Lh, Ll, Uh, Ul, r, n, r, n, bs);
+            GK_LAUNCH_CHECK();
+            continue;
+        }
         if (sizeof(T) == 8) {
             double* Ad = (double*)A;
             constexpr int BT = 64;
@@ -1551,9 +1687,11 @@ gk_status gk_internal_twolevel_setup(int64_t n, const double* K, int64_t ldk, co
 }
 gk_status gk_internal_twolevel_setup_f64(int64_t n, const double* K, int64_t ldk, const int32_t* perm,
                                          const double* d, int64_t r, int bs, double* A, int64_t lda, int32_t* ipiv,
-                                         void* work, size_t wbytes, gk_info* info, cudaStream_t st) {
-    return twolevel_setup<double>(n, K, ldk, perm, d, r, bs, A, lda, ipiv, work, wbytes, info, st);
+                                         void* work, size_t wbytes, gk_info* info, cudaStream_t st,
+                                         float* ffpanel) {
+    return twolevel_setup<double>(n, K, ldk, perm, d, r, bs, A, lda, ipiv, work, wbytes, info, st, ffpanel);
 }
+size_t gk_internal_ff_panel_floats(int64_t n) { return (size_t)4 * kFfPanel * (size_t)n; }
 gk_status gk_internal_twolevel_apply(int64_t n, const float* A, int64_t lda, const int32_t* perm, const double* d,
                                      int64_t r, int bs, const double* v, double* z, float* t, void* work,
                                      size_t wbytes, gk_info* info, cudaStream_t st) {

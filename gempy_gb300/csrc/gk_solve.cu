@@ -26,7 +26,9 @@ size_t gk_internal_lu_ws_f32(int64_t n);
 size_t gk_internal_lu_ws_f64(int64_t n);
 gk_status gk_internal_twolevel_setup_f64(int64_t n, const double* K, int64_t ldk, const int32_t* perm,
                                          const double* d, int64_t r, int bs, double* A, int64_t lda, int32_t* ipiv,
-                                         void* work, size_t wbytes, gk_info* info, cudaStream_t st);
+                                         void* work, size_t wbytes, gk_info* info, cudaStream_t st,
+                                         float* ffpanel);
+size_t gk_internal_ff_panel_floats(int64_t n);
 gk_status gk_internal_twolevel_apply_f64(int64_t n, const double* A, int64_t lda, const int32_t* perm,
                                          const double* d, int64_t r, int bs, const double* v, double* z, double* t,
                                          void* work, size_t wbytes, gk_info* info, cudaStream_t st);
@@ -460,9 +462,17 @@ extern "C" gk_status gk_solve_mixed(int64_t n, const double* K, int64_t ldk, con
 // ---------------------------------------------------------------------------
 // FGMRES with the two-level (block-Jacobi + low-rank) preconditioner
 // ---------------------------------------------------------------------------
+// GK_FF: FP64 storage, restricted updates in float-float on the FP32 pipe
+// (panel split buffers appended to the workspace).
+static size_t twolevel_bytes(int64_t n, gk_prec prec) {
+    size_t b = mixed_bytes(n, prec == GK_F32 ? 4 : 8, kRestartTwoLevel);
+    if (prec == GK_FF) b += al(gk_internal_ff_panel_floats(n) * sizeof(float));
+    return b;
+}
+
 extern "C" size_t gk_solve_twolevel_workspace_bytes(int64_t n, gk_prec prec) {
-    if (n <= 0 || (prec != GK_F32 && prec != GK_F64)) return 0;
-    return mixed_bytes(n, prec == GK_F64 ? 8 : 4, kRestartTwoLevel);
+    if (n <= 0 || (prec != GK_F32 && prec != GK_F64 && prec != GK_FF)) return 0;
+    return twolevel_bytes(n, prec);
 }
 
 extern "C" gk_status gk_solve_twolevel(int64_t n, const double* K, int64_t ldk, const double* b, double* x,
@@ -473,9 +483,10 @@ extern "C" gk_status gk_solve_twolevel(int64_t n, const double* K, int64_t ldk, 
     if (n <= 0 || K == nullptr || b == nullptr || x == nullptr || perm == nullptr || ldk < n || max_iter < 1)
         return GK_ERR_ARG;
     if (r <= 0 || r >= n || (r % 64) != 0 || bs <= 0 || (bs % 64) != 0 || bs > 4096) return GK_ERR_ARG;
-    if (prec != GK_F32 && prec != GK_F64) return GK_ERR_ARG;
-    const int es = prec == GK_F64 ? 8 : 4;
-    if (work == nullptr || work_bytes < mixed_bytes(n, es, kRestartTwoLevel)) return GK_ERR_SIZE;
+    if (prec != GK_F32 && prec != GK_F64 && prec != GK_FF) return GK_ERR_ARG;
+    const int es = prec == GK_F32 ? 4 : 8;
+    if (work == nullptr || work_bytes < twolevel_bytes(n, prec)) return GK_ERR_SIZE;
+    float* ffpanel = prec == GK_FF ? (float*)((char*)work + mixed_bytes(n, es, kRestartTwoLevel)) : nullptr;
     Solver S;
     S.n = n; S.K = K; S.ldk = ldk; S.w = carve(work, n, es, kRestartTwoLevel); S.ld32 = ld32_of(n); S.st = st;
     S.m = kRestartTwoLevel;
@@ -483,7 +494,7 @@ extern "C" gk_status gk_solve_twolevel(int64_t n, const double* K, int64_t ldk, 
     S.info = info;
     S.vb = (unsigned)((n + 255) / 256);
     S.rb = (unsigned)((n * 32 + 255) / 256);
-    S.mode = prec == GK_F64 ? 2 : 1;
+    S.mode = prec == GK_F32 ? 1 : 2;
     S.perm = perm;
     S.r = r;
     S.bs = bs;
@@ -491,9 +502,9 @@ extern "C" gk_status gk_solve_twolevel(int64_t n, const double* K, int64_t ldk, 
     GK_CUDA_TRY(cudaMemsetAsync(info, 0, sizeof(gk_info), st));
     equil_kernel<<<S.rb, 256, 0, st>>>(K, ldk, n, w.d);
     GK_LAUNCH_CHECK();
-    gk_status s = prec == GK_F64
+    gk_status s = prec != GK_F32
                       ? gk_internal_twolevel_setup_f64(n, K, ldk, perm, w.d, r, bs, w.K64, S.ld32, w.ipiv, w.luw,
-                                                       w.luw_bytes, info, st)
+                                                       w.luw_bytes, info, st, ffpanel)
                       : gk_internal_twolevel_setup(n, K, ldk, perm, w.d, r, bs, w.K32, S.ld32, w.ipiv, w.luw,
                                                    w.luw_bytes, info, st);
     if (s != GK_OK) return s;

@@ -268,7 +268,8 @@ def twolevel_permutation(series: DeviceSeries, n_landmarks, seed=0, policy="rand
 def solve_twolevel(series: DeviceSeries, n_landmarks=1024, block=512, tol=1e-8, max_iter=2000, K=None, b=None,
                    seed=0, policy="random", prec=None):
     """FGMRES with the two-level (block-Jacobi + low-rank) preconditioner;
-    ``prec`` (GK_F32 / GK_F64, default GK_F64) is the preconditioner's storage."""
+    ``prec`` is the preconditioner's arithmetic: GK_F32, GK_FF (FP64 storage,
+    float-float updates) or GK_F64 (the default)."""
     lib = _lib.load()
     prec = GK_F64 if prec is None else int(prec)
     if K is None:

@@ -29,9 +29,9 @@ import numpy as np
 import torch
 
 from . import _lib, kernels
-from ._lib import GK_F32, GK_F64, GK_SYSTEM_FEATURES, GkAdam, GkMlp, check
+from ._lib import GK_F32, GK_F64, GK_FF, GK_SYSTEM_FEATURES, GkAdam, GkMlp, check
 
-CONFIG_FEATURES = 4
+CONFIG_FEATURES = 5
 IN_DIM = GK_SYSTEM_FEATURES + CONFIG_FEATURES
 # outputs: log(seconds of the FGMRES run), failure indicator, log(seconds of the FP64 LU fallback)
 OUT_DIM = 3
@@ -45,19 +45,19 @@ class PrecondConfig:
     landmarks: int        # requested landmark count (rounded up to a multiple of 64 with the drift)
     block: int            # block-Jacobi block size
     policy: str           # kernels.LANDMARK_POLICIES
-    prec: int             # GK_F32 / GK_F64 storage of the preconditioner
+    prec: int             # GK_F32, GK_FF (FP64 storage, float-float updates) or GK_F64
 
     def features(self):
         return np.array([np.log2(self.landmarks) / 13.0, np.log2(self.block) / 10.0,
-                         float(kernels.LANDMARK_POLICIES.index(self.policy)), float(self.prec == GK_F64)],
-                        dtype=np.float32)
+                         float(kernels.LANDMARK_POLICIES.index(self.policy)), float(self.prec != GK_F32),
+                         float(self.prec == GK_FF)], dtype=np.float32)
 
 
 CANDIDATES = tuple(PrecondConfig(r, bs, pol, pr)
                    for r in (512, 1024, 2048, 4096, 8192, 16384)
                    for bs in (256, 512)
                    for pol in kernels.LANDMARK_POLICIES
-                   for pr in (GK_F32, GK_F64))
+                   for pr in (GK_F32, GK_FF, GK_F64))
 
 # The method without the network: one fixed configuration for every system.
 DEFAULT_CONFIG = PrecondConfig(1024, 512, "random", GK_F64)

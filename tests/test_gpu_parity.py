@@ -389,7 +389,8 @@ def test_mixed_solve_without_pivoting_on_kriging_matrix():
 
 @pytest.mark.parametrize("n_land,block,prec,policy", [(256, 64, 1, "random"), (512, 128, 1, "stratified"),
                                                       (1024, 256, 1, "random"), (256, 64, 0, "stratified"),
-                                                      (1024, 256, 0, "random")])
+                                                      (1024, 256, 0, "random"), (256, 64, 2, "stratified"),
+                                                      (512, 128, 2, "random")])
 def test_twolevel_fgmres_judged_by_fp64_lu(n_land, block, prec, policy):
     """Block-Jacobi + low-rank preconditioned FGMRES reaches 1e-8; the FP64 LU
     (plain form) judges the solution."""

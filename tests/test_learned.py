@@ -61,9 +61,9 @@ def test_param_count_matches_library():
 
 def test_config_features_and_candidates():
     from gempy_gb300 import learned
-    assert learned.IN_DIM == 20
+    assert learned.IN_DIM == 21
     c = learned.CANDIDATES
-    assert len(c) == len(set(c)) == 48
+    assert len(c) == len(set(c)) == 72
     f = np.stack([x.features() for x in c])
     assert np.unique(f, axis=0).shape[0] == len(c)
     assert all(x.landmarks <= 3000 for x in learned.candidates_for(6000))
@@ -229,7 +229,7 @@ def test_training_reduces_loss():
 
 
 @pytest.mark.gpu
-def test_twolevel_fp64_storage_matches_lu():
+def test_twolevel_fp64_and_ff_storage_match_lu():
     from gempy_gb300 import kernels, learned, synthetic
     m = synthetic.training_system(1, base_seed=3, n_min=3000, n_max=3500)
     s = learned.series_of(m)
@@ -237,8 +237,8 @@ def test_twolevel_fp64_storage_matches_lu():
     x_lu, _ = learned.solve_plain_K(K, b)
     pts = learned.judge_points(s)
     f_lu = learned.field_at(s, x_lu, pts)
-    for policy in ("random", "stratified"):
-        x, inf = learned.solve_with(s, learned.PrecondConfig(512, 256, policy, kernels.GK_F64), K, b, tol=1e-10,
+    for policy, prec in (("random", kernels.GK_F64), ("stratified", kernels.GK_F64), ("stratified", kernels.GK_FF)):
+        x, inf = learned.solve_with(s, learned.PrecondConfig(512, 256, policy, prec), K, b, tol=1e-10,
                                     max_iter=1500)
         assert int(inf["status"]) == 0, inf
         assert learned.field_error(s, x, f_lu, pts) < 1e-6
