@@ -186,7 +186,7 @@ def main():
     ap.add_argument("--learned-points", type=int, default=20000,
                     help="surface points of the config-5 system (orientations: 30 %%)")
     ap.add_argument("--learned-config", default=None,
-                    help="landmarks,block,policy,f32|f64: use this two-level configuration instead of the network's")
+                    help="landmarks,block,policy,f32|ff|f64: use this two-level configuration instead of the network's")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -551,7 +551,7 @@ def learned_section(n_points=20000, force_config=None):
     forced = None
     if force_config:
         r_, bs_, pol_, pr_ = force_config.split(",")
-        forced = learned.PrecondConfig(int(r_), int(bs_), pol_, K.GK_F64 if pr_ == "f64" else K.GK_F32)
+        forced = learned.PrecondConfig(int(r_), int(bs_), pol_, {"f32": K.GK_F32, "ff": K.GK_FF, "f64": K.GK_F64}[pr_])
     elif not os.path.exists(learned.DEFAULT_MODEL):
         return {"unavailable": "no trained model in the package"}
     model = None if forced else learned.CostModel.load()

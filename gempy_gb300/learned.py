@@ -304,23 +304,42 @@ def solve_plain_K(K, b):
     return kernels.lu_solve(f, b), kernels.read_info(f.info)
 
 
+# FP32 configurations either converge quickly or stall at a large residual;
+# at inference they get this iteration cap so a wrong pick costs little.
+MAX_ITER_F32 = 400
+
+
 def solve_learned(series, model, K=None, b=None, tol=1e-8, max_iter=MAX_ITER, config=None):
-    """Solve with the configuration the network picks (or ``config``); FP64
-    LU if FGMRES misses the tolerance."""
+    """Solve with the configuration the network ranks first (or ``config``).
+    If FGMRES misses the tolerance with an FP32 configuration, the best-ranked
+    FP64-storage configuration is tried next; the FP64 LU is the last resort."""
     if K is None:
         K, b = kernels.build(series, GK_F64)
+    N = K.shape[0]
     t0 = time.perf_counter()
-    cfg = config if config is not None else model.choose(series, K.shape[0])
+    if config is not None:
+        ranked = [config]
+    else:
+        cands = candidates_for(N)
+        if cands:
+            feats = system_features(series).cpu().numpy()
+            ranked = [cands[i] for i in np.argsort(model.expected_cost(feats, cands), kind="stable")]
+        else:
+            ranked = []
     t_choose = time.perf_counter() - t0
-    if cfg is None:
-        x, inf = solve_plain_K(K, b)
-        return LearnedResult(x, None, int(inf["status"]), 0, 0.0, True, t_choose)
-    x, inf = solve_with(series, cfg, K, b, tol, max_iter)
-    if int(inf["status"]) != 0:
-        x, _ = solve_plain_K(K, b)
-        return LearnedResult(x, cfg, int(inf["status"]), int(inf["iterations"]), float(inf["residual"]), True,
-                             t_choose)
-    return LearnedResult(x, cfg, 0, int(inf["iterations"]), float(inf["residual"]), False, t_choose)
+    tries = ranked[:1]
+    if ranked and ranked[0].prec == GK_F32:
+        tries += [c for c in ranked if c.prec != GK_F32][:1]
+    cfg, inf, total_its = None, None, 0
+    for cfg in tries:
+        cap = min(max_iter, MAX_ITER_F32) if cfg.prec == GK_F32 else max_iter
+        x, inf = solve_with(series, cfg, K, b, tol, cap)
+        total_its += int(inf["iterations"])
+        if int(inf["status"]) == 0:
+            return LearnedResult(x, cfg, 0, total_its, float(inf["residual"]), False, t_choose)
+    x, _ = solve_plain_K(K, b)
+    return LearnedResult(x, cfg, int(inf["status"]) if inf is not None else 0, total_its,
+                         float(inf["residual"]) if inf is not None else 0.0, True, t_choose)
 
 
 def series_of(model, device="cuda"):
