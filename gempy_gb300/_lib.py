@@ -148,6 +148,8 @@ SIGNATURES = [
                                   ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     ("gk_mlp_bwd", ctypes.c_int, [ctypes.POINTER(GkMlp), ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("gk_mlp_fwd_tc", ctypes.c_int, [ctypes.POINTER(GkMlp), ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+                                     ctypes.c_void_p, ctypes.c_void_p]),
     ("gk_mlp_mse", ctypes.c_int, [ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     ("gk_mlp_adam", ctypes.c_int, [ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

@@ -147,6 +147,18 @@ class Mlp:
                                                     w.numel(), _stream()))
         return y
 
+    def forward_tc(self, x):
+        """Inference on the tensor cores (BF16 activations between layers)."""
+        x = x.to(device=self.device, dtype=torch.float32).contiguous()
+        B = x.shape[0]
+        y = torch.empty((B, self.out_dim), dtype=torch.float32, device=self.device)
+        err = torch.zeros(1, dtype=torch.int32, device=self.device)
+        check("gk_mlp_fwd_tc", _lib.load().gk_mlp_fwd_tc(ctypes.byref(self._net()), B, _ptr(x), _ptr(y), _ptr(err),
+                                                          _stream()))
+        if int(err.item()) != 0:
+            raise _lib.GkError("gk_mlp_fwd_tc", int(err.item()))
+        return y
+
     def gradient(self, x, dy):
         """Forward on x, then the gradient of sum(dy * y) (FP32, parameter layout)."""
         lib = _lib.load()

@@ -391,6 +391,12 @@ gk_status gk_mlp_fwd(const gk_mlp* net, int64_t batch, const float* x,
 gk_status gk_mlp_bwd(const gk_mlp* net, int64_t batch, const float* x,
                      const float* dy, float* grad, void* work,
                      size_t work_bytes, gk_stream stream);
+/* Inference pass of the same network on the tensor cores (tcgen05.mma,
+ * BF16 x BF16 -> FP32 in tensor memory, 128 samples per CTA): y = net(x) with
+ * the activations between layers rounded to BF16.  ``err`` (device, may be
+ * NULL) receives GK_ERR_TIMEOUT if an MMA completion wait gives up. */
+gk_status gk_mlp_fwd_tc(const gk_mlp* net, int64_t batch, const float* x,
+                        float* y, int32_t* err, gk_stream stream);
 /* Weighted mean-squared error loss = sum_i w_i |y_i - t_i|^2 / sum_i w_i
  * (w may be NULL: all ones) into loss[0], and its gradient dy (may be NULL). */
 gk_status gk_mlp_mse(int64_t batch, int32_t out_dim, const float* y,

@@ -59,6 +59,18 @@ def forward(flat, x, in_dim, out_dim):
     return h, acts
 
 
+def forward_bf16_activations(flat, x, in_dim, out_dim):
+    """Forward pass with the layer inputs rounded to BF16 (nearest even), as
+    the tensor-core inference kernel feeds them to the MMA; sums in float64."""
+    layers = unpack(flat, in_dim, out_dim)
+    h = np.asarray(x, dtype=np.float64)
+    for li, (W, b) in enumerate(layers):
+        h = bf16_value(bf16_bits(h.astype(np.float32))).astype(np.float64)
+        z = h @ W.T + b
+        h = np.maximum(z, 0.0) if li < 2 else z
+    return h
+
+
 def backward(flat, acts, dy, in_dim, out_dim):
     """Gradient of sum(dy * y) with respect to the flat parameters."""
     layers = unpack(flat, in_dim, out_dim)

@@ -303,3 +303,15 @@ def test_compute_model_routes_large_series_through_learned_solve():
     band = 1e-5 * np.abs(zp).max()
     outside = (np.abs(zp[:, None] - iso[None, :]) > band).all(1)
     assert np.array_equal(ids_p[outside], ids_l[outside])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("F,O,B", [(21, 3, 48), (21, 3, 300), (7, 1, 1), (64, 16, 257)])
+def test_mlp_tensor_core_forward_matches_oracle(F, O, B):
+    """tcgen05 inference pass vs the oracle with BF16-rounded layer inputs
+    (FP32 accumulation on the tensor cores vs float64 sums)."""
+    net, p = _net(F, O, 7)
+    x = np.random.default_rng(8).normal(0, 1, (B, F)).astype(np.float32)
+    y = net.forward_tc(torch.as_tensor(x).cuda()).cpu().numpy()
+    yo = omlp.forward_bf16_activations(p, x, F, O)
+    assert np.abs(y - yo).max() <= 2e-3 * max(1.0, np.abs(yo).max()), np.abs(y - yo).max()
