@@ -610,6 +610,14 @@ def learned_section(n_points=20000, force_config=None):
     ev1.record()
     torch.cuda.synchronize()
     fwd_ms = ev0.elapsed_time(ev1) / reps
+    for _ in range(3):
+        model.mlp.forward_tc(x)
+    ev0.record()
+    for _ in range(reps):
+        model.mlp.forward_tc(x)
+    ev1.record()
+    torch.cuda.synchronize()
+    tc_ms = ev0.elapsed_time(ev1) / reps
     flops = 2.0 * B * (256 * (learned.IN_DIM + 1) + 256 * 257 + learned.OUT_DIM * 257)
     return {
         "workload": f"{n_points} surface points, {int(0.3 * n_points)} orientations, 10 folded surfaces, "
@@ -628,6 +636,7 @@ def learned_section(n_points=20000, force_config=None):
         "roofline": roof,
         "gain_vs_default_config": t_def_total / t_learned,
         "network": {"samples_per_forward": B, "forward_ms": fwd_ms, "forward_tflops": flops / (fwd_ms * 1e-3) / 1e12,
+                    "forward_tc_ms": tc_ms, "forward_tc_tflops": flops / (tc_ms * 1e-3) / 1e12,
                     "training": model.meta},
     }
 

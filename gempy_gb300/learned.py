@@ -222,16 +222,19 @@ class CostModel:
     def _norm(self, X):
         return (np.asarray(X, np.float32) - self.x_mean) / self.x_std
 
-    def predict(self, sys_feats, configs):
-        """Per candidate: (run seconds, failure probability, LU seconds)."""
+    def predict(self, sys_feats, configs, tensor_cores=True):
+        """Per candidate: (run seconds, failure probability, LU seconds).
+        Inference runs on the tensor cores (tcgen05, BF16 layer inputs) unless
+        ``tensor_cores`` is False (the FP32-activation path used in training)."""
         sf = np.asarray(sys_feats, np.float32).reshape(1, -1)
         X = np.concatenate([np.repeat(sf, len(configs), 0), np.stack([c.features() for c in configs])], 1)
-        y = self.mlp.forward(torch.as_tensor(self._norm(X)).to(self.mlp.device)).cpu().numpy().astype(np.float64)
+        xt = torch.as_tensor(self._norm(X)).to(self.mlp.device)
+        y = (self.mlp.forward_tc(xt) if tensor_cores else self.mlp.forward(xt)).cpu().numpy().astype(np.float64)
         y = y * self.y_std + self.y_mean
         return np.exp(y[:, 0]), np.clip(y[:, 1], 0.0, 1.0), np.exp(y[:, 2])
 
-    def expected_cost(self, sys_feats, configs):
-        t_run, p_fail, t_lu = self.predict(sys_feats, configs)
+    def expected_cost(self, sys_feats, configs, tensor_cores=True):
+        t_run, p_fail, t_lu = self.predict(sys_feats, configs, tensor_cores)
         return t_run + p_fail * t_lu
 
     def choose(self, series, N=None):

@@ -315,3 +315,22 @@ def test_mlp_tensor_core_forward_matches_oracle(F, O, B):
     y = net.forward_tc(torch.as_tensor(x).cuda()).cpu().numpy()
     yo = omlp.forward_bf16_activations(p, x, F, O)
     assert np.abs(y - yo).max() <= 2e-3 * max(1.0, np.abs(yo).max()), np.abs(y - yo).max()
+
+
+@pytest.mark.gpu
+def test_tensor_core_inference_agrees_with_training_path():
+    """The trained network's cost predictions on the tensor cores (BF16 layer
+    inputs) and on the FP32 path it was trained with pick equally good
+    configurations."""
+    from gempy_gb300 import learned, synthetic
+    if not os.path.exists(learned.DEFAULT_MODEL):
+        pytest.skip("no trained model in the package")
+    model = learned.CostModel.load()
+    for idx in range(4):
+        s = learned.series_of(synthetic.training_system(idx, base_seed=77))
+        cands = learned.candidates_for(s.N)
+        f = learned.system_features(s).cpu().numpy()
+        c_tc = model.expected_cost(f, cands, tensor_cores=True)
+        c_32 = model.expected_cost(f, cands, tensor_cores=False)
+        assert np.abs(np.log(c_tc) - np.log(c_32)).max() < 0.15
+        assert c_32[int(np.argmin(c_tc))] <= 1.1 * c_32.min()
