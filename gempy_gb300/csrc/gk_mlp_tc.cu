@@ -100,13 +100,20 @@ __global__ void __launch_bounds__(kThreads, 1) fwd_kernel(const __nv_bfloat16* _
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-    // layer-0 A operand: the samples, a ones column at F, zeros up to the padded width
+    // layer-0 A operand: the samples, a ones column at F, zeros up to the padded
+    // width; one 16-byte core-matrix row (8 consecutive k) per store
     const int k1p = pad16(F + 1);
-    for (int e = tid; e < kM * k1p; e += kThreads) {
-        const int row = e / k1p, k = e % k1p;
-        float v = 0.f;
-        if (m0 + row < B) v = k < F ? x[(m0 + row) * F + k] : (k == F ? 1.f : 0.f);
-        put_bf16(As, core_off(row, k, k1p), v);
+    for (int e = tid; e < kM * (k1p / 8); e += kThreads) {
+        const int row = e / (k1p / 8), k0 = (e % (k1p / 8)) * 8;
+        __align__(16) __nv_bfloat16 v[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int k = k0 + j;
+            float f = 0.f;
+            if (m0 + row < B) f = k < F ? x[(m0 + row) * F + k] : (k == F ? 1.f : 0.f);
+            v[j] = __float2bfloat16_rn(f);
+        }
+        *reinterpret_cast<uint4*>(As + core_off(row, k0, k1p)) = *reinterpret_cast<const uint4*>(v);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -121,10 +128,15 @@ __global__ void __launch_bounds__(kThreads, 1) fwd_kernel(const __nv_bfloat16* _
         const int np = L == 2 ? 16 : kN;  // MMA N: a multiple of 16, at least 16
         const int kp = pad16(kin + 1);
         const __nv_bfloat16* W = P + off;
-        for (int e = tid; e < np * kp; e += kThreads) {
-            const int n = e / kp, k = e % kp;
-            const __nv_bfloat16 v = (n < nout && k <= kin) ? W[(int64_t)n * (kin + 1) + k] : __float2bfloat16_rn(0.f);
-            *reinterpret_cast<__nv_bfloat16*>(Bs + core_off(n, k, kp)) = v;
+        for (int e = tid; e < np * (kp / 8); e += kThreads) {
+            const int n = e / (kp / 8), k0 = (e % (kp / 8)) * 8;
+            __align__(16) __nv_bfloat16 v[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int k = k0 + j;
+                v[j] = (n < nout && k <= kin) ? W[(int64_t)n * (kin + 1) + k] : __float2bfloat16_rn(0.f);
+            }
+            *reinterpret_cast<uint4*>(Bs + core_off(n, k0, kp)) = *reinterpret_cast<const uint4*>(v);
         }
         off += (int64_t)nout * (kin + 1);
         // generic-proxy writes of the operands -> visible to the tensor core
@@ -168,8 +180,13 @@ __global__ void __launch_bounds__(kThreads, 1) fwd_kernel(const __nv_bfloat16* _
                 uint32_t r[16];
                 tmem_ld16(lanes + (uint32_t)c0, r);
 #pragma unroll
-                for (int j = 0; j < 16; ++j)
-                    put_bf16(As, core_off(row, c0 + j, kKmax), fmaxf(__uint_as_float(r[j]), 0.f));
+                for (int h = 0; h < 2; ++h) {
+                    __align__(16) __nv_bfloat16 v[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) v[j] = __float2bfloat16_rn(fmaxf(__uint_as_float(r[8 * h + j]), 0.f));
+                    *reinterpret_cast<uint4*>(As + core_off(row, c0 + 8 * h, kKmax)) =
+                        *reinterpret_cast<const uint4*>(v);
+                }
             }
             for (int k = kN; k < kKmax; ++k) put_bf16(As, core_off(row, k, kKmax), k == kN ? 1.f : 0.f);
         } else {
