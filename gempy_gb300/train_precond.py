@@ -59,6 +59,8 @@ def main(argv=None):
     ap.add_argument("--out", default="precond_training")
     ap.add_argument("--resume", default=None, help="model .npz to continue training from")
     ap.add_argument("--dataset", default=None, help="reuse a dataset .npz instead of generating one")
+    ap.add_argument("--extra-dataset", action="append", default=[],
+                    help="dataset .npz of an earlier run to train on together with the new one (repeatable)")
     a = ap.parse_args(argv)
     os.makedirs(a.out, exist_ok=True)
     summary = dict(args=vars(a))
@@ -78,8 +80,11 @@ def main(argv=None):
         with open(os.path.join(a.out, "records.json"), "w") as f:
             json.dump(records, f)
     summary["generate_seconds"] = time.perf_counter() - t0
-    summary["samples"] = int(len(ds["cost_s"]))
     summary["systems"] = len(records)
+    for path in a.extra_dataset:
+        z = np.load(path)
+        ds = {k: np.concatenate([ds[k], z[k]]) for k in ds}
+    summary["samples"] = int(len(ds["cost_s"]))
 
     model = learned.CostModel.load(a.resume) if a.resume else None
     torch.cuda.synchronize()
