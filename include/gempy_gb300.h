@@ -181,17 +181,17 @@ gk_status gk_solve_mixed(int64_t n, const double* K, int64_t ldk,
  * multiple of 64, at most 4096).  Setup, in ``prec`` (GK_F32, GK_FF or GK_F64)
  * on the equilibrated, permuted matrix: LU without pivoting of the landmark block,
  * the landmark rows/columns (the rank-r coupling), and LU of the bs x bs
- * diagonal blocks of the Schur complement (with GK_F64, then their explicit
- * inverses, kept in unused off-diagonal space, when at least two blocks are
- * full).  GK_F32 halves the setup's memory
- * traffic but only preconditions systems with kappa(K) eps32 well below 1;
- * GK_F64 covers the densely sampled, nugget-dominated systems beyond that;
- * GK_FF keeps FP64 storage but runs the O(N r^2) restricted updates in
- * float-float on the FP32 pipe (~1e-12 relative per update), several times
- * faster than FP64 on this part.
- * The Krylov iteration is FP64 on the FP64 K, to ||b - K x||_2 <= tol ||b||_2
- * or ``max_iter`` steps; ``info`` reports status, iterations and the final
- * residual. */
+ * diagonal blocks of the Schur complement (with FP64 storage, then their
+ * explicit inverses, kept in unused off-diagonal space, when at least two
+ * blocks are full).  GK_F32 halves the setup's memory traffic but only
+ * preconditions systems with kappa(K) eps32 well below 1; GK_F64 covers the
+ * densely sampled, nugget-dominated systems beyond that; GK_FF keeps FP64
+ * storage but runs the O(N r^2) restricted updates in float-float on the FP32
+ * pipe (~1e-12 relative per update), several times faster than FP64 on this
+ * part.  The Krylov iteration is FGMRES(200) in FP64 on the FP64 K, to
+ * ||b - K x||_2 <= tol ||b||_2 or ``max_iter`` steps (it also stops when a
+ * whole restart cycle gains less than 2 %); ``info`` reports status,
+ * iterations and the final residual. */
 size_t gk_solve_twolevel_workspace_bytes(int64_t n, gk_prec prec);
 gk_status gk_solve_twolevel(int64_t n, const double* K, int64_t ldk,
                             const double* b, double* x, const int32_t* perm,

@@ -57,6 +57,36 @@ def test_struct_layouts_match_header():
     assert ctypes.sizeof(_lib.GkSystem) == 6 * 4 + 4 * 8 + 7 * 8
     assert ctypes.sizeof(_lib.GkPoints) == 16 + 8 + 48 + 8
     assert ctypes.sizeof(_lib.GkSegment) == 8 + 8 + 8 * 32 + 8 * 33
+    assert ctypes.sizeof(_lib.GkMlp) == 4 + 4 + 8
+    assert ctypes.sizeof(_lib.GkAdam) == 5 * 4
+
+
+def test_struct_layouts_match_compiled_header(tmp_path):
+    """sizeof / offsetof of every ABI struct as a C compiler sees the header."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    src = tmp_path / "layout.c"
+    src.write_text("""
+#include <stdio.h>
+#include <stddef.h>
+#include "gempy_gb300.h"
+int main(void) {
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(gk_info), sizeof(gk_system), sizeof(gk_points),
+         sizeof(gk_segment), sizeof(gk_mlp), sizeof(gk_adam), offsetof(gk_mlp, params), offsetof(gk_system, range));
+  return 0;
+}
+""")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", inc, str(src), "-o", str(exe)], check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    want = [ctypes.sizeof(_lib.GkInfo), ctypes.sizeof(_lib.GkSystem), ctypes.sizeof(_lib.GkPoints),
+            ctypes.sizeof(_lib.GkSegment), ctypes.sizeof(_lib.GkMlp), ctypes.sizeof(_lib.GkAdam),
+            _lib.GkMlp.params.offset, _lib.GkSystem.range.offset]
+    assert got == want
 
 
 def test_invalid_arguments_rejected_before_any_launch(lib):
