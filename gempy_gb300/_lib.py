@@ -112,7 +112,8 @@ SIGNATURES = [
                                               ctypes.c_void_p]),
     ("gk_solve_twolevel_workspace_bytes", ctypes.c_size_t, [ctypes.c_int64, ctypes.c_int]),
     ("gk_solve_twolevel", ctypes.c_int, [ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
-                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32,
+                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                         ctypes.c_int32,
                                          ctypes.c_int, ctypes.c_double, ctypes.c_int32, ctypes.c_void_p,
                                          ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]),
     ("gk_eval_model_bytes", ctypes.c_size_t, [ctypes.POINTER(GkSystem)]),

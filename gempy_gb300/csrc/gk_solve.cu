@@ -296,7 +296,8 @@ struct Solver {
 
 // Restarted FGMRES(S.m) in FP64 with right preconditioning S.precond;
 // convergence tested on the host between Arnoldi steps.
-static gk_status fgmres(Solver& S, const double* b, double* x, double tol, int max_iter, int& status, int& its,
+static gk_status fgmres(Solver& S, const double* b, double* x, const double* x0, double tol, int max_iter,
+                        int& status, int& its,
                         double& rel) {
     MixedWork& w = S.w;
     const int64_t n = S.n;
@@ -306,7 +307,10 @@ static gk_status fgmres(Solver& S, const double* b, double* x, double tol, int m
     gk_status s;
     double bnorm = 0.0;
     if ((s = S.norm2(b, bnorm)) != GK_OK) return s;
-    GK_CUDA_TRY(cudaMemsetAsync(x, 0, n * sizeof(double), st));
+    if (x0 != nullptr)  // warm start (e.g. the previous weights of the same series)
+        GK_CUDA_TRY(cudaMemcpyAsync(x, x0, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    else
+        GK_CUDA_TRY(cudaMemsetAsync(x, 0, n * sizeof(double), st));
     status = GK_ERR_NOT_CONVERGED;
     its = 0;
     rel = 1.0;
@@ -444,7 +448,7 @@ extern "C" gk_status gk_solve_mixed(int64_t n, const double* K, int64_t ldk, con
 
     int status = GK_ERR_NOT_CONVERGED, its = 0;
     double rel = 1.0;
-    if ((s = fgmres(S, b, x, tol, max_iter, status, its, rel)) != GK_OK) return s;
+    if ((s = fgmres(S, b, x, nullptr, tol, max_iter, status, its, rel)) != GK_OK) return s;
     {
         gk_info hi;
         GK_CUDA_TRY(cudaMemcpyAsync(&hi, info, sizeof(gk_info), cudaMemcpyDeviceToHost, st));
@@ -476,12 +480,13 @@ extern "C" size_t gk_solve_twolevel_workspace_bytes(int64_t n, gk_prec prec) {
 }
 
 extern "C" gk_status gk_solve_twolevel(int64_t n, const double* K, int64_t ldk, const double* b, double* x,
-                                       const int32_t* perm, int64_t r, int32_t bs, gk_prec prec, double tol,
+                                       const double* x0, const int32_t* perm, int64_t r, int32_t bs, gk_prec prec, double tol,
                                        int32_t max_iter, void* work, size_t work_bytes, gk_info* info,
                                        gk_stream stream) {
     cudaStream_t st = (cudaStream_t)stream;
     if (n <= 0 || K == nullptr || b == nullptr || x == nullptr || perm == nullptr || ldk < n || max_iter < 1)
         return GK_ERR_ARG;
+    if (x0 == x) return GK_ERR_ARG;
     if (r <= 0 || r >= n || (r % 64) != 0 || bs <= 0 || (bs % 64) != 0 || bs > 4096) return GK_ERR_ARG;
     if (prec != GK_F32 && prec != GK_F64 && prec != GK_FF) return GK_ERR_ARG;
     const int es = prec == GK_F32 ? 4 : 8;
@@ -514,7 +519,7 @@ extern "C" gk_status gk_solve_twolevel(int64_t n, const double* K, int64_t ldk, 
     int status = GK_ERR_NOT_CONVERGED, its = 0;
     double rel = 1.0;
     if (fst == 0) {
-        if ((s = fgmres(S, b, x, tol, max_iter, status, its, rel)) != GK_OK) return s;
+        if ((s = fgmres(S, b, x, x0, tol, max_iter, status, its, rel)) != GK_OK) return s;
     } else {
         status = fst;
     }

@@ -83,10 +83,19 @@ def _load_cost_model(path, device):
     return learned.CostModel.load(path, device=device)
 
 
-def _solve_learned(dev_s, cost_model, tol):
+def _warm_start(interpolation_input, i, n, device):
+    """The series' previous weights (``InterpolationInput.weights``, as gempy
+    passes them back, ``_engine_factory.py:45-48``) when their size fits."""
+    ws = getattr(interpolation_input, "weights", None) or []
+    if i < len(ws) and ws[i] is not None and np.size(ws[i]) == n:
+        return torch.as_tensor(np.asarray(ws[i], dtype=np.float64).ravel()).to(device)
+    return None
+
+
+def _solve_learned(dev_s, cost_model, tol, x0=None):
     """Network-chosen two-level FGMRES (FP64 LU fallback); (w, gk_info tensor)."""
     from . import learned
-    r = learned.solve_learned(dev_s, cost_model, tol=tol)
+    r = learned.solve_learned(dev_s, cost_model, tol=tol, x0=x0)
     rec = np.zeros(1, dtype=K.INFO_DTYPE)
     rec["status"] = 0 if r.fallback or r.status == 0 else r.status
     rec["iterations"] = r.iterations
@@ -191,7 +200,7 @@ def compute_model(interpolation_input, options, data_descriptor, geophysics_inpu
     series = []
     cost_model = None
     conds = []
-    for dev_s, s_off, n_s, rel in _split(interpolation_input, options, data_descriptor, device):
+    for si, (dev_s, s_off, n_s, rel) in enumerate(_split(interpolation_input, options, data_descriptor, device)):
         if getattr(ko, "compute_condition_number", False):
             Kc, _ = K.build(dev_s, GK_F64)
             conds.append(K.condition_number(Kc))
@@ -200,7 +209,8 @@ def compute_model(interpolation_input, options, data_descriptor, geophysics_inpu
             if cost_model is None:
                 cost_model = _load_cost_model(cfg.learned_model, device)
         if mixed and cost_model is not None and dev_s.N >= cfg.learned_min_n:
-            w, info = _solve_learned(dev_s, cost_model, cfg.learned_tol)
+            w, info = _solve_learned(dev_s, cost_model, cfg.learned_tol,
+                                     _warm_start(interpolation_input, si, dev_s.N, device))
         elif mixed:
             w, info = K.solve_mixed(dev_s, tol=cfg.solver_tol, max_iter=cfg.solver_max_iter)
         else:

@@ -266,10 +266,10 @@ def twolevel_permutation(series: DeviceSeries, n_landmarks, seed=0, policy="rand
 
 
 def solve_twolevel(series: DeviceSeries, n_landmarks=1024, block=512, tol=1e-8, max_iter=2000, K=None, b=None,
-                   seed=0, policy="random", prec=None):
+                   seed=0, policy="random", prec=None, x0=None):
     """FGMRES with the two-level (block-Jacobi + low-rank) preconditioner;
     ``prec`` is the preconditioner's arithmetic: GK_F32, GK_FF (FP64 storage,
-    float-float updates) or GK_F64 (the default)."""
+    float-float updates) or GK_F64 (the default); ``x0`` an initial guess."""
     lib = _lib.load()
     prec = GK_F64 if prec is None else int(prec)
     if K is None:
@@ -281,7 +281,11 @@ def solve_twolevel(series: DeviceSeries, n_landmarks=1024, block=512, tol=1e-8, 
     work = torch.empty(wb, dtype=torch.uint8, device=K.device)
     x = torch.empty(n, dtype=torch.float64, device=K.device)
     info = new_info(K.device)
-    check("gk_solve_twolevel", lib.gk_solve_twolevel(n, _ptr(K), K.stride(0), _ptr(b), _ptr(x), _ptr(pt), r,
+    if x0 is not None:
+        x0 = x0.to(device=K.device, dtype=torch.float64).contiguous()
+        if x0.shape != (n,):
+            raise ValueError("initial guess has the wrong size")
+    check("gk_solve_twolevel", lib.gk_solve_twolevel(n, _ptr(K), K.stride(0), _ptr(b), _ptr(x), _ptr(x0), _ptr(pt), r,
                                                      int(block), prec, float(tol), int(max_iter), _ptr(work), wb,
                                                      _ptr(info), _stream()))
     return x, info, r

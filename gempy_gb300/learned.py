@@ -307,9 +307,10 @@ class LearnedResult:
     seconds_choose: float
 
 
-def solve_with(series, cfg, K, b, tol=1e-8, max_iter=MAX_ITER, seed=0):
+def solve_with(series, cfg, K, b, tol=1e-8, max_iter=MAX_ITER, seed=0, x0=None):
     x, info, _ = kernels.solve_twolevel(series, n_landmarks=cfg.landmarks, block=cfg.block, tol=tol,
-                                        max_iter=max_iter, K=K, b=b, seed=seed, policy=cfg.policy, prec=cfg.prec)
+                                        max_iter=max_iter, K=K, b=b, seed=seed, policy=cfg.policy, prec=cfg.prec,
+                                        x0=x0)
     return x, kernels.read_info(info)
 
 
@@ -324,10 +325,11 @@ def solve_plain_K(K, b):
 MAX_ITER_F32 = 400
 
 
-def solve_learned(series, model, K=None, b=None, tol=1e-8, max_iter=MAX_ITER, config=None):
+def solve_learned(series, model, K=None, b=None, tol=1e-8, max_iter=MAX_ITER, config=None, x0=None):
     """Solve with the configuration the network ranks first (or ``config``).
     If FGMRES misses the tolerance with an FP32 configuration, the best-ranked
-    FP64-storage configuration is tried next; the FP64 LU is the last resort."""
+    FP64-storage configuration is tried next; the FP64 LU is the last resort.
+    ``x0``: initial guess of FGMRES (e.g. the series' previous weights)."""
     if K is None:
         K, b = kernels.build(series, GK_F64)
     N = K.shape[0]
@@ -348,7 +350,7 @@ def solve_learned(series, model, K=None, b=None, tol=1e-8, max_iter=MAX_ITER, co
     cfg, inf, total_its = None, None, 0
     for cfg in tries:
         cap = min(max_iter, MAX_ITER_F32) if cfg.prec == GK_F32 else max_iter
-        x, inf = solve_with(series, cfg, K, b, tol, cap)
+        x, inf = solve_with(series, cfg, K, b, tol, cap, x0=x0)
         total_its += int(inf["iterations"])
         if int(inf["status"]) == 0:
             return LearnedResult(x, cfg, 0, total_its, float(inf["residual"]), False, t_choose)

@@ -191,10 +191,13 @@ gk_status gk_solve_mixed(int64_t n, const double* K, int64_t ldk,
  * part.  The Krylov iteration is FGMRES(200) in FP64 on the FP64 K, to
  * ||b - K x||_2 <= tol ||b||_2 or ``max_iter`` steps (it also stops when a
  * whole restart cycle gains less than 2 %); ``info`` reports status,
- * iterations and the final residual. */
+ * iterations and the final residual.  ``x0`` (device, may be NULL; must not
+ * be ``x``) is the initial guess -- the engine passes the series' previous
+ * weights (``InterpolationInput.weights``) -- otherwise FGMRES starts from 0. */
 size_t gk_solve_twolevel_workspace_bytes(int64_t n, gk_prec prec);
 gk_status gk_solve_twolevel(int64_t n, const double* K, int64_t ldk,
-                            const double* b, double* x, const int32_t* perm,
+                            const double* b, double* x, const double* x0,
+                            const int32_t* perm,
                             int64_t r, int32_t bs, gk_prec prec, double tol,
                             int32_t max_iter, void* work, size_t work_bytes,
                             gk_info* info, gk_stream stream);

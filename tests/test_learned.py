@@ -334,3 +334,22 @@ def test_tensor_core_inference_agrees_with_training_path():
         c_32 = model.expected_cost(f, cands, tensor_cores=False)
         assert np.abs(np.log(c_tc) - np.log(c_32)).max() < 0.15
         assert c_32[int(np.argmin(c_tc))] <= 1.1 * c_32.min()
+
+
+@pytest.mark.gpu
+def test_twolevel_warm_start_from_previous_weights():
+    """FGMRES started from the previous weights (InterpolationInput.weights)
+    needs no iteration when they already solve the system and fewer than a
+    cold start when they are perturbed."""
+    from gempy_gb300 import kernels, learned, synthetic
+    s = learned.series_of(synthetic.training_system(2, base_seed=5, n_min=3000, n_max=3500))
+    K, b = kernels.build(s, kernels.GK_F64)
+    cfg = learned.PrecondConfig(512, 256, "stratified", kernels.GK_FF)
+    x, inf = learned.solve_with(s, cfg, K, b)
+    assert int(inf["status"]) == 0
+    x2, inf2 = learned.solve_with(s, cfg, K, b, x0=x)
+    assert int(inf2["status"]) == 0 and int(inf2["iterations"]) == 0
+    assert torch.equal(x2, x)
+    xp = x * (1 + 1e-6 * torch.randn_like(x))
+    x3, inf3 = learned.solve_with(s, cfg, K, b, x0=xp)
+    assert int(inf3["status"]) == 0 and int(inf3["iterations"]) < int(inf["iterations"])
