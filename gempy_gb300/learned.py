@@ -265,12 +265,18 @@ def targets(dataset):
 
 
 def train(dataset, epochs=300, batch=256, lr=2e-3, weight_decay=1e-3, seed=0, model=None, device="cuda",
-          log_every=0):
+          log_every=0, lu_weight_alpha=0.0):
     """Fit (or, given ``model``, continue fitting) the cost model on a dataset
-    from ``generate`` with AdamW under a cosine learning-rate schedule.
-    Returns (model, per-epoch mean losses)."""
+    from ``generate`` with AdamW under a cosine learning-rate schedule.  With
+    ``lu_weight_alpha`` > 0 each sample's loss is weighted by (its system's LU
+    time)^alpha, so the large systems -- where a wrong pick costs seconds --
+    count for more.  Returns (model, per-epoch mean losses)."""
     X = np.concatenate([dataset["sys_feats"], dataset["cfg_feats"]], 1).astype(np.float32)
     Y = targets(dataset)
+    wts = None
+    if lu_weight_alpha > 0:
+        w = np.asarray(dataset["t_lu"], np.float64) ** lu_weight_alpha
+        wts = torch.as_tensor((w / w.mean()).astype(np.float32)).to(device)
     if model is None:
         x_mean, x_std = X.mean(0), X.std(0) + 1e-3
         model = CostModel(Mlp(IN_DIM, OUT_DIM, seed=seed, device=device), x_mean, x_std, Y.mean(0),
@@ -286,7 +292,8 @@ def train(dataset, epochs=300, batch=256, lr=2e-3, weight_decay=1e-3, seed=0, mo
         losses = []
         for i in range(0, n, batch):
             idx = order[i:i + batch]
-            losses.append(model.mlp.train_step(Xn[idx], Yn[idx], lr=lr_ep, weight_decay=weight_decay))
+            losses.append(model.mlp.train_step(Xn[idx], Yn[idx], None if wts is None else wts[idx], lr=lr_ep,
+                                               weight_decay=weight_decay))
         hist.append(float(torch.stack(losses).mean()))
         if log_every and ep % log_every == 0:
             print(f"epoch {ep} loss {hist[-1]:.4f}", flush=True)

@@ -47,6 +47,23 @@ def evaluate(model, n_systems, base_seed, n_min, n_max, log=print):
     return out
 
 
+def rescore(model, summary_path):
+    """The new model's picks on an earlier run's held-out systems, every
+    candidate of which was run and judged there (no new solves)."""
+    with open(summary_path) as f:
+        old = json.load(f)["heldout"]
+    out = []
+    for h in old:
+        rows = h["runs"]
+        cands = [learned.PrecondConfig(**r["config"]) for r in rows]
+        k = int(np.argmin(model.expected_cost(np.asarray(h["sys_feats"], np.float32), cands)))
+        rec = dict(h)
+        rec["pick"] = rows[k]
+        rec["rank_of_pick"] = int(sorted(r["cost_s"] for r in rows).index(rows[k]["cost_s"]))
+        out.append(rec)
+    return out
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--systems", type=int, default=90)
@@ -58,6 +75,10 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--out", default="precond_training")
     ap.add_argument("--resume", default=None, help="model .npz to continue training from")
+    ap.add_argument("--lu-weight-alpha", type=float, default=0.0,
+                    help="weight each sample's loss by (LU seconds of its system)^alpha")
+    ap.add_argument("--heldout-json", default=None,
+                    help="summary.json of an earlier run: re-score its held-out runs instead of running new ones")
     ap.add_argument("--dataset", default=None, help="reuse a dataset .npz instead of generating one")
     ap.add_argument("--extra-dataset", action="append", default=[],
                     help="dataset .npz of an earlier run to train on together with the new one (repeatable)")
@@ -90,7 +111,7 @@ def main(argv=None):
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     model, hist = learned.train(ds, epochs=a.epochs, batch=256, lr=2e-3, weight_decay=1e-3, seed=a.seed, model=model,
-                                log_every=50)
+                                log_every=50, lu_weight_alpha=a.lu_weight_alpha)
     torch.cuda.synchronize()
     summary["train_seconds"] = time.perf_counter() - t1
     summary["train_steps"] = int(model.mlp.step)
@@ -99,7 +120,10 @@ def main(argv=None):
                            steps=int(model.mlp.step), final_loss=hist[-1]))
     model.save(os.path.join(a.out, "precond_cost.npz"))
 
-    ev = evaluate(model, a.heldout, base_seed=99, n_min=4000, n_max=12000)
+    if a.heldout_json:
+        ev = rescore(model, a.heldout_json)
+    else:
+        ev = evaluate(model, a.heldout, base_seed=99, n_min=4000, n_max=12000)
     summary["heldout"] = ev
     tp = sum(r["pick"]["cost_s"] for r in ev)
     td = sum(r["default"]["cost_s"] for r in ev)
