@@ -97,15 +97,16 @@ def main(argv=None):
                                      n_max=20000, seed=a.seed + 1, log=print)
         ds = {k: np.concatenate([ds1[k], ds2[k]]) for k in ds1}
         records = rec1 + rec2
-        np.savez(os.path.join(a.out, "dataset.npz"), **ds)
         with open(os.path.join(a.out, "records.json"), "w") as f:
             json.dump(records, f)
     summary["generate_seconds"] = time.perf_counter() - t0
     summary["systems"] = len(records)
+    summary["new_samples"] = int(len(ds["cost_s"]))
     for path in a.extra_dataset:
         z = np.load(path)
         ds = {k: np.concatenate([ds[k], z[k]]) for k in ds}
     summary["samples"] = int(len(ds["cost_s"]))
+    np.savez(os.path.join(a.out, "dataset.npz"), **ds)  # everything the model was trained on
 
     model = learned.CostModel.load(a.resume) if a.resume else None
     torch.cuda.synchronize()
