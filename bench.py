@@ -111,6 +111,25 @@ class ClockSampler:
                 "samples": len(rows), "power_w_max": float(max(r[2] for r in rows))}
 
 
+def slowest_rank_ms(ms, world):
+    """Replicas: the job takes as long as its slowest rank (max all-reduce of
+    the rank's own time; the only collective of the multi-GPU path)."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(points_per_rank, ms, world):
+    """Whole-job grid points/s: every rank evaluates its own grid (weak
+    scaling), the time is the slowest rank's."""
+    return world * points_per_rank / (ms * 1e-3)
+
+
 def launch_count():
     """Kernels launched so far by libgempy_gb300.so (its own counter)."""
     from gempy_gb300 import _lib
@@ -273,11 +292,7 @@ def main():
         torch.cuda.synchronize()
         if world > 1:
             dist.barrier()
-        ms = float(np.sum(per))
-        if world > 1:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = slowest_rank_ms(float(np.sum(per)), world)
         ev_ms = float(np.mean([a.elapsed_time(b) for a, b in evs]))
         return ms / steps, ev_ms
 
@@ -377,7 +392,7 @@ def main():
     ms_step = ms_mixed
     line = {
         "metric": METRIC,
-        "value": world * n_pts / (ms_step * 1e-3),
+        "value": replica_throughput(n_pts, ms_step, world),
         "unit": "grid points/s",
         "n_gpus": world,
         "steps": args.steps,
@@ -421,7 +436,7 @@ def main():
                      "fp32_pipe_achieved": achieved_tf * 168 / 20,
                      "fp32_pipe_frac": achieved_tf * 168 / 20 / fp32_peak},
     }
-    if not args.no_extra:
+    if not args.no_extra and rank == 0:
         line["batch"] = batch_section(n_real=args.batch_realisations)
         line["octree"] = octree_section()
         line["learned"] = learned_section(args.learned_points, args.learned_config)
