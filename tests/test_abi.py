@@ -97,6 +97,23 @@ def test_invalid_arguments_rejected_before_any_launch(lib):
     assert lib.gk_build(ctypes.byref(s), 0, None, 0, None, None) == _lib.GK_ERR_ARG
     assert lib.gk_lu_factor(0, -1, None, 0, None, None, 0, None, None) == _lib.GK_ERR_ARG
     assert lib.gk_solve_mixed(0, None, 0, None, None, 1e-10, 10, None, 0, None, None) == _lib.GK_ERR_ARG
+    # two-level: landmark count / block size rules, x0 aliasing x, precision enum
+    buf = ctypes.c_void_p(64)  # never dereferenced: the checks come first
+    for r, bs, prec, x0 in [(100, 64, 0, None), (64, 100, 0, None), (64, 8192, 0, None), (64, 64, 7, None),
+                            (64, 64, 0, buf)]:
+        assert lib.gk_solve_twolevel(1000, buf, 1000, buf, buf, x0, buf, r, bs, prec, 1e-8, 10, None, 0, None,
+                                     None) == _lib.GK_ERR_ARG
+    assert lib.gk_solve_twolevel_workspace_bytes(1000, 7) == 0
+    assert lib.gk_solve_twolevel_workspace_bytes(1000, _lib.GK_FF) > lib.gk_solve_twolevel_workspace_bytes(
+        1000, _lib.GK_F64)
+    # network entry points
+    net = _lib.GkMlp()
+    net.in_dim, net.out_dim, net.params = 21, 3, None
+    assert lib.gk_mlp_fwd_tc(ctypes.byref(net), 1, buf, buf, None, None) == _lib.GK_ERR_ARG
+    net.params = 64
+    assert lib.gk_mlp_fwd_tc(ctypes.byref(net), 0, buf, buf, None, None) == _lib.GK_ERR_SIZE
+    assert lib.gk_mlp_adam(10, None, None, None, None, None, None, 1, None) == _lib.GK_ERR_ARG
+    assert lib.gk_gemv(10, None, 10, None, None, None) == _lib.GK_ERR_ARG
 
 
 def test_tuning_tables_are_well_formed():
