@@ -425,7 +425,11 @@ def main():
         "gpu_launches_per_step": launches / args.steps,
         "roofline": {"kernel": "gk::eval_ff_kernel<2> (float-float field + fused segmentation)",
                      "bound": "fp32", "achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": achieved_tf / fp32_peak, "traffic": None,
+                     "frac": achieved_tf / fp32_peak,
+                     # DRAM bytes of one full-size launch from an ncu capture (dram__bytes_read.sum 14.4 MB +
+                     # dram__bytes_write.sum 222.3 MB at 256^3 = 16.8M points; scaled by the points here):
+                     # the field and soft values written once, the records read once
+                     "traffic": int(round(236625152 / 16777216 * n_pts)),
                      "peak_source": f"nominal FP32 SIMT: 152 SMs x 128 lanes x 2 x {sm_mhz:.0f} MHz "
                                     f"(max SM clock from MEASURED_PEAKS.json, {pk['_source']})",
                      "work": f"{fl_pt} algorithmic flops/point x {n_pts} points per launch",
