@@ -369,35 +369,44 @@ __global__ void __launch_bounds__(256) diag_lu_kernel(T* __restrict__ A, int64_t
     }
 }
 
-// L21 = A21 U11^-1: rows r >= k + kb, 64 rows per CTA staged in shared memory
-// (transposed so a thread walks its row without bank conflicts).
+// L21 = A21 U11^-1: rows r >= k + kb, 64 rows per CTA staged in shared memory.
+// Four threads share a row: for each column j they split the dot product over
+// the earlier columns, combine it with two shuffles and the row's first lane
+// finishes x_j, so the sequential chain per row is a quarter as long as with
+// one thread per row.
+constexpr int kTrsmRows = 64, kTrsmLanes = 4;
+
 template <typename T, int NB>
-__global__ void __launch_bounds__(64) trsm_right_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k,
-                                                        int kb) {
+__global__ void __launch_bounds__(kTrsmRows * kTrsmLanes) trsm_right_kernel(T* __restrict__ A, int64_t lda,
+                                                                            int64_t n, int64_t k, int kb) {
     __shared__ T U[NB][NB + 1];
-    __shared__ T X[NB][64 + 1];  // X[c][row]
-    const int tid = threadIdx.x;
-    for (int idx = tid; idx < NB * NB; idx += blockDim.x) {
-        int r = idx / NB, c = idx % NB;
+    __shared__ T X[kTrsmRows][NB + 1];  // X[row][c]
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int idx = tid; idx < NB * NB; idx += nt) {
+        const int r = idx / NB, c = idx % NB;
         U[r][c] = (r < kb && c < kb) ? A[(k + r) * lda + k + c] : (T)0;
     }
-    const int64_t row0 = k + kb + (int64_t)blockIdx.x * 64;
-    for (int idx = tid; idx < 64 * NB; idx += blockDim.x) {
-        int r = idx / NB, c = idx % NB;
-        int64_t gr = row0 + r;
-        X[c][r] = (gr < n && c < kb) ? A[gr * lda + k + c] : (T)0;
+    const int64_t row0 = k + kb + (int64_t)blockIdx.x * kTrsmRows;
+    for (int idx = tid; idx < kTrsmRows * NB; idx += nt) {
+        const int r = idx / NB, c = idx % NB;
+        const int64_t gr = row0 + r;
+        X[r][c] = (gr < n && c < kb) ? A[gr * lda + k + c] : (T)0;
     }
     __syncthreads();
+    const int r = tid / kTrsmLanes, part = tid % kTrsmLanes;
     for (int j = 0; j < kb; ++j) {
-        T v = X[j][tid];
-        for (int i = 0; i < j; ++i) v -= X[i][tid] * U[i][j];
-        X[j][tid] = v / U[j][j];
+        T s = (T)0;
+        for (int i = part; i < j; i += kTrsmLanes) s += X[r][i] * U[i][j];
+        s += __shfl_xor_sync(0xffffffffu, s, 1);
+        s += __shfl_xor_sync(0xffffffffu, s, 2);
+        if (part == 0) X[r][j] = (X[r][j] - s) / U[j][j];
+        __syncwarp();
     }
     __syncthreads();
-    for (int idx = tid; idx < 64 * NB; idx += blockDim.x) {
-        int r = idx / NB, c = idx % NB;
-        int64_t gr = row0 + r;
-        if (gr < n && c < kb) A[gr * lda + k + c] = X[c][r];
+    for (int idx = tid; idx < kTrsmRows * NB; idx += nt) {
+        const int rr = idx / NB, c = idx % NB;
+        const int64_t gr = row0 + rr;
+        if (gr < n && c < kb) A[gr * lda + k + c] = X[rr][c];
     }
 }
 
@@ -1205,7 +1214,8 @@ static gk_status lu_factor_nopiv(int64_t n, T* A, int64_t lda, int32_t* ipiv, vo
         GK_LAUNCH_CHECK();
         int64_t rest = n - k - kb;
         if (rest > 0) {
-            trsm_right_kernel<T, NB><<<(unsigned)((rest + 63) / 64), 64, 0, st>>>(A, lda, n, k, kb);
+            trsm_right_kernel<T, NB><<<(unsigned)((rest + kTrsmRows - 1) / kTrsmRows), kTrsmRows * kTrsmLanes, 0, st>>>(
+                A, lda, n, k, kb);
             GK_LAUNCH_CHECK();
             trsm_kernel<T, NB><<<(unsigned)((rest + 127) / 128), 128, 0, st>>>(A, lda, n, k, kb);
             GK_LAUNCH_CHECK();
@@ -1562,7 +1572,8 @@ static gk_status twolevel_setup(int64_t n, const double* K, int64_t ldk, const i
         diag_lu_kernel<T, NB><<<1, 256, 0, st>>>(A, lda, k, kb, ipiv, info);
         GK_LAUNCH_CHECK();
         const int64_t rest = n - k - kb;
-        trsm_right_kernel<T, NB><<<(unsigned)((rest + 63) / 64), 64, 0, st>>>(A, lda, n, k, kb);
+        trsm_right_kernel<T, NB><<<(unsigned)((rest + kTrsmRows - 1) / kTrsmRows), kTrsmRows * kTrsmLanes, 0, st>>>(
+                A, lda, n, k, kb);
         GK_LAUNCH_CHECK();
         trsm_kernel<T, NB><<<(unsigned)((rest + 127) / 128), 128, 0, st>>>(A, lda, n, k, kb);
         GK_LAUNCH_CHECK();
