@@ -48,17 +48,16 @@ inline int chunks_for(int64_t batch) {
 }
 
 // Workspace: H1, H2 (saved activations), D1, D2 (gradient scratch), each
-// batch x 256 FP32, then the chunked weight-gradient partials, then a few
-// floats for the loss reduction.
+// batch x 256 FP32, then the chunked weight-gradient partials.
 struct Work {
-    float *h1, *h2, *d1, *d2, *part, *red;
+    float *h1, *h2, *d1, *d2, *part;
 };
 
 inline size_t work_bytes(int in_dim, int out_dim, int64_t batch) {
     int64_t big = layer_params(1, in_dim, out_dim);
     int64_t l0 = layer_params(0, in_dim, out_dim);
     if (l0 > big) big = l0;
-    return sizeof(float) * (size_t)(4 * batch * kHidden + (int64_t)kMaxChunks * big + 64);
+    return sizeof(float) * (size_t)(4 * batch * kHidden + (int64_t)kMaxChunks * big);
 }
 
 inline Work carve(void* w, int64_t batch) {
@@ -68,7 +67,6 @@ inline Work carve(void* w, int64_t batch) {
     k.h2 = p; p += batch * kHidden;
     k.d1 = p; p += batch * kHidden;
     k.d2 = p; p += batch * kHidden;
-    k.red = p; p += 64;
     k.part = p;
     return k;
 }
