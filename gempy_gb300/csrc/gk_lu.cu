@@ -626,7 +626,8 @@ __global__ void __launch_bounds__(256) ffgemm_range_kernel(double* __restrict__ 
                                                            const float* __restrict__ Uh, const float* __restrict__ Ul,
                                                            int64_t r_lo, int64_t r_hi, int64_t c_lo, int64_t c_hi,
                                                            int diag_bs) {
-    constexpr int BM = 64, BN = 64, BK = 16, TM = 4, TN = 4;
+    // the whole 32-column panel slice is staged at once: one barrier pair per tile
+    constexpr int BM = 64, BN = 64, BK = kFfPanel, TM = 4, TN = 4;
     __shared__ float Ash[BK][BM + 1], Asl[BK][BM + 1];
     __shared__ float Bsh[BK][BN], Bsl[BK][BN];
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
