@@ -353,3 +353,30 @@ def test_twolevel_warm_start_from_previous_weights():
     xp = x * (1 + 1e-6 * torch.randn_like(x))
     x3, inf3 = learned.solve_with(s, cfg, K, b, x0=xp)
     assert int(inf3["status"]) == 0 and int(inf3["iterations"]) < int(inf["iterations"])
+
+
+@pytest.mark.parametrize("policy", ["random", "stratified"])
+def test_twolevel_permutation_layout(policy):
+    """Host-side permutation of the two-level solve: a permutation of all
+    unknowns, r a multiple of 64, every drift unknown among the landmarks,
+    the rest in Morton order, stratified landmarks spread over the Z-curve."""
+    from gempy_gb300 import kernels, learned, synthetic
+    m = synthetic.training_system(4, base_seed=11, n_min=1500, n_max=1600)
+    s = learned.series_of(m, device="cpu")
+    perm, r = kernels.twolevel_permutation(s, 300, seed=3, policy=policy)
+    N = s.N
+    assert sorted(perm.tolist()) == list(range(N))
+    assert r % 64 == 0 and 300 <= r < N
+    pos, nd = kernels.unknown_positions(s)
+    assert set(range(N - nd, N)) <= set(perm[:r].tolist())
+    rest = perm[r:]
+    codes = kernels.morton_codes(pos[rest])
+    assert np.all(np.diff(codes) >= 0)
+    if policy == "stratified":
+        # one landmark per equal stretch of the Z-curve over the covariance unknowns
+        order = np.argsort(kernels.morton_codes(pos[:N - nd]), kind="stable")
+        rank = np.empty(N - nd, dtype=np.int64)
+        rank[order] = np.arange(N - nd)
+        lm = np.sort(rank[perm[:r][perm[:r] < N - nd]])
+        step = (N - nd) / (r - nd)
+        assert np.all(np.diff(lm) <= 2 * step + 1)
