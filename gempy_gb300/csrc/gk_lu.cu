@@ -590,13 +590,18 @@ __global__ void __launch_bounds__(256) gemm_range_kernel(T* __restrict__ A, int6
 // the cross terms, and a TwoSum into a (hi, lo) accumulator whose low word
 // collects the errors (accuracy ~1e-12 of sum |a b| per update; the FP32 form
 // gives ~1e-6).  Only the epilogue (C -= hi + lo) touches the FP64 pipe.
-// Panels: L rows [o, n) x columns [k, k + kb) as Lh/Ll[i * kFfPanel + p];
-// U rows [k, k + kb) x columns [o, n) as Uh/Ul[p * n + j].
+// Panels come in pairs of two 32-column LU steps, so each trailing-update
+// launch covers 64 columns and the FP64 epilogue is paid half as often:
+// L rows x pair columns as Lh/Ll[i * kFfPair + c], U pair rows x columns as
+// Uh/Ul[c * n + j] (c = column of the pair).
 // ----------------------------------------------------------------------------
-constexpr int kFfPanel = 32;  // == LuCfg<double>::NB
+constexpr int kFfPanel = 32;  // == LuCfg<double>::NB: one LU step
+constexpr int kFfPair = 2 * kFfPanel;
 
+// Split the panel at k (kb columns; L rows [o, n), U columns [o, n)) into
+// pair columns [coff, coff + kb).
 __global__ void split_panel_kernel(const double* __restrict__ A, int64_t lda, int64_t n, int64_t k, int kb,
-                                   int64_t o, float* __restrict__ Lh, float* __restrict__ Ll,
+                                   int64_t o, int coff, float* __restrict__ Lh, float* __restrict__ Ll,
                                    float* __restrict__ Uh, float* __restrict__ Ul) {
     const int64_t m = (n - o) * kFfPanel;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < 2 * m; e += (int64_t)gridDim.x * blockDim.x) {
@@ -608,12 +613,12 @@ __global__ void split_panel_kernel(const double* __restrict__ A, int64_t lda, in
             const int64_t i = o + f / kFfPanel;
             const int p = (int)(f % kFfPanel);
             if (p < kb) v = A[i * lda + k + p];
-            dst = i * kFfPanel + p;
+            dst = i * kFfPair + coff + p;
         } else {
             const int p = (int)(f / (n - o));
             const int64_t j = o + f % (n - o);
             if (p < kb) v = A[(k + p) * lda + j];
-            dst = (int64_t)p * n + j;
+            dst = (int64_t)(coff + p) * n + j;
         }
         const float h = (float)v;
         const float l = (float)(v - (double)h);
@@ -648,8 +653,8 @@ __global__ void __launch_bounds__(256) ffgemm_range_kernel(double* __restrict__ 
             const int m = idx / BK, p = idx % BK;
             const int64_t gi = i0 + m;
             const bool ok = gi < r_hi && p0 + p < kb;
-            Ash[p][m] = ok ? Lh[gi * kFfPanel + p0 + p] : 0.f;
-            Asl[p][m] = ok ? Ll[gi * kFfPanel + p0 + p] : 0.f;
+            Ash[p][m] = ok ? Lh[gi * kFfPair + p0 + p] : 0.f;
+            Asl[p][m] = ok ? Ll[gi * kFfPair + p0 + p] : 0.f;
         }
         for (int idx = threadIdx.x; idx < BK * BN; idx += 256) {
             const int p = idx / BN, c = idx % BN;
@@ -1568,7 +1573,54 @@ static gk_status twolevel_setup(int64_t n, const double* K, int64_t ldk, const i
     permute_scale_kernel<T><<<(unsigned)((n * 32 + 255) / 256), 256, 0, st>>>(K, ldk, n, perm, d, A, lda);
     GK_LAUNCH_CHECK();
     const int64_t nblk = (n - r + bs - 1) / bs;
-    for (int64_t k = 0; k < r; k += NB) {
+    if (sizeof(T) == 8 && ffpanel != nullptr) {
+        // float-float updates, two LU steps per trailing update (r % 64 == 0)
+        double* Ad = (double*)A;
+        constexpr int BT = 64;
+        float* Lh = ffpanel;
+        float* Ll = Lh + n * kFfPair;
+        float* Uh = Ll + n * kFfPair;
+        float* Ul = Uh + n * kFfPair;
+        auto step = [&](int64_t kk) -> gk_status {  // diagonal block, L below it, U right of it
+            diag_lu_kernel<T, NB><<<1, 256, 0, st>>>(A, lda, kk, NB, ipiv, info);
+            GK_LAUNCH_CHECK();
+            const int64_t rest = n - kk - NB;
+            trsm_right_kernel<T, NB><<<(unsigned)((rest + kTrsmRows - 1) / kTrsmRows), kTrsmRows * kTrsmLanes, 0,
+                                       st>>>(A, lda, n, kk, NB);
+            GK_LAUNCH_CHECK();
+            trsm_kernel<T, NB><<<(unsigned)((rest + 127) / 128), 128, 0, st>>>(A, lda, n, kk, NB);
+            GK_LAUNCH_CHECK();
+            return GK_OK;
+        };
+        auto update = [&](int kb, int64_t r_lo, int64_t r_hi, int64_t c_lo, int64_t c_hi, int diag) -> gk_status {
+            if (r_hi <= r_lo || c_hi <= c_lo) return GK_OK;
+            const int64_t rows = diag ? diag : r_hi - r_lo, cols = diag ? diag : c_hi - c_lo;
+            dim3 g((unsigned)((cols + BT - 1) / BT), (unsigned)((rows + BT - 1) / BT), diag ? (unsigned)nblk : 1u);
+            ffgemm_range_kernel<<<g, 256, 0, st>>>(Ad, lda, n, kb, Lh, Ll, Uh, Ul, r_lo, r_hi, c_lo, c_hi, diag);
+            GK_LAUNCH_CHECK();
+            return GK_OK;
+        };
+        const unsigned sgrid = 4 * kSMs;
+        gk_status e;
+        for (int64_t k = 0; k < r; k += kFfPair) {
+            const int64_t o1 = k + kFfPanel, o2 = k + kFfPair;
+            if ((e = step(k)) != GK_OK) return e;
+            split_panel_kernel<<<sgrid, 256, 0, st>>>(Ad, lda, n, k, kFfPanel, o1, 0, Lh, Ll, Uh, Ul);
+            GK_LAUNCH_CHECK();
+            // the second step's columns (all rows below) and rows (all columns right)
+            if ((e = update(kFfPanel, o1, n, o1, o2, 0)) != GK_OK) return e;
+            if ((e = update(kFfPanel, o1, o2, o2, n, 0)) != GK_OK) return e;
+            if ((e = step(o1)) != GK_OK) return e;
+            split_panel_kernel<<<sgrid, 256, 0, st>>>(Ad, lda, n, o1, kFfPanel, o2, kFfPanel, Lh, Ll, Uh, Ul);
+            GK_LAUNCH_CHECK();
+            // both steps at once: landmark rows x all columns, other rows x landmark
+            // columns, diagonal blocks of the Schur complement
+            if ((e = update(kFfPair, o2, r, o2, n, 0)) != GK_OK) return e;
+            if ((e = update(kFfPair, r, n, o2, r, 0)) != GK_OK) return e;
+            if ((e = update(kFfPair, r, n, r, n, bs)) != GK_OK) return e;
+        }
+    }
+    for (int64_t k = 0; k < r && ffpanel == nullptr; k += NB) {
         const int kb = (int)min((int64_t)NB, r - k);
         diag_lu_kernel<T, NB><<<1, 256, 0, st>>>(A, lda, k, kb, ipiv, info);
         GK_LAUNCH_CHECK();
@@ -1579,28 +1631,6 @@ static gk_status twolevel_setup(int64_t n, const double* K, int64_t ldk, const i
         trsm_kernel<T, NB><<<(unsigned)((rest + 127) / 128), 128, 0, st>>>(A, lda, n, k, kb);
         GK_LAUNCH_CHECK();
         const int64_t o = k + kb;
-        if (sizeof(T) == 8 && ffpanel != nullptr) {
-            double* Ad = (double*)A;
-            constexpr int BT = 64;
-            float* Lh = ffpanel;
-            float* Ll = Lh + n * kFfPanel;
-            float* Uh = Ll + n * kFfPanel;
-            float* Ul = Uh + n * kFfPanel;
-            split_panel_kernel<<<4 * kSMs, 256, 0, st>>>(Ad, lda, n, k, kb, o, Lh, Ll, Uh, Ul);
-            GK_LAUNCH_CHECK();
-            if (o < r) {
-                dim3 ga((unsigned)((n - o + BT - 1) / BT), (unsigned)((r - o + BT - 1) / BT));
-                ffgemm_range_kernel<<<ga, 256, 0, st>>>(Ad, lda, n, kb, Lh, Ll, Uh, Ul, o, r, o, n, 0);
-                GK_LAUNCH_CHECK();
-                dim3 gb((unsigned)((r - o + BT - 1) / BT), (unsigned)((n - r + BT - 1) / BT));
-                ffgemm_range_kernel<<<gb, 256, 0, st>>>(Ad, lda, n, kb, Lh, Ll, Uh, Ul, r, n, o, r, 0);
-                GK_LAUNCH_CHECK();
-            }
-            dim3 gc((unsigned)((bs + BT - 1) / BT), (unsigned)((bs + BT - 1) / BT), (unsigned)nblk);
-            ffgemm_range_kernel<<<gc, 256, 0, st>>>(Ad, lda, n, kb, Lh, Ll, Uh, Ul, r, n, r, n, bs);
-            GK_LAUNCH_CHECK();
-            continue;
-        }
         if (sizeof(T) == 8) {
             double* Ad = (double*)A;
             constexpr int BT = 64;
@@ -1703,7 +1733,7 @@ gk_status gk_internal_twolevel_setup_f64(int64_t n, const double* K, int64_t ldk
                                          float* ffpanel) {
     return twolevel_setup<double>(n, K, ldk, perm, d, r, bs, A, lda, ipiv, work, wbytes, info, st, ffpanel);
 }
-size_t gk_internal_ff_panel_floats(int64_t n) { return (size_t)4 * kFfPanel * (size_t)n; }
+size_t gk_internal_ff_panel_floats(int64_t n) { return (size_t)4 * kFfPair * (size_t)n; }
 gk_status gk_internal_twolevel_apply(int64_t n, const float* A, int64_t lda, const int32_t* perm, const double* d,
                                      int64_t r, int bs, const double* v, double* z, float* t, void* work,
                                      size_t wbytes, gk_info* info, cudaStream_t st) {
