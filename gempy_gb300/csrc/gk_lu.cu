@@ -345,22 +345,29 @@ __global__ void __launch_bounds__(256) diag_lu_kernel(T* __restrict__ A, int64_t
     }
     if (tid < kb) ipiv[k + tid] = (int32_t)(k + tid);
     __syncthreads();
+    // Right-looking sweep with one barrier per step: the multipliers are used
+    // unscaled (S[i][j] * inv on the fly) and column j, which no later step
+    // reads, is scaled in one pass after the sweep.
+    int steps = kb;
     for (int j = 0; j < kb; ++j) {
         const T pv = S[j][j];
         const bool bad = !(pv == pv) || pv == (T)0 || !(gabs(pv) < (T)INFINITY);
         if (bad) {
             if (tid == 0) report(info, GK_ERR_SINGULAR, (int)(k + j));
+            steps = j;
             break;  // uniform: every thread sees the same pivot
         }
         const T inv = (T)1 / pv;
-        for (int i = j + 1 + tid; i < kb; i += blockDim.x) S[i][j] *= inv;
-        __syncthreads();
         const int w = kb - j - 1;
         for (int idx = tid; idx < w * w; idx += blockDim.x) {
             const int i = j + 1 + idx / w, c = j + 1 + idx % w;
-            S[i][c] -= S[i][j] * S[j][c];
+            S[i][c] -= (S[i][j] * inv) * S[j][c];
         }
         __syncthreads();
+    }
+    for (int idx = tid; idx < NB * NB; idx += blockDim.x) {
+        const int i = idx / NB, j = idx % NB;
+        if (j < steps && i > j && i < kb) S[i][j] *= (T)1 / S[j][j];  // the same rounding as inv above
     }
     __syncthreads();
     for (int idx = tid; idx < NB * NB; idx += blockDim.x) {
