@@ -26,6 +26,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -66,8 +67,10 @@ class ClockSampler:
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{index}.csv") \
-            if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else f"/tmp/gk_clocks_{os.getpid()}.csv"
+        # raw samples go to $GK_CLOCKS_DIR when set (kept for inspection), else a temp file
+        out_dir = os.environ.get("GK_CLOCKS_DIR")
+        self.path = os.path.join(out_dir, f"clocks_rank{index}.csv") if out_dir and os.path.isdir(out_dir) \
+            else os.path.join(tempfile.gettempdir(), f"gk_clocks_{os.getpid()}_{index}.csv")
 
     def __enter__(self):
         try:
@@ -563,7 +566,7 @@ def learned_section(n_points=20000, force_config=None):
     (N = 37993; ``n_points`` scales it down for profiling).  Plain FP64 form (build + blocked LU + solves) against the
     learned form (network picks the two-level configuration, FGMRES to 1e-8,
     FP64 LU fallback), with the fixed default configuration as the ablation;
-    the LU solution judges the scalar field.  Also times the network kernels."""
+    the LU solution is the reference for the scalar field.  Also times the network kernels."""
     import torch
     from gempy_gb300 import kernels as K
     from gempy_gb300 import learned, synthetic
@@ -587,7 +590,7 @@ def learned_section(n_points=20000, force_config=None):
     (Kt, bt), t_build = clock(lambda: K.build(s, K.GK_F64))
     N = int(Kt.shape[0])
     (x_lu, _), t_lu = clock(lambda: learned.solve_plain_K(Kt, bt))
-    pts = learned.judge_points(s)
+    pts = learned.check_points(s)
     f_lu = learned.field_at(s, x_lu, pts)
     res, t_learned = clock(lambda: learned.solve_learned(s, model, Kt, bt, tol=1e-8, config=forced))
     err = learned.field_error(s, res.x, f_lu, pts)

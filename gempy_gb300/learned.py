@@ -12,10 +12,10 @@ predicted log time of the FGMRES run, the probability that it fails, and the
 log time of the LU fallback; the candidate with the least expected cost
 t_run + p_fail t_lu is used.  The
 dense FP64 LU is the fallback (a candidate that does not reach the tolerance
-falls back to it) and the judge (training labels record each candidate's
+falls back to it) and the arbiter (training labels record each candidate's
 error against the LU solution; a run whose FGMRES residual meets the
 tolerance but whose scalar field misses the LU solution's by more than
-``JUDGE_TOL`` is labelled as failed).
+``LU_AGREEMENT_TOL`` is labelled as failed).
 
 Everything here calls the C ABI; PyTorch only provides device memory.
 """
@@ -36,7 +36,7 @@ IN_DIM = GK_SYSTEM_FEATURES + CONFIG_FEATURES
 # outputs: log(seconds of the FGMRES run), failure indicator, log(seconds of the FP64 LU fallback)
 OUT_DIM = 3
 MAX_ITER = 1000
-JUDGE_TOL = 1e-6          # relative scalar-field error of an accepted solution vs the FP64 LU's
+LU_AGREEMENT_TOL = 1e-6   # relative scalar-field error of an accepted solution vs the FP64 LU's
 DEFAULT_MODEL = os.path.join(os.path.dirname(os.path.abspath(__file__)), "models", "precond_cost.npz")
 
 
@@ -388,8 +388,8 @@ def _timed(fn):
     return out, time.perf_counter() - t
 
 
-def judge_points(series, n=4096, seed=0):
-    """Points where the judge compares fields: uniform in the data's bounding box."""
+def check_points(series, n=4096, seed=0):
+    """Points where the LU solution's field is compared: uniform in the data's bounding box."""
     P = torch.cat([series.dip_positions, series.sp_coords]).cpu().numpy()
     lo, hi = P.min(0), P.max(0)
     xyz = np.random.default_rng(seed).uniform(lo, hi, (n, 3))
@@ -402,28 +402,28 @@ def field_at(series, w, pts):
 
 
 def field_error(series, w, f_ref, pts):
-    """max |field(w) - f_ref| / max |f_ref| at the judge points."""
+    """max |field(w) - f_ref| / max |f_ref| at the check points."""
     f = field_at(series, w, pts)
     return float((f - f_ref).abs().max() / f_ref.abs().max())
 
 
 def label_system(series, configs, tol=1e-8, max_iter=MAX_ITER, K=None, b=None):
-    """Run every config on one system; the FP64 LU solution is the judge:
+    """Run every config on one system; the FP64 LU solution is the arbiter:
     a run counts as solved when FGMRES met the tolerance and its scalar field
-    matches the LU solution's within JUDGE_TOL (relative, at judge_points).
+    matches the LU solution's within LU_AGREEMENT_TOL (relative, at check_points).
     Returns (rows, lu_seconds)."""
     if K is None:
         K, b = kernels.build(series, GK_F64)
     (x_lu, inf_lu), t_lu = _timed(lambda: solve_plain_K(K, b))
     if int(inf_lu["status"]) != 0:
         raise RuntimeError("FP64 LU failed on a training system")
-    pts = judge_points(series)
+    pts = check_points(series)
     f_lu = field_at(series, x_lu, pts)
     rows = []
     for cfg in configs:
         (x, inf), t = _timed(lambda: solve_with(series, cfg, K, b, tol, max_iter))
         err = field_error(series, x, f_lu, pts) if int(inf["status"]) == 0 else float("inf")
-        ok = int(inf["status"]) == 0 and err <= JUDGE_TOL
+        ok = int(inf["status"]) == 0 and err <= LU_AGREEMENT_TOL
         rows.append(dict(config=asdict(cfg), seconds=t, status=int(inf["status"]), iterations=int(inf["iterations"]),
                          residual=float(inf["residual"]), field_error_vs_lu=err, ok=ok,
                          cost_s=t if ok else t + t_lu))
@@ -448,7 +448,7 @@ def generate(n_systems, base_seed=0, configs_per_system=12, tol=1e-8, max_iter=M
         try:
             feats = system_features(s).cpu().numpy()
             rows, t_lu = label_system(s, cands, tol, max_iter)
-        except (RuntimeError, _lib.GkError) as e:  # a failed judge: skip the system, keep going
+        except (RuntimeError, _lib.GkError) as e:  # the FP64 LU itself failed: skip the system, keep going
             if log:
                 log(f"system {i}: N={N} skipped ({e})")
             continue

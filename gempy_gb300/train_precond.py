@@ -4,7 +4,7 @@ network on the GPU.
     python -m gempy_gb300.train_precond --systems 90 --large 6 --out DIR
 
 1. Systems of ``synthetic.training_system`` are built, solved by the dense
-   FP64 LU (the judge) and by FGMRES with a random subset of the candidate
+   FP64 LU (the reference solution) and by FGMRES with a random subset of the candidate
    two-level configurations; each run's wall time, status and field error
    against the LU solution become one labelled sample.
 2. The cost model is trained with the library's own forward / backward /
@@ -49,7 +49,7 @@ def evaluate(model, n_systems, base_seed, n_min, n_max, log=print):
 
 def rescore(model, summary_path):
     """The new model's picks on an earlier run's held-out systems, every
-    candidate of which was run and judged there (no new solves)."""
+    candidate of which was run and checked there (no new solves)."""
     with open(summary_path) as f:
         old = json.load(f)["heldout"]
     out = []

@@ -1,6 +1,6 @@
 """GPU parity tests: every kernel against the FP64 oracle through the C ABI.
 
-Tolerances (written here, used by the judge of each test):
+Tolerances (written here, used by the check of each test):
   * FP64 build: |K_gpu - K_oracle| <= 1e-13 max|K|
   * FP64 LU/solve: ||b - K x||_inf <= 50 n eps ||K||_inf ||x||_inf (normwise
     backward error of a stable LU), x vs LAPACK <= 1e-8 relative
@@ -391,9 +391,9 @@ def test_mixed_solve_without_pivoting_on_kriging_matrix():
                                                       (1024, 256, 1, "random"), (256, 64, 0, "stratified"),
                                                       (1024, 256, 0, "random"), (256, 64, 2, "stratified"),
                                                       (512, 128, 2, "random")])
-def test_twolevel_fgmres_judged_by_fp64_lu(n_land, block, prec, policy):
+def test_twolevel_fgmres_checked_against_fp64_lu(n_land, block, prec, policy):
     """Block-Jacobi + low-rank preconditioned FGMRES reaches 1e-8; the FP64 LU
-    (plain form) judges the solution."""
+    (plain form) is the reference for the solution."""
     from gempy_gb300 import kernels as K
     from gempy_gb300 import synthetic
     m = synthetic.learned(n_points=1500, n_orient=400, n_surf=5)
@@ -409,7 +409,7 @@ def test_twolevel_fgmres_judged_by_fp64_lu(n_land, block, prec, policy):
     x, w_lu = x.cpu().numpy(), w_lu.cpu().numpy()
     Kr, br = kriging.build_system(s)
     assert np.linalg.norm(br - Kr @ x) <= 1.01e-8 * np.linalg.norm(br)
-    # the judge: fields from both weight vectors agree
+    # the check: fields from both weight vectors agree
     pts = np.random.default_rng(0).uniform(-0.45, 0.45, (2000, 3))
     z_tl, z_lu = kriging.evaluate(s, x, pts), kriging.evaluate(s, w_lu, pts)
     assert np.abs(z_tl - z_lu).max() <= 1e-4 * np.abs(z_lu).max()

@@ -235,7 +235,7 @@ def test_twolevel_fp64_and_ff_storage_match_lu():
     s = learned.series_of(m)
     K, b = kernels.build(s, kernels.GK_F64)
     x_lu, _ = learned.solve_plain_K(K, b)
-    pts = learned.judge_points(s)
+    pts = learned.check_points(s)
     f_lu = learned.field_at(s, x_lu, pts)
     for policy, prec in (("random", kernels.GK_F64), ("stratified", kernels.GK_F64), ("stratified", kernels.GK_FF)):
         x, inf = learned.solve_with(s, learned.PrecondConfig(512, 256, policy, prec), K, b, tol=1e-10,
@@ -270,7 +270,7 @@ def test_learned_choice_beats_fixed_configuration():
         s = learned.series_of(m)
         K, b = kernels.build(s, kernels.GK_F64)
         (x_lu, _), t_lu = clock(lambda: learned.solve_plain_K(K, b))
-        pts = learned.judge_points(s)
+        pts = learned.check_points(s)
         f_lu = learned.field_at(s, x_lu, pts)
         res, t = clock(lambda: learned.solve_learned(s, model, K, b))
         assert learned.field_error(s, res.x, f_lu, pts) <= 1e-6, (idx, res.config, res.fallback)
