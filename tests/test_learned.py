@@ -380,3 +380,22 @@ def test_twolevel_permutation_layout(policy):
         lm = np.sort(rank[perm[:r][perm[:r] < N - nd]])
         step = (N - nd) / (r - nd)
         assert np.all(np.diff(lm) <= 2 * step + 1)
+
+
+def test_cost_model_checkpoint_round_trip(tmp_path):
+    """Weights, optimizer state, step and normalisation survive save/load
+    (host-side; no network evaluation)."""
+    from gempy_gb300 import learned
+    net = learned.Mlp(seed=4, device="cpu")
+    net.m.fill_(0.25)
+    net.v.fill_(0.5)
+    net.step = 17
+    model = learned.CostModel(net, np.arange(learned.IN_DIM), np.ones(learned.IN_DIM) * 2, [1.0, 2.0, 3.0],
+                              [0.5, 0.5, 0.5], {"note": "test"})
+    path = tmp_path / "m.npz"
+    model.save(str(path))
+    back = learned.CostModel.load(str(path), device="cpu")
+    assert back.mlp.step == 17 and back.meta == {"note": "test"}
+    assert torch.equal(back.mlp.params, net.params) and torch.equal(back.mlp.master, net.master)
+    assert torch.equal(back.mlp.m, net.m) and torch.equal(back.mlp.v, net.v)
+    assert np.array_equal(back.y_mean, [1.0, 2.0, 3.0]) and np.array_equal(back.x_std, model.x_std)
