@@ -33,6 +33,26 @@ def test_anticline_scalar_field_approval_file():
     assert np.abs(sampled - approved).max() < 3e-5
 
 
+def test_anticline_residual_is_affine():
+    """The 2.2e-5 difference to the approval file is an affine function of the
+    field and x (a 4.5e-5 relative field scale and a small tilt): after an
+    affine fit under 1e-6 remains, i.e. the conventions reproduce the
+    reference's field shape to ~1e-6."""
+    g = load_golden("anticline_corners.json")
+    s = oracle_series_from_golden(g)
+    oc = g["octree"]
+    levels = pipeline.compute_octree([s], [segmentation.BASEMENT], g["unit_values"], g["sigmoid_slope"],
+                                     golden_extent(g), oc["base_resolution"], oc["levels"])
+    P, z = levels[-1][0], levels[-1][1].fields[0]
+    step = len(z) // 50
+    zs, Ps = z[::step], P[::step]
+    d = zs - np.array(oc["approved_scalar_field_last_level"])
+    A = np.column_stack([np.ones_like(zs), zs, Ps])
+    c, *_ = np.linalg.lstsq(A, d, rcond=None)
+    assert np.abs(A @ c - d).max() < 1e-6
+    assert abs(c[1] + 4.5e-5) < 1e-5  # the relative field scale
+
+
 def test_kernel_symmetric_and_rhs():
     g = load_golden("anticline_corners.json")
     s = oracle_series_from_golden(g)
