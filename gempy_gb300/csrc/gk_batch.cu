@@ -393,13 +393,13 @@ __global__ void __launch_bounds__(256) batch_prepare_kernel(const BatchDesc* __r
         double z = 0.0;
         for (int o = lane; o < d.n_ori; o += 32) {
             const double hx = d.dip[3 * o] - x0, hy = d.dip[3 * o + 1] - y0, hz = d.dip[3 * o + 2] - z0;
-            const double rr = sqrt(hx * hx + hy * hy + hz * hz);
+            const double rr = sqrt(hx * hx + hy * hy + hz * hz + kDistEps2);
             z += d.c_o * cv.d1_r(rr) *
                  (wv[o] * hx + wv[d.n_ori + o] * hy + wv[2 * d.n_ori + o] * hz);
         }
         for (int p = lane; p < d.n_sp; p += 32) {
             const double hx = x0 - d.sp[3 * p], hy = y0 - d.sp[3 * p + 1], hz = z0 - d.sp[3 * p + 2];
-            z += d.c_o * d.alpha[p] * cv.C(sqrt(hx * hx + hy * hy + hz * hz));
+            z += d.c_o * d.alpha[p] * cv.C(sqrt(hx * hx + hy * hy + hz * hz + kDistEps2));
         }
         for (int o = 16; o > 0; o >>= 1) z += __shfl_down_sync(0xffffffffu, z, o);
         if (lane == 0) {
@@ -515,6 +515,7 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchDesc* __rest
         const BatchDesc& d = D[s];
         const int64_t c = item - chunk_prefix[s];
         const double q = d.meta[0], inv_a = d.meta[2];
+        const float eps2 = (float)(kDistEps2 * inv_a * inv_a);
         const int nt = tiles_of(s);
         const int to = (d.n_ori + rec_ori - 1) / rec_ori;
         const int nyz = d.dims[1] * d.dims[2];
@@ -585,7 +586,7 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchDesc* __rest
 #pragma unroll
                     for (int p = 0; p < kPPT; ++p) {
                         float dh[3], dl[3];
-                        ff r2 = ff_dist2(X[p], ph, pl, dh, dl);
+                        ff r2 = ff_dist2(X[p], ph, pl, dh, dl, eps2);
                         if (r2.h >= 1.f) continue;
                         ff sr = ff_sqrt(r2);
                         ff kk = ff_add_f(ff_mul_f(r2, 5.25f), -17.5f);
@@ -607,7 +608,7 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchDesc* __rest
 #pragma unroll
                     for (int p = 0; p < kPPT; ++p) {
                         float dh[3], dl[3];
-                        ff r2 = ff_dist2(X[p], ph, pl, dh, dl);
+                        ff r2 = ff_dist2(X[p], ph, pl, dh, dl, eps2);
                         if (r2.h >= 1.f) continue;
                         ff sr = ff_sqrt(r2);
                         ff cc = ff_add_f(ff_mul_f(r2, 0.75f), -3.5f);

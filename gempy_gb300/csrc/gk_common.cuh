@@ -37,6 +37,15 @@ constexpr int kSMs = 152;  // GB300: 2 dies x 76 SMs (queried at run time too)
 // Regulariser of h_u h_v / r^2 in the gradient-gradient block.
 constexpr double kGradEps = 1e-5;
 
+// Every distance is r = sqrt(|h|^2 + kDistEps2).  The reference engine
+// differentiates its kernel with PyTorch autodiff with respect to the point
+// and orientation positions and asserts finite gradients
+// (test/test_modules/test_ad/test_ad_I.py:48-54), which a bare sqrt at r = 0
+// (the diagonal) would make NaN, so its distances carry a regulariser.  The
+// value 1e-10 (r = 1e-5 at coincident points, transformed frame) is the one
+// the anticline approval file selects; it moves C'/r(0) by 105/4 * 1e-5 / a^3.
+constexpr double kDistEps2 = 1e-10;
+
 // Iteration cap of every inter-CTA spin wait: ~seconds at worst, then the
 // kernel records GK_ERR_TIMEOUT and returns instead of hanging the GPU.
 constexpr long long kSpinLimit = 20LL * 1000 * 1000;

@@ -294,7 +294,7 @@ __global__ void __launch_bounds__(256) eval_kernel(const EvalParams P) {
 #pragma unroll
                         for (int p = 0; p < PPT; ++p) {
                             const T hx = ox - x[p][0], hy = oy - x[p][1], hz = oz - x[p][2];
-                            const T r = fast_r<T>(hx * hx + hy * hy + hz * hz);
+                            const T r = fast_r<T>(hx * hx + hy * hy + hz * hz + (T)kDistEps2);
                             const T k1 = cv.d1_r(r);
                             const T wh = wx * hx + wy * hy + wz * hz;
                             zt[p] += k1 * wh;
@@ -315,7 +315,7 @@ __global__ void __launch_bounds__(256) eval_kernel(const EvalParams P) {
 #pragma unroll
                         for (int p = 0; p < PPT; ++p) {
                             const T hx = x[p][0] - px, hy = x[p][1] - py, hz = x[p][2] - pz;
-                            const T r = fast_r<T>(hx * hx + hy * hy + hz * hz);
+                            const T r = fast_r<T>(hx * hx + hy * hy + hz * hz + (T)kDistEps2);
                             zt[p] += al * cv.C(r);
                             if (GRAD) {
                                 const T k1 = al * cv.d1_r(r);
@@ -410,6 +410,7 @@ __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const 
     }
     __syncthreads();
     const double q = meta[0], inv_a = meta[2];
+    const float eps2 = (float)(kDistEps2 * inv_a * inv_a);
     const int64_t chunk_pts = (int64_t)blockDim.x * PPT;
     const int64_t n_chunks = (P.n + chunk_pts - 1) / chunk_pts;
     const int n_tiles = P.tiles_ori + P.tiles_sp;
@@ -479,7 +480,7 @@ __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const 
 #pragma unroll
                         for (int p = 0; p < PPT; ++p) {
                             float dh[3], dl[3];
-                            ff r2 = ff_dist2(X[p], ph, pl, dh, dl);
+                            ff r2 = ff_dist2(X[p], ph, pl, dh, dl, eps2);
                             if (r2.h >= 1.f) continue;  // beyond the range: C'/r = 0
                             ff sr = ff_sqrt(r2);
                             ff k = ff_add_f(ff_mul_f(r2, 5.25f), -17.5f);
@@ -502,7 +503,7 @@ __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const 
 #pragma unroll
                         for (int p = 0; p < PPT; ++p) {
                             float dh[3], dl[3];
-                            ff r2 = ff_dist2(X[p], ph, pl, dh, dl);
+                            ff r2 = ff_dist2(X[p], ph, pl, dh, dl, eps2);
                             if (r2.h >= 1.f) continue;  // beyond the range: C = 0
                             ff sr = ff_sqrt(r2);
                             ff c = ff_add_f(ff_mul_f(r2, 0.75f), -3.5f);

@@ -119,9 +119,11 @@ __device__ __forceinline__ void ff_point(const double* xd, double inv_a, double 
     }
 }
 
-// r^2 of d = x - p as float-float; d_k = dh_k + dl_k with dh_k exact when the
-// split is exact, else recovered with a two-sum.
-__device__ __forceinline__ ff ff_dist2(const PointFF& X, const float* ph, const float* pl, float* dh, float* dl) {
+// r^2 + eps2 of d = x - p as float-float (eps2 is the distance regulariser
+// in the scaled frame, kDistEps2 / range^2); d_k = dh_k + dl_k with dh_k exact
+// when the split is exact, else recovered with a two-sum.
+__device__ __forceinline__ ff ff_dist2(const PointFF& X, const float* ph, const float* pl, float* dh, float* dl,
+                                       float eps2) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         if (X.exact) {
@@ -136,7 +138,7 @@ __device__ __forceinline__ ff ff_dist2(const PointFF& X, const float* ph, const 
     ff a0 = two_prod(dh[0], dh[0]), a1 = two_prod(dh[1], dh[1]), a2 = two_prod(dh[2], dh[2]);
     ff s1 = two_sum(a0.h, a1.h);
     ff s2 = two_sum(s1.h, a2.h);
-    float low = s1.l + s2.l + a0.l + a1.l + a2.l;
+    float low = s1.l + s2.l + a0.l + a1.l + a2.l + eps2;
     low = __fmaf_rn(dl[0], 2.f * dh[0] + dl[0], low);
     low = __fmaf_rn(dl[1], 2.f * dh[1] + dl[1], low);
     low = __fmaf_rn(dl[2], 2.f * dh[2] + dl[2], low);

@@ -94,7 +94,7 @@ __device__ inline T dist(const T* a, const T* b, T* h) {
     h[0] = a[0] - b[0];
     h[1] = a[1] - b[1];
     h[2] = a[2] - b[2];
-    return gsqrt<T>(h[0] * h[0] + h[1] * h[1] + h[2] * h[2]);
+    return gsqrt<T>(h[0] * h[0] + h[1] * h[1] + h[2] * h[2] + (T)kDistEps2);
 }
 
 template <typename T>

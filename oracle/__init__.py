@@ -17,14 +17,17 @@ FP64, and anchors parity on the reference's own call site
 (``gempy/modules/data_manipulation/_engine_factory.py:14-58``) and its
 known-answer tests:
 
-* pinned: the anticline cube-corner lithology ids ``[3,3,3,3,1,1,1,1]``
+* pinned, ids: the anticline cube-corner lithology ids ``[3,3,3,3,1,1,1,1]``
   (``test/test_modules/test_grids/test_custom_grid.py:44-65``), reproduced
   from the bundled ``examples/data/input_data/jan_models/model2_*.csv`` inputs
   with the input transform pinned by the reference's approved model JSON
   (``test_custom_grid.test_custom_grid.verify/fold.approved.txt:108-126``);
-* not pinned (parity at the block level is unpinned): the 50-value scalar-field
-  approval files of ``test/test_model_types`` depend on the engine's octree
-  refinement rule and point order, which are not in the reference.
+* pinned, field: the 51-value scalar-field approval file of the anticline's
+  finest octree level (``test/test_model_types/test_example_models_I.py:41-53``)
+  under the reference's comparator ``np.allclose(rtol=1e-5, atol=1e-5)``
+  (``test/verify_helper.py:70-103``), octree point order included.  The
+  block-level conventions (``kriging`` module docstring) were chosen with this
+  file; the fault and combination approval files judge them independently.
 
 Modules: ``covariance`` (kernel functions), ``kriging`` (matrix build, solve,
 evaluation), ``segmentation`` (sigmoid ids, series masks), ``octree`` (corner

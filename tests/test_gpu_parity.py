@@ -281,7 +281,8 @@ def test_compute_model_anticline_pins():
     z = sol.octrees_output[-1].outputs[0].scalar_field
     approved = np.array(g["octree"]["approved_scalar_field_last_level"])
     assert len(z) == 7808
-    assert np.abs(z[:: len(z) // 50] - approved).max() < 3e-5
+    # the reference's comparator (test/verify_helper.py:70-103)
+    assert np.allclose(z[:: len(z) // 50], approved, rtol=1e-5, atol=1e-5)
     s = oracle_series_from_golden(g)
     lv = pipeline.compute_octree([s], [segmentation.BASEMENT], g["unit_values"], g["sigmoid_slope"], ext,
                                  [2, 2, 2], 5)
