@@ -147,9 +147,9 @@ def reference_arm(args):
         return
     from gempy_gb300 import synthetic
     from oracle import kriging, segmentation
-    from tests._models import oracle_series_list
+    from oracle.inputs import series_from_engine_inputs
     m = synthetic.precision()
-    (s,) = oracle_series_list(m)
+    (s,) = series_from_engine_inputs(m.interpolation_input, m.options, m.data_descriptor)
     grid = m.interpolation_input.grid.dense_grid
     n_total = grid.n_points
     rng = np.random.default_rng(0)
@@ -665,8 +665,8 @@ def learned_section(n_points=20000, force_config=None):
 
 def cpu_baseline(m, sample=4096):
     from oracle import kriging, segmentation
-    from tests._models import oracle_series_list
-    (s,) = oracle_series_list(m)
+    from oracle.inputs import series_from_engine_inputs
+    (s,) = series_from_engine_inputs(m.interpolation_input, m.options, m.data_descriptor)
     grid = m.interpolation_input.grid.dense_grid
     n_total = grid.n_points
     rng = np.random.default_rng(0)

@@ -15,7 +15,12 @@ Unknown ordering of one series (n_o orientations, n_k surfaces, n_p points):
   point is the reference point and every other point ("rest") gives one row;
   n_i = n_p - n_k;
 * drift unknowns: uni_degree 1 -> (x, y, z); uni_degree 2 -> additionally
-  (x^2, y^2, z^2, xy, xz, yz); uni_degree 0 -> none.
+  (x^2, y^2, z^2, xy, xz, yz); uni_degree 0 -> none;
+* fault-drift unknowns: one per older FAULT series that offsets this one
+  (``fault_relations[j, i]``, ``gempy/core/data/structural_frame.py:244-273``).
+  Its drift function F_f is that fault series' block -- its sigmoid-segmented
+  values -- so the column holds gi_res (F_f(rest_i) - F_f(ref_i)) on the
+  interface rows and 0 on the gradient rows (a block is piecewise constant).
 
 Matrix entries (c_o = sill, C = unit covariance, h = x_a - x_b, r = |h|):
 
@@ -26,13 +31,15 @@ Matrix entries (c_o = sill, C = unit covariance, h = x_a - x_b, r = |h|):
 * II[i,j]         = c_o [i_res (C(rest_i,rest_j) - C(rest_i,ref_j)
                                 - C(ref_i,rest_j) + C(ref_i,ref_j)) + delta nugget[rest_i]]
 * UG[(u,o), d]    = d f_d / d x_u at x_o;  UI[i, d] = gi_res (f_d(rest_i) - f_d(ref_i))
+* FI[i, f]        = gi_res (F_f(rest_i) - F_f(ref_i));  FG = 0
 * rhs: b[(u,o)] = G[o, u]; zero elsewhere.
 
 With the defaults i_res = gi_res^2 (4 and 2) the interface rows are a symmetric
 diagonal rescaling of the textbook system.
 
 Field at x:  Z(x) = gi_res * ( sum_(u,o) w c_o C'/r(x_o,x) (x_o - x)_u
-                   + sum_i gi_res w_i c_o [C(x,rest_i) - C(x,ref_i)] + sum_d mu_d f_d(x) )
+                   + sum_i gi_res w_i c_o [C(x,rest_i) - C(x,ref_i)] + sum_d mu_d f_d(x)
+                   + sum_f nu_f F_f(x) )
 
 Distances.  Every distance is r = sqrt(|h|^2 + DIST_EPS2), DIST_EPS2 = 1e-10
 (transformed frame).  The reference runs its kernel under PyTorch autodiff
@@ -84,6 +91,7 @@ class Series:
     kernel: str = "cubic"
     i_res: float = 4.0
     gi_res: float = 2.0
+    fault_sp: np.ndarray = None          # (n_p, n_f) fault-block values at the points
     ref_rest: tuple = field(default=None, repr=False)
 
     @property
@@ -107,8 +115,12 @@ class Series:
         return self.n_p - self.n_k
 
     @property
+    def n_f(self):
+        return 0 if self.fault_sp is None else int(np.shape(self.fault_sp)[1])
+
+    @property
     def size(self):
-        return 3 * self.n_o + self.n_i + self.n_d
+        return 3 * self.n_o + self.n_i + self.n_d + self.n_f
 
     def ref_rest_index(self):
         """(ref_idx, rest_idx) arrays of length n_i; ref = first point of its surface."""
@@ -165,9 +177,9 @@ def build_system(s: Series):
     """Dense K (N x N) and rhs b (N,) in FP64."""
     C, dC_r, d2C, _ = functions(kernel_id(s.kernel))
     a, c_o = float(s.range), float(s.c_o)
-    n_o, n_i, n_d = s.n_o, s.n_i, s.n_d
+    n_o, n_i, n_d, n_f = s.n_o, s.n_i, s.n_d, s.n_f
     ng = 3 * n_o
-    N = ng + n_i + n_d
+    N = ng + n_i + n_d + n_f
     K = np.zeros((N, N))
     ref_idx, rest_idx = s.ref_rest_index()
     ref = s.sp_coords[ref_idx]
@@ -205,12 +217,19 @@ def build_system(s: Series):
     if n_d:
         UG = drift_gradients(xo, s.uni_degree)          # (n_o, 3, n_d)
         UG = UG.transpose(1, 0, 2).reshape(ng, n_d)
-        K[:ng, ng + n_i:] = UG
-        K[ng + n_i:, :ng] = UG.T
+        K[:ng, ng + n_i:ng + n_i + n_d] = UG
+        K[ng + n_i:ng + n_i + n_d, :ng] = UG.T
         if n_i:
             UI = (drift_values(rest, s.uni_degree) - drift_values(ref, s.uni_degree)) * s.gi_res
-            K[ng:ng + n_i, ng + n_i:] = UI
-            K[ng + n_i:, ng:ng + n_i] = UI.T
+            K[ng:ng + n_i, ng + n_i:ng + n_i + n_d] = UI
+            K[ng + n_i:ng + n_i + n_d, ng:ng + n_i] = UI.T
+
+    # fault drift
+    if n_f and n_i:
+        F = np.asarray(s.fault_sp, dtype=np.float64)
+        FI = (F[rest_idx] - F[ref_idx]) * s.gi_res
+        K[ng:ng + n_i, ng + n_i + n_d:] = FI
+        K[ng + n_i + n_d:, ng:ng + n_i] = FI.T
 
     b = np.zeros(N)
     b[:ng] = s.dip_gradients.T.reshape(-1)
@@ -236,16 +255,23 @@ def point_coefficients(s: Series, w):
     return alpha
 
 
-def evaluate(s: Series, w, x, gradient=False, chunk=200_000):
+def evaluate(s: Series, w, x, gradient=False, chunk=200_000, fault_x=None):
     """Scalar field (and gradient) at points x (n, 3); chunked like the
-    reference's ``evaluation_chunk_size``."""
+    reference's ``evaluation_chunk_size``.  ``fault_x`` (n, n_f) holds the
+    offsetting faults' block values at x (required when the series has fault
+    drift); the block is piecewise constant, so it adds nothing to the gradient."""
     C, dC_r, _, d3C_r = functions(kernel_id(s.kernel))
     a, c_o = float(s.range), float(s.c_o)
     x = np.atleast_2d(np.asarray(x, dtype=np.float64))
     n = x.shape[0]
     ng = 3 * s.n_o
     wg = w[:ng].reshape(3, s.n_o).T                   # (n_o, 3)
-    mu = w[ng + s.n_i:]
+    mu = w[ng + s.n_i:ng + s.n_i + s.n_d]
+    nu = w[ng + s.n_i + s.n_d:]
+    if s.n_f:
+        if fault_x is None:
+            raise ValueError("the series has fault drift: fault block values at x are required")
+        fault_x = np.asarray(fault_x, dtype=np.float64).reshape(n, s.n_f)
     alpha = point_coefficients(s, w)
     Z = np.empty(n)
     G = np.empty((n, 3)) if gradient else None
@@ -260,6 +286,8 @@ def evaluate(s: Series, w, x, gradient=False, chunk=200_000):
         z += c_o * (C(rp, a) * alpha[None, :]).sum(1)
         if len(mu):
             z += drift_values(xc, s.uni_degree) @ mu
+        if s.n_f:
+            z += fault_x[c0:c0 + chunk] @ nu
         Z[c0:c0 + chunk] = s.gi_res * z
         if gradient:
             k3 = d3C_r(r, a)
@@ -271,7 +299,13 @@ def evaluate(s: Series, w, x, gradient=False, chunk=200_000):
     return (Z, G) if gradient else Z
 
 
+def reference_starts(s: Series):
+    return np.concatenate([[0], np.cumsum(s.points_per_surface)[:-1]]).astype(np.int64)
+
+
 def isovalues(s: Series, w):
-    """Scalar field at each surface's reference (first) point."""
-    starts = np.concatenate([[0], np.cumsum(s.points_per_surface)[:-1]]).astype(np.int64)
-    return evaluate(s, w, s.sp_coords[starts])
+    """Scalar field at each surface's reference (first) point
+    (``scalar_field_at_surface_points``, ``gempy/core/data/geo_model.py:107-108``)."""
+    starts = reference_starts(s)
+    fx = None if s.fault_sp is None else np.asarray(s.fault_sp)[starts]
+    return evaluate(s, w, s.sp_coords[starts], fault_x=fx)

@@ -13,15 +13,27 @@ and ids = rint(v).  Element ids are ``1..n`` in stack order with the basement
 last (``gempy/core/data/structural_frame.py:368-370``); the top surface maps to
 id 1 (pinned by ``test/test_modules/test_grids/test_custom_grid.py:44-47``).
 
+Block ids.  ids are the hard classification the soft values approach: a
+point takes the unit of the highest surface it lies below,
+    id(Z) = u_1 + sum_k (u_(k+1) - u_k) [Z < z_(k) - TIE_TOL],
+which equals rint(v) except within TIE_TOL of an isovalue.  A point that lies
+exactly on a surface -- an octree corner that coincides with a surface's
+reference point, where Z == z_k up to rounding -- belongs to the unit above
+it.  The reference's own result is set by its rounding at such ties; the
+combination model (``test_example_models_I.py:71-88``, corner (0, 0, 250) m,
+rock1's reference point) shows the unit above.
+
 Series masks (``structural_frame.py:326-330``: the last group is forced to
 BASEMENT): an ERODE series owns the points above its lowest isovalue; an ONLAP
 series owns the points above the highest isovalue of the next (older) series;
-BASEMENT owns everything; a younger series' points are removed from all older
-ones.  FAULT series are not part of this path.
+BASEMENT owns everything; a FAULT series owns no lithology (its block offsets
+the younger series through their fault drift); a younger series' points are
+removed from all older ones.
 """
 import numpy as np
 
 ERODE, ONLAP, FAULT, BASEMENT = 1, 2, 3, 4
+TIE_TOL = 1e-9     # field distance below which a point counts as on a surface
 
 
 def sigmoid(t):
@@ -54,14 +66,16 @@ def segment(Z, iso, unit_values, slope):
     return v, np.rint(v)
 
 
-def hard_ids(Z, iso, unit_values):
-    """Step-function ids (the slope -> infinity limit)."""
+def hard_ids(Z, iso, unit_values, tol=None):
+    """Block ids: the slope -> infinity limit of the soft values, a point on
+    a surface (within ``tol``, default TIE_TOL) taking the unit above it."""
+    tol = TIE_TOL if tol is None else tol
     iso = np.asarray(iso, dtype=np.float64)
     u = np.asarray(unit_values, dtype=np.float64)
     zs = iso[order_surfaces(iso)]
     v = np.full(np.shape(Z), u[0])
     for k in range(len(zs)):
-        v += (u[k + 1] - u[k]) * (Z < zs[k])
+        v += (u[k + 1] - u[k]) * (np.asarray(Z) < zs[k] - tol)
     return v
 
 
@@ -77,8 +91,10 @@ def series_masks(fields, isos, relations):
             raw.append(fields[s] >= np.min(isos[s]))
         elif rel == ONLAP:
             raw.append(fields[s + 1] >= np.max(isos[s + 1]))
+        elif rel == FAULT:
+            raw.append(np.zeros(np.shape(fields[s]), dtype=bool))
         else:
-            raise ValueError(f"relation {rel} is not part of this path")
+            raise ValueError(f"unknown relation {rel}")
     taken = np.zeros(np.shape(fields[0]), dtype=bool)
     out = []
     for s in range(n_s):
