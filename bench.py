@@ -268,9 +268,10 @@ def main():
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        fld, _, vals, _ = K.evaluate(ds, model, pts, K.GK_FF if mixed else K.GK_F64, seg=seg, out=out_buf)
+        fld, _, vals, bid = K.evaluate(ds, model, pts, K.GK_FF if mixed else K.GK_F64, seg=seg, out=out_buf,
+                                       want_ids=True)
         e1.record(stream)
-        cv, ci, _ = K.combine(fld[None], vals[None], [4], [iso.min()], [iso.max()], want_masks=False)
+        cv, ci, _ = K.combine(fld[None], vals[None], bid[None], [4], [iso.min()], [iso.max()], want_masks=False)
         if record is not None:
             record.append((e0, e1))
         return w, info, iso, fld, ci

@@ -17,6 +17,8 @@ STATUS_NAMES = {0: "OK", 1: "ERR_ARG", 2: "ERR_SIZE", 3: "ERR_CUDA", 4: "ERR_SIN
 GK_F64, GK_F32, GK_FF = 0, 1, 2
 GK_KERNEL_CUBIC, GK_KERNEL_EXPONENTIAL = 0, 1
 GK_MAX_SURFACES = 32
+GK_MAX_FAULTS = 16
+GK_TIE_TOL = 1e-9
 GK_NOALLOC_MAX_N = 1024
 GK_TUNE_EVAL_FF, GK_TUNE_EVAL_F32, GK_TUNE_BATCH_EVAL = 0, 1, 2
 TUNABLES = {"eval_ff": GK_TUNE_EVAL_FF, "eval_f32": GK_TUNE_EVAL_F32, "batch_eval": GK_TUNE_BATCH_EVAL}
@@ -32,19 +34,19 @@ class GkInfo(ctypes.Structure):
 
 class GkSystem(ctypes.Structure):
     _fields_ = [("n_ori", ctypes.c_int32), ("n_sp", ctypes.c_int32), ("n_iface", ctypes.c_int32),
-                ("uni_degree", ctypes.c_int32), ("kernel", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("uni_degree", ctypes.c_int32), ("kernel", ctypes.c_int32), ("n_fault", ctypes.c_int32),
                 ("range", ctypes.c_double), ("c_o", ctypes.c_double), ("i_res", ctypes.c_double),
                 ("gi_res", ctypes.c_double),
                 ("dip_positions", ctypes.c_void_p), ("dip_gradients", ctypes.c_void_p),
                 ("nugget_grad", ctypes.c_void_p), ("sp_coords", ctypes.c_void_p),
                 ("nugget_sp", ctypes.c_void_p), ("ref_index", ctypes.c_void_p),
-                ("rest_index", ctypes.c_void_p)]
+                ("rest_index", ctypes.c_void_p), ("fault_sp", ctypes.c_void_p)]
 
 
 class GkPoints(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int32), ("dims", ctypes.c_int32 * 3), ("n", ctypes.c_int64),
                 ("origin", ctypes.c_double * 3), ("spacing", ctypes.c_double * 3),
-                ("xyz", ctypes.c_void_p)]
+                ("xyz", ctypes.c_void_p), ("fault_values", ctypes.c_void_p), ("fault_ld", ctypes.c_int64)]
 
 
 class GkSegment(ctypes.Structure):
@@ -123,14 +125,14 @@ SIGNATURES = [
                                ctypes.c_int, ctypes.POINTER(GkSegment), ctypes.c_void_p, ctypes.c_void_p,
                                ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     ("gk_combine_series", ctypes.c_int, [ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
-                                         c_int32_p, c_double_p, c_double_p, ctypes.c_void_p,
+                                         ctypes.c_void_p, c_int32_p, c_double_p, c_double_p, ctypes.c_void_p,
                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     ("gk_octree_corners", ctypes.c_int, [ctypes.c_int64, ctypes.c_void_p, c_double_p, ctypes.c_void_p,
                                          ctypes.c_void_p]),
     ("gk_octree_workspace_bytes", ctypes.c_size_t, [ctypes.c_int64]),
     ("gk_octree_refine", ctypes.c_int, [ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
-                                        c_double_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
-                                        ctypes.c_size_t, ctypes.c_void_p]),
+                                        ctypes.c_int32, c_double_p, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     ("gk_batch_workspace_bytes", ctypes.c_size_t, [ctypes.POINTER(GkBatch)]),
     ("gk_batch_points", ctypes.c_int64, [ctypes.POINTER(GkBatch)]),
     ("gk_batch_plan", ctypes.c_int, [ctypes.POINTER(GkBatch), ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),

@@ -104,6 +104,7 @@ __global__ void __launch_bounds__(256) batch_build_kernel(const BatchDesc* __res
         P.kernel = d.kernel; P.N = d.N; P.range = d.range; P.c_o = d.c_o; P.i_res = d.i_res; P.gi_res = d.gi_res;
         P.dip_positions = d.dip; P.dip_gradients = d.grad; P.nugget_grad = d.nug_g; P.sp_coords = d.sp;
         P.nugget_sp = d.nug_sp; P.ref_index = d.ref; P.rest_index = d.rest;
+        P.n_fault = 0; P.fault_sp = nullptr; P.n_sp = d.n_sp;
         const int64_t t = item - tile_prefix[sys];
         const int64_t r0 = (t / d.tile_side) * 32, c0 = (t % d.tile_side) * 32;
         if (tid < 32) {
@@ -641,15 +642,17 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchDesc* __rest
                      mu[8] * Y0 * Z0;
             const int64_t o = d.out_off + pid[p];
             if (field) field[o] = z;
-            double v = d.unit_values[0];
+            double v = d.unit_values[0], vid = d.unit_values[0];
             for (int k2 = 0; k2 < d.n_surf; ++k2) {
                 const double targ = d.slope * (d.iso[k2] - z);
                 const float tf = (float)targ;
                 const float sg = tf >= 0.f ? 1.f / (1.f + expf(-tf)) : expf(tf) / (1.f + expf(tf));
                 v += (d.unit_values[k2 + 1] - d.unit_values[k2]) * (double)sg;
+                // block id: a point on a surface takes the unit above it
+                if (z < d.iso[k2] - GK_TIE_TOL) vid += d.unit_values[k2 + 1] - d.unit_values[k2];
             }
             if (values) values[o] = v;
-            if (ids) ids[o] = (int32_t)rint(v);
+            if (ids) ids[o] = (int32_t)rint(vid);
         }
         }  // pass
     }

@@ -1,10 +1,12 @@
-// Kriging-matrix build: K = [[C_GG, C_GI, U_G], [C_IG, C_II, U_I], [U_G^T, U_I^T, 0]]
-// and the right-hand side, for one series, in FP64 or FP32.
+// Kriging-matrix build: K = [[C_GG, C_GI, U_G, 0], [C_IG, C_II, U_I, F_I],
+// [U_G^T, U_I^T, 0, 0], [0, F_I^T, 0, 0]] and the right-hand side, for one
+// series, in FP64 or FP32 (F_I: the fault-block drift of the faults that offset
+// the series).
 //
 // Row/column ordering (shared with the Python host code and the oracle):
 //   gradient unknowns component-major (u * n_ori + o), interface rows in the
 //   order of ref_index/rest_index, then the drift functions
-//   (x, y, z [, x^2, y^2, z^2, xy, xz, yz]).
+//   (x, y, z [, x^2, y^2, z^2, xy, xz, yz]), then the fault drifts.
 // Entry formulas restate the published co-kriging (GemPy 1.0, GMD 2019); the
 // placement of i_res / gi_res, the nuggets inside the c_o factor and the 1e-5
 // regulariser follow the conventions fitted to the reference's anticline
@@ -54,7 +56,7 @@ using namespace gk;
 
 extern "C" int64_t gk_system_size(const gk_system* s) {
     if (s == nullptr) return -1;
-    return 3 * (int64_t)s->n_ori + s->n_iface + drift_count(s->uni_degree);
+    return 3 * (int64_t)s->n_ori + s->n_iface + drift_count(s->uni_degree) + s->n_fault;
 }
 
 static gk_status check_system(const gk_system* s) {
@@ -65,6 +67,9 @@ static gk_status check_system(const gk_system* s) {
     if (!(s->range > 0.0)) return GK_ERR_ARG;
     if (s->n_ori > 0 && (!s->dip_positions || !s->dip_gradients || !s->nugget_grad)) return GK_ERR_ARG;
     if (s->n_iface > 0 && (!s->sp_coords || !s->nugget_sp || !s->ref_index || !s->rest_index)) return GK_ERR_ARG;
+    if (s->n_fault < 0) return GK_ERR_ARG;
+    if (s->n_fault > GK_MAX_FAULTS) return GK_ERR_SIZE;
+    if (s->n_fault > 0 && s->n_iface > 0 && !s->fault_sp) return GK_ERR_ARG;
     if (gk_system_size(s) <= 0) return GK_ERR_SIZE;
     return GK_OK;
 }
@@ -83,6 +88,7 @@ extern "C" gk_status gk_build(const gk_system* s, gk_prec prec, void* K, int64_t
     P.range = s->range; P.c_o = s->c_o; P.i_res = s->i_res; P.gi_res = s->gi_res;
     P.dip_positions = s->dip_positions; P.dip_gradients = s->dip_gradients; P.nugget_grad = s->nugget_grad;
     P.sp_coords = s->sp_coords; P.nugget_sp = s->nugget_sp; P.ref_index = s->ref_index; P.rest_index = s->rest_index;
+    P.n_fault = s->n_fault; P.fault_sp = s->fault_sp; P.n_sp = s->n_sp;
     dim3 block(32, 8), grid((unsigned)((N + 31) / 32), (unsigned)((N + 31) / 32));
     cudaStream_t st_ = (cudaStream_t)stream;
     if (prec == GK_F64)

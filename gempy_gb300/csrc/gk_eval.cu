@@ -22,6 +22,12 @@ namespace gk {
 
 static size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// Drift weights of the packed model (times gi_res): slots 0..8 the polynomial
+// drift, slots kFaultSlot.. the fault drifts.
+constexpr int kFaultSlot = 9;
+constexpr int kMuSlots = 32;
+static_assert(kFaultSlot + GK_MAX_FAULTS <= kMuSlots, "drift slots");
+
 struct ModelLayout {
     size_t ori64, sp64, mu64, ori32, sp32, alpha, ffori, ffsp, ffmeta, total;
 };
@@ -31,7 +37,7 @@ static ModelLayout model_layout(int n_ori, int n_sp) {
     size_t o = 0;
     L.ori64 = o; o += al256((size_t)n_ori * 8 * sizeof(double));
     L.sp64 = o;  o += al256((size_t)n_sp * 4 * sizeof(double));
-    L.mu64 = o;  o += al256(16 * sizeof(double));
+    L.mu64 = o;  o += al256(kMuSlots * sizeof(double));
     L.ori32 = o; o += al256((size_t)n_ori * 8 * sizeof(float));
     L.sp32 = o;  o += al256((size_t)n_sp * 4 * sizeof(float));
     L.alpha = o; o += al256((size_t)n_sp * sizeof(double));
@@ -61,7 +67,7 @@ __global__ void alpha_ref_kernel(const int32_t* __restrict__ ref, int n_iface, c
     atomicAdd(alpha + ref[t], -gi * s);
 }
 
-__global__ void pack_kernel(int n_ori, int n_sp, int n_iface, int n_drift, double scale, double gi,
+__global__ void pack_kernel(int n_ori, int n_sp, int n_iface, int n_drift, int n_fault, double scale, double gi,
                             const double* __restrict__ dip, const double* __restrict__ sp,
                             const double* __restrict__ w, const double* __restrict__ alpha, double* ori64,
                             double* sp64, double* mu64, float* ori32, float* sp32) {
@@ -75,7 +81,13 @@ __global__ void pack_kernel(int n_ori, int n_sp, int n_iface, int n_drift, doubl
         double rec[4] = {sp[3 * i], sp[3 * i + 1], sp[3 * i + 2], scale * alpha[i]};
         for (int k = 0; k < 4; ++k) { sp64[4 * i + k] = rec[k]; sp32[4 * i + k] = (float)rec[k]; }
     }
-    if (i < 16) mu64[i] = i < n_drift ? gi * w[3 * n_ori + n_iface + i] : 0.0;
+    if (i < kMuSlots) {
+        const int64_t d0 = 3 * (int64_t)n_ori + n_iface;
+        double m = 0.0;
+        if (i < n_drift) m = gi * w[d0 + i];
+        else if (i >= kFaultSlot && i < kFaultSlot + n_fault) m = gi * w[d0 + n_drift + (i - kFaultSlot)];
+        mu64[i] = m;
+    }
 }
 
 // Float-float records.  Coordinates are scaled by 1/range (so s = |x-p|/a
@@ -163,8 +175,10 @@ struct EvalParams {
     int64_t n;
     double origin[3], spacing[3];
     const double* xyz;
-    int n_ori, n_sp, n_drift, degree, kernel;
+    int n_ori, n_sp, n_drift, degree, kernel, n_fault;
     double range;
+    const double* fault_values;  // n_fault x fault_ld
+    int64_t fault_ld;
     const void* ori;   // packed records in T
     const void* sp;
     const double* mu;
@@ -194,6 +208,22 @@ template <> __device__ __forceinline__ float sigm<float>(double t) {
     if (tf >= 0.f) return 1.f / (1.f + expf(-tf));
     float e = expf(tf);
     return e / (1.f + e);
+}
+
+// Fault-drift contribution at point i: sum_f nu_f F_f(x_i).
+__device__ __forceinline__ double fault_term(const EvalParams& P, int64_t i) {
+    double z = 0.0;
+    for (int f = 0; f < P.n_fault; ++f) z += P.mu[kFaultSlot + f] * P.fault_values[f * P.fault_ld + i];
+    return z;
+}
+
+// Block id: u_0 + sum_k (u_(k+1) - u_k) [z < z_k - GK_TIE_TOL] (a point on a
+// surface takes the unit above it).
+__device__ __forceinline__ int32_t block_id(const gk_segment& S, double z) {
+    double v = S.unit_values[0];
+    for (int k = 0; k < S.n_surf; ++k)
+        if (z < S.isovalues[k] - GK_TIE_TOL) v += S.unit_values[k + 1] - S.unit_values[k];
+    return (int32_t)rint(v);
 }
 
 template <typename T, int PPT, bool GRAD>
@@ -345,6 +375,7 @@ __global__ void __launch_bounds__(256) eval_kernel(const EvalParams P) {
             if (P.n_drift >= 3) z += mu[0] * X + mu[1] * Y + mu[2] * Zc;
             if (P.n_drift >= 9)
                 z += mu[3] * X * X + mu[4] * Y * Y + mu[5] * Zc * Zc + mu[6] * X * Y + mu[7] * X * Zc + mu[8] * Y * Zc;
+            if (P.n_fault) z += fault_term(P, pid[p]);
             if (P.field) P.field[pid[p]] = z;
             if (GRAD && P.grad) {
                 double gx = G[p][0], gy = G[p][1], gz = G[p][2];
@@ -364,7 +395,7 @@ __global__ void __launch_bounds__(256) eval_kernel(const EvalParams P) {
                     v += (P.seg.unit_values[k + 1] - P.seg.unit_values[k]) *
                          (double)sigm<T>(P.seg.slope * (P.seg.isovalues[k] - z));
                 if (P.values) P.values[pid[p]] = v;
-                if (P.ids) P.ids[pid[p]] = (int32_t)rint(v);
+                if (P.ids) P.ids[pid[p]] = block_id(P.seg, z);
             }
         }
     }
@@ -533,6 +564,7 @@ __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const 
             if (P.n_drift >= 9)
                 z += mu[3] * Xx * Xx + mu[4] * Yy * Yy + mu[5] * Zc * Zc + mu[6] * Xx * Yy + mu[7] * Xx * Zc +
                      mu[8] * Yy * Zc;
+            if (P.n_fault) z += fault_term(P, pidp);
             if (P.field) P.field[pidp] = z;
             if (P.has_seg) {
                 double v = P.seg.unit_values[0];
@@ -540,7 +572,7 @@ __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const 
                     v += (P.seg.unit_values[k + 1] - P.seg.unit_values[k]) *
                          (double)sigm<float>(P.seg.slope * (P.seg.isovalues[k] - z));
                 if (P.values) P.values[pidp] = v;
-                if (P.ids) P.ids[pidp] = (int32_t)rint(v);
+                if (P.ids) P.ids[pidp] = block_id(P.seg, z);
             }
         }
     }
@@ -560,6 +592,7 @@ struct CombineParams {
     int64_t n;
     const double* fields;
     const double* values;
+    const int32_t* ids;
     int relations[GK_MAX_SURFACES];
     double min_iso[GK_MAX_SURFACES];
     double max_iso[GK_MAX_SURFACES];
@@ -573,19 +606,24 @@ __global__ void combine_kernel(const CombineParams P) {
     if (i >= P.n) return;
     bool taken = false;
     double v = 0.0;
+    int32_t id = 0;
     for (int s = 0; s < P.n_series; ++s) {
         bool raw;
         const int rel = P.relations[s];
         if (rel == 4 || s == P.n_series - 1) raw = true;                              // BASEMENT / last
         else if (rel == 1) raw = P.fields[(int64_t)s * P.n + i] >= P.min_iso[s];      // ERODE
-        else raw = P.fields[(int64_t)(s + 1) * P.n + i] >= P.max_iso[s + 1];          // ONLAP
+        else if (rel == 2) raw = P.fields[(int64_t)(s + 1) * P.n + i] >= P.max_iso[s + 1];  // ONLAP
+        else raw = false;                                                             // FAULT: no lithology
         bool m = raw && !taken;
         taken = taken || m;
-        if (m) v += P.values[(int64_t)s * P.n + i];
+        if (m) {
+            v += P.values[(int64_t)s * P.n + i];
+            id += P.ids[(int64_t)s * P.n + i];
+        }
         if (P.masks) P.masks[(int64_t)s * P.n + i] = m ? 1 : 0;
     }
     if (P.out_values) P.out_values[i] = v;
-    if (P.out_ids) P.out_ids[i] = (int32_t)rint(v);
+    if (P.out_ids) P.out_ids[i] = id;
 }
 
 }  // namespace gk
@@ -619,8 +657,9 @@ extern "C" gk_status gk_eval_prepare(const gk_system* s, const double* w, void* 
     }
     int nmax = s->n_ori > s->n_sp ? s->n_ori : s->n_sp;
     if (nmax < 16) nmax = 16;
+    if (nmax < kMuSlots) nmax = kMuSlots;
     pack_kernel<<<(unsigned)((nmax + 255) / 256), 256, 0, cs>>>(
-        s->n_ori, s->n_sp, s->n_iface, n_drift, s->c_o * s->gi_res, s->gi_res, s->dip_positions, s->sp_coords, w,
+        s->n_ori, s->n_sp, s->n_iface, n_drift, s->n_fault, s->c_o * s->gi_res, s->gi_res, s->dip_positions, s->sp_coords, w,
         alpha, (double*)(m + L.ori64), (double*)(m + L.sp64), (double*)(m + L.mu64), (float*)(m + L.ori32),
         (float*)(m + L.sp32));
     GK_LAUNCH_CHECK();
@@ -715,6 +754,7 @@ extern "C" gk_status gk_eval(const gk_system* s, const void* model, const gk_poi
     if (seg != nullptr && (seg->n_surf < 0 || seg->n_surf > GK_MAX_SURFACES)) return GK_ERR_SIZE;
     if ((values || ids) && seg == nullptr) return GK_ERR_ARG;
     if (s->n_ori + s->n_sp == 0) return GK_ERR_ARG;
+    if (s->n_fault > 0 && (pts->fault_values == nullptr || pts->fault_ld < pts->n)) return GK_ERR_ARG;
     ModelLayout L = model_layout(s->n_ori, s->n_sp);
     const char* m = (const char*)model;
     EvalParams P;
@@ -733,6 +773,9 @@ extern "C" gk_status gk_eval(const gk_system* s, const void* model, const gk_poi
     P.degree = s->uni_degree;
     P.kernel = s->kernel;
     P.range = s->range;
+    P.n_fault = s->n_fault;
+    P.fault_values = pts->fault_values;
+    P.fault_ld = pts->fault_ld;
     P.mu = (const double*)(m + L.mu64);
     P.has_seg = seg != nullptr;
     if (seg) P.seg = *seg;
@@ -767,10 +810,12 @@ extern "C" gk_status gk_eval(const gk_system* s, const void* model, const gk_poi
 }
 
 extern "C" gk_status gk_combine_series(int32_t n_series, int64_t n, const double* fields, const double* values,
-                                       const int32_t* relations, const double* min_iso, const double* max_iso,
-                                       double* out_values, int32_t* out_ids, uint8_t* masks, gk_stream stream) {
+                                       const int32_t* ids, const int32_t* relations, const double* min_iso,
+                                       const double* max_iso, double* out_values, int32_t* out_ids, uint8_t* masks,
+                                       gk_stream stream) {
     if (n_series < 1 || n_series > GK_MAX_SURFACES || n < 0) return GK_ERR_ARG;
-    if (fields == nullptr || values == nullptr || relations == nullptr || min_iso == nullptr || max_iso == nullptr)
+    if (fields == nullptr || values == nullptr || ids == nullptr || relations == nullptr || min_iso == nullptr ||
+        max_iso == nullptr)
         return GK_ERR_ARG;
     if (n == 0) return GK_OK;
     CombineParams P;
@@ -779,8 +824,10 @@ extern "C" gk_status gk_combine_series(int32_t n_series, int64_t n, const double
     P.n = n;
     P.fields = fields;
     P.values = values;
+    P.ids = ids;
     for (int s = 0; s < n_series; ++s) {
-        if (relations[s] != 1 && relations[s] != 2 && relations[s] != 4) return GK_ERR_ARG;
+        if (relations[s] < 1 || relations[s] > 4) return GK_ERR_ARG;
+        if (relations[s] == 2 && s == n_series - 1) return GK_ERR_ARG;  // ONLAP needs an older series
         P.relations[s] = relations[s];
         P.min_iso[s] = min_iso[s];
         P.max_iso[s] = max_iso[s];

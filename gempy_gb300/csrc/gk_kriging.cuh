@@ -4,7 +4,10 @@
 // Row/column ordering (shared with the Python host code and the oracle):
 //   gradient unknowns component-major (u * n_ori + o), interface rows in the
 //   order of ref_index/rest_index, then the drift functions
-//   (x, y, z [, x^2, y^2, z^2, xy, xz, yz]).
+//   (x, y, z [, x^2, y^2, z^2, xy, xz, yz]), then one fault-drift unknown per
+//   offsetting fault, whose function is that fault's block F_f (given at the
+//   surface points): gi_res (F_f(rest) - F_f(ref)) on the interface rows, 0 on
+//   the gradient rows (a block is piecewise constant) and in the drift block.
 // Entry formulas restate the published co-kriging (GemPy 1.0, GMD 2019); the
 // placement of i_res / gi_res, the nuggets inside the c_o factor and the 1e-5
 // regulariser follow the conventions fitted to the reference's anticline
@@ -16,16 +19,17 @@
 namespace gk {
 
 struct Item {          // one row/column of K, decoded
-    int type;          // 0 = gradient, 1 = interface, 2 = drift
-    int comp;          // gradient component u, or drift index d
+    int type;          // 0 = gradient, 1 = interface, 2 = drift, 3 = fault drift
+    int comp;          // gradient component u, drift index d, or fault f
     int idx;           // orientation o, interface row t
+    int rest, ref;     // surface-point indices (interface rows)
     double p[3];       // orientation position, or rest point
     double q[3];       // reference point (interface rows)
     double nug;        // diagonal nugget (already times c_o)
 };
 
 struct BuildParams {
-    int n_ori, n_iface, n_drift, degree, kernel;
+    int n_ori, n_iface, n_drift, degree, kernel, n_fault;
     int64_t N;
     double range, c_o, i_res, gi_res;
     const double* dip_positions;
@@ -35,11 +39,14 @@ struct BuildParams {
     const double* nugget_sp;
     const int32_t* ref_index;
     const int32_t* rest_index;
+    const double* fault_sp;   // n_fault x n_sp
+    int n_sp;
 };
 
 __device__ inline void decode(const BuildParams& P, int64_t i, Item& it) {
     const int ng = 3 * P.n_ori;
     it.nug = 0.0;
+    it.rest = it.ref = 0;
     if (i < ng) {
         it.type = 0;
         it.comp = (int)(i / P.n_ori);
@@ -52,12 +59,19 @@ __device__ inline void decode(const BuildParams& P, int64_t i, Item& it) {
         it.idx = (int)(i - ng);
         it.comp = 0;
         int rest = P.rest_index[it.idx], ref = P.ref_index[it.idx];
+        it.rest = rest;
+        it.ref = ref;
         for (int k = 0; k < 3; ++k) it.p[k] = P.sp_coords[3 * rest + k];
         for (int k = 0; k < 3; ++k) it.q[k] = P.sp_coords[3 * ref + k];
         it.nug = P.c_o * P.nugget_sp[rest];
-    } else {
+    } else if (i < ng + P.n_iface + P.n_drift) {
         it.type = 2;
         it.comp = (int)(i - ng - P.n_iface);
+        it.idx = it.comp;
+        for (int k = 0; k < 3; ++k) { it.p[k] = 0.0; it.q[k] = 0.0; }
+    } else {
+        it.type = 3;
+        it.comp = (int)(i - ng - P.n_iface - P.n_drift);
         it.idx = it.comp;
         for (int k = 0; k < 3; ++k) { it.p[k] = 0.0; it.q[k] = 0.0; }
     }
@@ -134,6 +148,14 @@ __device__ T entry(const BuildParams& P, const Cov<T>& cv, const Item& A, const 
     if (A.type == 2 && B.type == 0) return drift_df<T>(A.comp, B.comp, bp);
     if (A.type == 1 && B.type == 2) return (T)P.gi_res * (drift_f<T>(B.comp, ap) - drift_f<T>(B.comp, aq));
     if (A.type == 2 && B.type == 1) return (T)P.gi_res * (drift_f<T>(A.comp, bp) - drift_f<T>(A.comp, bq));
+    if (A.type == 1 && B.type == 3) {
+        const double* F = P.fault_sp + (int64_t)B.comp * P.n_sp;
+        return (T)(P.gi_res * (F[A.rest] - F[A.ref]));
+    }
+    if (A.type == 3 && B.type == 1) {
+        const double* F = P.fault_sp + (int64_t)A.comp * P.n_sp;
+        return (T)(P.gi_res * (F[B.rest] - F[B.ref]));
+    }
     return (T)0;
 }
 

@@ -1,11 +1,12 @@
 // Octree refinement: voxel corners, marking and ordered compaction of the
 // children of marked voxels.  Replaces the engine's octree step over the
 // reference's octree grid (gempy/core/data/grid.py:128-151,
-// grid_modules/regular_grid.py:36-43).  A voxel is refined when the ids at
-// its 8 corners are not all equal; children are listed 8 per refined voxel
-// (x slowest, z fastest) in parent order, which matches the point order of
-// the reference's approved anticline scalar field
-// (test/test_model_types/test_example_models_I.py:19-23).
+// grid_modules/regular_grid.py:36-43).  A voxel is refined when its 8 corners
+// differ in any id set -- the lithology ids, then each fault series' block
+// ids; children are listed 8 per refined voxel (x slowest, z fastest) in
+// parent order, which matches the point order of the reference's approved
+// anticline and fault-model scalar fields
+// (test/test_model_types/test_example_models_I.py:19-23, 41-68).
 #include "gk_common.cuh"
 
 namespace gk {
@@ -31,25 +32,26 @@ __global__ void corners_kernel(int64_t n, const double* __restrict__ c, double h
 
 constexpr int kScanBlock = 256;
 
+// voxel v is marked when its 8 corners differ in any of the n_sets id arrays
+// (set s at ids + s * 8n)
+__device__ __forceinline__ int voxel_marked(const int32_t* __restrict__ ids, int n_sets, int64_t n, int64_t v) {
+    int m = 0;
+    for (int s = 0; s < n_sets && !m; ++s) {
+        const int32_t* c = ids + (int64_t)s * 8 * n + 8 * v;
+        const int32_t a = c[0];
+        for (int k = 1; k < 8; ++k) m |= (c[k] != a);
+    }
+    return m;
+}
+
 // per-block count of marked voxels
-__global__ void mark_count_kernel(int64_t n, const int32_t* __restrict__ ids, int refine_all,
+__global__ void mark_count_kernel(int64_t n, const int32_t* __restrict__ ids, int n_sets, int refine_all,
                                   int64_t* __restrict__ block_counts) {
-    __shared__ int cnt;
-    if (threadIdx.x == 0) cnt = 0;
-    __syncthreads();
     int64_t v = (int64_t)blockIdx.x * kScanBlock + threadIdx.x;
     int m = 0;
-    if (v < n) {
-        if (refine_all) m = 1;
-        else {
-            const int32_t* c = ids + 8 * v;
-            int32_t a = c[0];
-            for (int k = 1; k < 8; ++k) m |= (c[k] != a);
-        }
-    }
+    if (v < n) m = refine_all ? 1 : voxel_marked(ids, n_sets, n, v);
     int w = __syncthreads_count(m);
     if (threadIdx.x == 0) block_counts[blockIdx.x] = w;
-    (void)cnt;
 }
 
 // exclusive scan of block counts in one CTA (sequential over chunks of 1024)
@@ -78,19 +80,12 @@ __global__ void scan_blocks_kernel(int64_t nb, int64_t* __restrict__ counts, int
 }
 
 __global__ void scatter_children_kernel(int64_t n, const double* __restrict__ c, const int32_t* __restrict__ ids,
-                                        int refine_all, const int64_t* __restrict__ block_off, double qx, double qy,
-                                        double qz, double* __restrict__ out) {
+                                        int n_sets, int refine_all, const int64_t* __restrict__ block_off, double qx,
+                                        double qy, double qz, double* __restrict__ out) {
     __shared__ int pref[kScanBlock];
     int64_t v = (int64_t)blockIdx.x * kScanBlock + threadIdx.x;
     int m = 0;
-    if (v < n) {
-        if (refine_all) m = 1;
-        else {
-            const int32_t* cc = ids + 8 * v;
-            int32_t a = cc[0];
-            for (int k = 1; k < 8; ++k) m |= (cc[k] != a);
-        }
-    }
+    if (v < n) m = refine_all ? 1 : voxel_marked(ids, n_sets, n, v);
     pref[threadIdx.x] = m;
     __syncthreads();
     for (int off = 1; off < kScanBlock; off <<= 1) {
@@ -131,10 +126,12 @@ extern "C" size_t gk_octree_workspace_bytes(int64_t n) {
     return (size_t)(nb + 1) * sizeof(int64_t);
 }
 
-extern "C" gk_status gk_octree_refine(int64_t n, const double* centres, const int32_t* corner_ids, int32_t refine_all,
-                                      const double spacing[3], double* children, int64_t* count, void* work,
-                                      size_t work_bytes, gk_stream stream) {
+extern "C" gk_status gk_octree_refine(int64_t n, const double* centres, const int32_t* corner_ids,
+                                      int32_t n_id_sets, int32_t refine_all, const double spacing[3],
+                                      double* children, int64_t* count, void* work, size_t work_bytes,
+                                      gk_stream stream) {
     if (n < 0 || spacing == nullptr || count == nullptr) return GK_ERR_ARG;
+    if (!refine_all && (n_id_sets < 1 || n_id_sets > 1 + GK_MAX_SURFACES)) return GK_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     if (n == 0) {
         GK_CUDA_TRY(cudaMemsetAsync(count, 0, sizeof(int64_t), st));
@@ -145,11 +142,11 @@ extern "C" gk_status gk_octree_refine(int64_t n, const double* centres, const in
     int64_t nb = (n + kScanBlock - 1) / kScanBlock;
     if (nb > 0x7fffffff) return GK_ERR_SIZE;
     int64_t* bc = (int64_t*)work;
-    mark_count_kernel<<<(unsigned)nb, kScanBlock, 0, st>>>(n, corner_ids, refine_all, bc);
+    mark_count_kernel<<<(unsigned)nb, kScanBlock, 0, st>>>(n, corner_ids, n_id_sets, refine_all, bc);
     GK_LAUNCH_CHECK();
     scan_blocks_kernel<<<1, 1024, 0, st>>>(nb, bc, count);
     GK_LAUNCH_CHECK();
-    scatter_children_kernel<<<(unsigned)nb, kScanBlock, 0, st>>>(n, centres, corner_ids, refine_all, bc,
+    scatter_children_kernel<<<(unsigned)nb, kScanBlock, 0, st>>>(n, centres, corner_ids, n_id_sets, refine_all, bc,
                                                                    spacing[0] / 4, spacing[1] / 4, spacing[2] / 4,
                                                                    children);
     GK_LAUNCH_CHECK();

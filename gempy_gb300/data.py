@@ -70,6 +70,16 @@ class EvaluationOptions:
     def number_octree_levels(self, v):
         self._number_octree_levels = int(v)
 
+    @property
+    def number_octree_levels_surface(self):
+        """Levels below this one also evaluate their voxel corners (for the
+        mesh extraction), and export them after the centres."""
+        return self._number_octree_levels_surface
+
+    @number_octree_levels_surface.setter
+    def number_octree_levels_surface(self, v):
+        self._number_octree_levels_surface = int(v)
+
 
 @dataclass
 class InterpolationOptions:
@@ -208,20 +218,40 @@ class TensorsStructure:
 
 @dataclass
 class StacksStructure:
+    """Per-stack sizes and relations.  ``faults_relations[j, i]`` true: the
+    FAULT stack j offsets the younger stack i (``structural_frame.py:244-273``)."""
     number_of_points_per_stack: np.ndarray
     number_of_orientations_per_stack: np.ndarray
     number_of_surfaces_per_stack: np.ndarray
     masking_descriptor: List[StackRelationType]
+    faults_relations: Optional[np.ndarray] = None
 
     def __post_init__(self):
         self.number_of_points_per_stack = np.asarray(self.number_of_points_per_stack, dtype=np.int64)
         self.number_of_orientations_per_stack = np.asarray(self.number_of_orientations_per_stack, dtype=np.int64)
         self.number_of_surfaces_per_stack = np.asarray(self.number_of_surfaces_per_stack, dtype=np.int64)
         self.masking_descriptor = [StackRelationType(int(r)) for r in self.masking_descriptor]
+        n = len(self.number_of_points_per_stack)
+        if self.faults_relations is not None:
+            fr = np.asarray(self.faults_relations, dtype=bool)
+            if fr.shape != (n, n):
+                raise ValueError(f"faults_relations must be {n} x {n}")
+            for j, i in zip(*np.nonzero(fr)):
+                if j >= i:
+                    raise ValueError(f"stack {j} cannot offset the older or same stack {i}")
+                if self.masking_descriptor[j] != StackRelationType.FAULT:
+                    raise ValueError(f"stack {j} offsets stack {i} but is not a FAULT stack")
+            self.faults_relations = fr
 
     @property
     def n_stacks(self):
         return len(self.number_of_points_per_stack)
+
+    def fault_sources(self, i):
+        """The FAULT stacks that offset stack i, oldest first."""
+        if self.faults_relations is None:
+            return []
+        return [int(j) for j in np.nonzero(self.faults_relations[:, i])[0]]
 
 
 @dataclass
@@ -231,14 +261,55 @@ class InputDataDescriptor:
     stack_structure: StacksStructure
 
     @classmethod
-    def from_arrays(cls, points_per_surface, surfaces_per_stack, orientations_per_stack, relations):
+    def from_arrays(cls, points_per_surface, surfaces_per_stack, orientations_per_stack, relations,
+                    faults_relations=None):
         pps = np.asarray(points_per_surface, dtype=np.int64)
         sps = np.asarray(surfaces_per_stack, dtype=np.int64)
         bounds = np.concatenate([[0], np.cumsum(sps)])
         pts = np.array([pps[bounds[i]:bounds[i + 1]].sum() for i in range(len(sps))], dtype=np.int64)
         rel = list(relations)
         rel[-1] = StackRelationType.BASEMENT
-        return cls(TensorsStructure(pps), StacksStructure(pts, orientations_per_stack, sps, rel))
+        return cls(TensorsStructure(pps), StacksStructure(pts, orientations_per_stack, sps, rel, faults_relations))
+
+    @classmethod
+    def from_structural_frame(cls, structural_frame, making_descriptor=None, faults_relations=None,
+                              faults_input_data=None):
+        """The descriptor the reference builds from a ``StructuralFrame``
+        (``gempy/core/data/structural_frame.py:306-317``): one stack per
+        structural group, surfaces per group, surface points per element,
+        orientations per group, the groups' relations (the last one BASEMENT)
+        and the fault relations.  ``structural_frame`` needs the attributes the
+        reference's frame has: ``structural_groups``, each with ``elements``
+        (each with ``number_of_points`` and ``number_of_orientations``) and
+        ``structural_relation``.  ``faults_input_data`` (finite-fault
+        thickness/offset) is accepted and must be unset: this path models
+        infinite faults."""
+        if faults_input_data is not None and any(f is not None for f in faults_input_data):
+            raise NotImplementedError("finite faults (faults_input_data) are not part of this path")
+        groups = list(structural_frame.structural_groups)
+        pps, sps, ops, rels = [], [], [], []
+        for g in groups:
+            els = list(g.elements)
+            sps.append(len(els))
+            pps.extend(int(e.number_of_points) for e in els)
+            ops.append(int(sum(int(e.number_of_orientations) for e in els)))
+            rels.append(_relation(g.structural_relation))
+        if making_descriptor is not None:
+            rels = [_relation(r) for r in making_descriptor]
+        if faults_relations is None:
+            faults_relations = getattr(structural_frame, "fault_relations", None)
+        return cls.from_arrays(pps, sps, ops, rels, faults_relations)
+
+
+def _relation(r):
+    """StackRelationType from an enum of this module, the reference's own enum
+    (matched by name) or an int."""
+    if isinstance(r, StackRelationType):
+        return r
+    name = getattr(r, "name", None)
+    if name is not None and name in StackRelationType.__members__:
+        return StackRelationType[name]
+    return StackRelationType(int(r))
 
 
 # ----------------------------------------------------------------------------- outputs
@@ -280,10 +351,18 @@ class CombinedOutput:
 
 @dataclass
 class OctreeLevel:
+    """One octree level.  ``outputs`` holds one evaluation per series over
+    the level's grid: the voxel centres, followed by the 8 corners of every
+    voxel (corner order x slowest, z fastest) on levels below
+    ``number_octree_levels_surface``, where the corners are evaluated for the
+    mesh extraction.  ``last_output_center`` is the combined block at the
+    centres, ``last_output_corners`` at the corners (or None)."""
     grid_centers: np.ndarray
     dxdydz: np.ndarray
     outputs_centers: List[InterpOutput]
     last_output_center: CombinedOutput
+    last_output_corners: Optional[CombinedOutput] = None
+    grid_corners: Optional[np.ndarray] = None
 
     @property
     def outputs(self):

@@ -93,6 +93,31 @@ class DeviceSeries:
         s.nugget_sp = self.nugget_sp.data_ptr()
         s.ref_index = self.ref_index.data_ptr()
         s.rest_index = self.rest_index.data_ptr()
+        self.fault_sp = None
+        s.n_fault = 0
+        s.fault_sp = 0
+
+    def set_fault_blocks(self, fault_sp):
+        """Fault-drift functions of this series: the blocks of the faults that
+        offset it at its surface points, an (n_fault, n_sp) FP64 CUDA tensor
+        (row f: fault f's soft segmented values)."""
+        if fault_sp is None or len(fault_sp) == 0:
+            self.fault_sp = None
+            self.sys.n_fault = 0
+            self.sys.fault_sp = 0
+            return
+        f = fault_sp.to(device=self.device, dtype=torch.float64).contiguous()
+        if f.dim() != 2 or f.shape[1] != self.sys.n_sp:
+            raise ValueError("fault blocks must be (n_fault, n_sp)")
+        if f.shape[0] > _lib.GK_MAX_FAULTS:
+            raise ValueError(f"at most {_lib.GK_MAX_FAULTS} faults offset one series")
+        self.fault_sp = f
+        self.sys.n_fault = int(f.shape[0])
+        self.sys.fault_sp = f.data_ptr()
+
+    @property
+    def n_faults(self):
+        return int(self.sys.n_fault)
 
     @property
     def n_surfaces(self):
@@ -342,9 +367,21 @@ def make_segment(isovalues_sorted, unit_values, slope):
 
 
 def evaluate(series: DeviceSeries, model, pts: Points, prec=GK_F64, seg=None, gradient=False, want_field=True,
-             want_values=True, want_ids=False, out=None):
+             want_values=True, want_ids=False, out=None, fault_values=None):
+    """Field (gradient, soft values, block ids) of one series at ``pts``;
+    ``fault_values`` (n_fault, n) holds the blocks of the faults that offset
+    the series at these points (required when it has fault drift)."""
     lib = _lib.load()
     n = pts.n
+    if series.n_faults:
+        if fault_values is None or tuple(fault_values.shape) != (series.n_faults, n):
+            raise ValueError("this series has fault drift: pass its faults' blocks at the points, (n_fault, n)")
+        fault_values = fault_values.contiguous()
+        pts.gk.fault_values = fault_values.data_ptr()
+        pts.gk.fault_ld = n
+    else:
+        pts.gk.fault_values = 0
+        pts.gk.fault_ld = 0
     dev = series.device
     o = out or {}
     field = o.get("field") if want_field else None
@@ -365,7 +402,9 @@ def evaluate(series: DeviceSeries, model, pts: Points, prec=GK_F64, seg=None, gr
     return field, grad, values, ids
 
 
-def combine(fields, values, relations, min_iso, max_iso, want_masks=True):
+def combine(fields, values, ids, relations, min_iso, max_iso, want_masks=True):
+    """Lithology block of several series (rows of ``fields``, ``values`` and
+    block ``ids``) with the squeezed series masks."""
     lib = _lib.load()
     n_series, n = fields.shape
     dev = fields.device
@@ -375,8 +414,9 @@ def combine(fields, values, relations, min_iso, max_iso, want_masks=True):
     rel = (ctypes.c_int32 * n_series)(*[int(r) for r in relations])
     mn = (ctypes.c_double * n_series)(*[float(v) for v in min_iso])
     mx = (ctypes.c_double * n_series)(*[float(v) for v in max_iso])
-    check("gk_combine_series", lib.gk_combine_series(n_series, n, _ptr(fields), _ptr(values), rel, mn, mx,
-                                                     _ptr(out_v), _ptr(out_i), _ptr(masks), _stream()))
+    ids = ids.contiguous()
+    check("gk_combine_series", lib.gk_combine_series(n_series, n, _ptr(fields), _ptr(values), _ptr(ids), rel, mn,
+                                                     mx, _ptr(out_v), _ptr(out_i), _ptr(masks), _stream()))
     return out_v, out_i, masks
 
 
@@ -390,15 +430,23 @@ def octree_corners(centres, spacing):
 
 
 def octree_refine(centres, corner_ids, spacing, refine_all=False):
+    """Children of the voxels whose corners differ in any id set:
+    ``corner_ids`` is (8n,) or (n_sets, 8n) -- the lithology ids, then each
+    fault series' block ids."""
     lib = _lib.load()
     n = centres.shape[0]
+    n_sets = 0
+    if corner_ids is not None:
+        corner_ids = corner_ids.reshape(-1, 8 * n).contiguous() if n else corner_ids
+        n_sets = int(corner_ids.shape[0]) if n else 1
     dev = centres.device
     children = torch.empty((8 * n, 3), dtype=torch.float64, device=dev)
     count = torch.zeros(1, dtype=torch.int64, device=dev)
     wb = lib.gk_octree_workspace_bytes(n)
     work = torch.empty(max(wb, 8), dtype=torch.uint8, device=dev)
     sp = (ctypes.c_double * 3)(*[float(v) for v in spacing])
-    check("gk_octree_refine", lib.gk_octree_refine(n, _ptr(centres), _ptr(corner_ids), int(bool(refine_all)),
-                                                   sp, _ptr(children), _ptr(count), _ptr(work), wb, _stream()))
+    check("gk_octree_refine", lib.gk_octree_refine(n, _ptr(centres), _ptr(corner_ids), n_sets,
+                                                   int(bool(refine_all)), sp, _ptr(children), _ptr(count),
+                                                   _ptr(work), wb, _stream()))
     m = int(count.item())
     return children[:m]

@@ -75,14 +75,23 @@ typedef struct gk_info {
  * ``Orientations(dip_positions, dip_gradients, nugget_effect_grad)``; the
  * options are ``KernelOptions{range, c_o, uni_degree, i_res, gi_res,
  * kernel_function}``.  ``ref_index``/``rest_index`` give, per interface row,
- * the surface's reference point and the other ("rest") point. */
+ * the surface's reference point and the other ("rest") point.
+ *
+ * Fault drift: ``n_fault`` older FAULT series offset this one (the engine's
+ * ``faults_relations``, set by ``gempy/core/data/structural_frame.py:
+ * 244-273``).  Each adds one drift unknown whose function is that fault's
+ * block -- its segmented soft values -- given at this series' surface points
+ * in ``fault_sp`` (n_fault x n_sp, row per fault); the unknown comes after the
+ * polynomial drift, with gi_res (F(rest) - F(ref)) on the interface rows and
+ * 0 on the gradient rows. */
+#define GK_MAX_FAULTS 16
 typedef struct gk_system {
     int32_t n_ori;        /* orientations                                    */
     int32_t n_sp;         /* surface points of the series                    */
     int32_t n_iface;      /* interface rows = n_sp - n_surfaces              */
     int32_t uni_degree;   /* 0, 1 or 2 (drift functions: 0, 3, 9)            */
     int32_t kernel;       /* gk_kernel                                       */
-    int32_t reserved;
+    int32_t n_fault;      /* 0 .. GK_MAX_FAULTS fault-drift unknowns         */
     double range, c_o, i_res, gi_res;
     const double* dip_positions; /* n_ori x 3 */
     const double* dip_gradients; /* n_ori x 3 */
@@ -91,13 +100,17 @@ typedef struct gk_system {
     const double* nugget_sp;     /* n_sp      */
     const int32_t* ref_index;    /* n_iface   */
     const int32_t* rest_index;   /* n_iface   */
+    const double* fault_sp;      /* n_fault x n_sp (may be NULL if n_fault 0) */
 } gk_system;
 
 /* Evaluation points.  kind 0: regular grid of cell centres generated in the
  * kernel, ``ij`` order (x slowest, z fastest) as the reference's
  * ``RegularGrid`` (``gempy/core/data/grid_modules/regular_grid.py:58-71,
  * 192-201``); kind 1: an explicit n x 3 FP64 list (octree centres/corners,
- * custom grid, surface points). */
+ * custom grid, surface points).  ``fault_values`` holds, for a series with
+ * fault drift, the blocks of its n_fault offsetting faults at these points
+ * (row f at fault_values + f * fault_ld, fault_ld >= n; the soft values
+ * gk_eval wrote for that fault series); NULL when the series has none. */
 typedef struct gk_points {
     int32_t kind;
     int32_t dims[3];
@@ -105,12 +118,19 @@ typedef struct gk_points {
     double origin[3];     /* first cell centre (kind 0)                      */
     double spacing[3];    /* cell size (kind 0)                              */
     const double* xyz;    /* n x 3 (kind 1)                                  */
+    const double* fault_values; /* n_fault x fault_ld, or NULL               */
+    int64_t fault_ld;
 } gk_points;
 
 /* Segmentation of one series (``sigmoid_slope``, element ids, isovalues).
  * ``n_surf`` <= GK_MAX_SURFACES; isovalues are the series' surfaces sorted by
  * isovalue, highest first; ``unit_values`` has n_surf + 1 entries. All HOST
- * values (copied into the launch). */
+ * values (copied into the launch).  Soft values are
+ * u_0 + sum_k (u_(k+1) - u_k) sigmoid(slope (z_k - Z)); block ids are their
+ * slope -> infinity limit, u_0 + sum_k (u_(k+1) - u_k) [Z < z_k - GK_TIE_TOL]:
+ * rint(soft value) except that a point lying on a surface (an octree corner
+ * on a surface's reference point) takes the unit above it. */
+#define GK_TIE_TOL 1e-9
 #define GK_MAX_SURFACES 32
 typedef struct gk_segment {
     int32_t n_surf;
@@ -122,7 +142,7 @@ typedef struct gk_segment {
 
 /* ---------------- kriging-matrix build (engine covariance build) -------- */
 
-/* N = 3 n_ori + n_iface + n_drift. */
+/* N = 3 n_ori + n_iface + n_drift + n_fault. */
 int64_t gk_system_size(const gk_system* sys /* HOST struct */);
 
 /* Fills K (N x N, row-major, ld ``ldk`` >= N) and rhs (N) in ``prec``
@@ -241,13 +261,15 @@ gk_status gk_eval(const gk_system* sys, const void* model,
                   const gk_segment* seg, double* field, double* grad,
                   double* values, int32_t* ids, gk_stream stream);
 
-/* Combination of series with the squeezed masks (ERODE / ONLAP / BASEMENT,
- * ``gempy/core/data/structural_frame.py:326-330``): ``fields`` and
- * ``values`` are n_series x n (row per series), ``relations`` and
- * ``min_iso``/``max_iso`` are HOST arrays of n_series.  Writes the final soft
- * values, rint ids and the squeezed masks (uint8, n_series x n, may be NULL). */
+/* Combination of series with the squeezed masks (ERODE / ONLAP / FAULT /
+ * BASEMENT, ``gempy/core/data/structural_frame.py:326-330``; a FAULT series
+ * owns no lithology): ``fields``, ``values`` and ``ids`` (block ids) are
+ * n_series x n (row per series), ``relations`` and ``min_iso``/``max_iso`` are
+ * HOST arrays of n_series.  Writes the final soft values, the lithology ids
+ * and the squeezed masks (uint8, n_series x n, may be NULL). */
 gk_status gk_combine_series(int32_t n_series, int64_t n, const double* fields,
-                            const double* values, const int32_t* relations,
+                            const double* values, const int32_t* ids,
+                            const int32_t* relations,
                             const double* min_iso, const double* max_iso,
                             double* out_values, int32_t* out_ids,
                             uint8_t* masks, gk_stream stream);
@@ -259,14 +281,16 @@ gk_status gk_octree_corners(int64_t n, const double* centres,
                             const double spacing[3] /* HOST */,
                             double* corners, gk_stream stream);
 
-/* Marks voxels whose 8 corner ids differ (or all voxels when
- * ``refine_all``), and writes the children of marked voxels (8 each, same
- * corner order, at centre +- spacing/4) in parent order.  ``count`` (device
- * int64) receives the number of children; ``work`` needs
- * gk_octree_workspace_bytes(n). */
+/* Marks voxels whose 8 corners differ in any of ``n_id_sets`` id arrays
+ * (``corner_ids``: n_id_sets x 8n, row per set -- the lithology ids followed
+ * by each fault series' block ids), or all voxels when ``refine_all``, and
+ * writes the children of marked voxels (8 each, same corner order, at centre
+ * +- spacing/4) in parent order.  ``count`` (device int64) receives the number
+ * of children; ``work`` needs gk_octree_workspace_bytes(n). */
 size_t gk_octree_workspace_bytes(int64_t n);
 gk_status gk_octree_refine(int64_t n, const double* centres,
-                           const int32_t* corner_ids, int32_t refine_all,
+                           const int32_t* corner_ids, int32_t n_id_sets,
+                           int32_t refine_all,
                            const double spacing[3] /* HOST */,
                            double* children, int64_t* count, void* work,
                            size_t work_bytes, gk_stream stream);

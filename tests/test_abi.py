@@ -50,12 +50,14 @@ def test_version_and_size_queries_without_gpu(lib):
     assert lib.gk_system_size(ctypes.byref(s)) == 6 + 18 + 9
     assert lib.gk_eval_model_bytes(ctypes.byref(s)) > 0
     assert lib.gk_octree_workspace_bytes(1000) >= 8
+    s.n_fault = 2          # two offsetting faults: one drift unknown each
+    assert lib.gk_system_size(ctypes.byref(s)) == 6 + 18 + 9 + 2
 
 
 def test_struct_layouts_match_header():
     assert ctypes.sizeof(_lib.GkInfo) == 24
-    assert ctypes.sizeof(_lib.GkSystem) == 6 * 4 + 4 * 8 + 7 * 8
-    assert ctypes.sizeof(_lib.GkPoints) == 16 + 8 + 48 + 8
+    assert ctypes.sizeof(_lib.GkSystem) == 6 * 4 + 4 * 8 + 8 * 8
+    assert ctypes.sizeof(_lib.GkPoints) == 16 + 8 + 48 + 8 + 8 + 8
     assert ctypes.sizeof(_lib.GkSegment) == 8 + 8 + 8 * 32 + 8 * 33
     assert ctypes.sizeof(_lib.GkMlp) == 4 + 4 + 8
     assert ctypes.sizeof(_lib.GkAdam) == 5 * 4
@@ -75,8 +77,9 @@ def test_struct_layouts_match_compiled_header(tmp_path):
 #include <stddef.h>
 #include "gempy_gb300.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(gk_info), sizeof(gk_system), sizeof(gk_points),
-         sizeof(gk_segment), sizeof(gk_mlp), sizeof(gk_adam), offsetof(gk_mlp, params), offsetof(gk_system, range));
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(gk_info), sizeof(gk_system), sizeof(gk_points),
+         sizeof(gk_segment), sizeof(gk_mlp), sizeof(gk_adam), offsetof(gk_mlp, params), offsetof(gk_system, range),
+         offsetof(gk_system, fault_sp), offsetof(gk_points, fault_values), offsetof(gk_points, fault_ld));
   return 0;
 }
 """)
@@ -85,7 +88,8 @@ int main(void) {
     got = [int(v) for v in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
     want = [ctypes.sizeof(_lib.GkInfo), ctypes.sizeof(_lib.GkSystem), ctypes.sizeof(_lib.GkPoints),
             ctypes.sizeof(_lib.GkSegment), ctypes.sizeof(_lib.GkMlp), ctypes.sizeof(_lib.GkAdam),
-            _lib.GkMlp.params.offset, _lib.GkSystem.range.offset]
+            _lib.GkMlp.params.offset, _lib.GkSystem.range.offset, _lib.GkSystem.fault_sp.offset,
+            _lib.GkPoints.fault_values.offset, _lib.GkPoints.fault_ld.offset]
     assert got == want
 
 
@@ -114,6 +118,24 @@ def test_invalid_arguments_rejected_before_any_launch(lib):
     assert lib.gk_mlp_fwd_tc(ctypes.byref(net), 0, buf, buf, None, None) == _lib.GK_ERR_SIZE
     assert lib.gk_mlp_adam(10, None, None, None, None, None, None, 1, None) == _lib.GK_ERR_ARG
     assert lib.gk_gemv(10, None, 10, None, None, None) == _lib.GK_ERR_ARG
+    # fault drift: too many faults, or fault values missing
+    s = _lib.GkSystem()
+    s.n_ori, s.n_sp, s.n_iface, s.uni_degree, s.range = 1, 2, 1, 1, 1.0
+    s.dip_positions = s.dip_gradients = s.nugget_grad = s.sp_coords = s.nugget_sp = 64
+    s.ref_index = s.rest_index = 64
+    s.n_fault = _lib.GK_MAX_FAULTS + 1
+    assert lib.gk_build(ctypes.byref(s), 0, buf, 64, buf, None) == _lib.GK_ERR_SIZE
+    s.n_fault = 1
+    assert lib.gk_build(ctypes.byref(s), 0, buf, 64, buf, None) == _lib.GK_ERR_ARG   # fault_sp NULL
+    # combination: ids are required; an ONLAP last series has nothing to onlap
+    rel = (ctypes.c_int32 * 2)(3, 2)
+    iso = (ctypes.c_double * 2)(0.0, 0.0)
+    assert lib.gk_combine_series(2, 10, buf, buf, None, rel, iso, iso, None, None, None, None) == _lib.GK_ERR_ARG
+    assert lib.gk_combine_series(2, 10, buf, buf, buf, rel, iso, iso, None, None, None, None) == _lib.GK_ERR_ARG
+    # octree marking needs at least one id set
+    sp3 = (ctypes.c_double * 3)(1.0, 1.0, 1.0)
+    cnt = ctypes.c_int64(0)
+    assert lib.gk_octree_refine(8, buf, buf, 0, 0, sp3, buf, ctypes.byref(cnt), buf, 1024, None) == _lib.GK_ERR_ARG
 
 
 def test_tuning_tables_are_well_formed():

@@ -15,7 +15,8 @@ import pytest
 torch = pytest.importorskip("torch")
 
 from oracle import kriging, octree, pipeline, segmentation  # noqa: E402
-from tests._models import golden_extent, load_golden, oracle_series_from_golden, oracle_series_list  # noqa: E402
+from tests._models import (engine_inputs_from_golden, golden_extent, load_golden,  # noqa: E402
+                           oracle_series_from_golden, oracle_series_list)
 
 pytestmark = pytest.mark.gpu
 
@@ -285,12 +286,24 @@ def test_compute_model_anticline_pins():
     assert np.allclose(z[:: len(z) // 50], approved, rtol=1e-5, atol=1e-5)
     s = oracle_series_from_golden(g)
     lv = pipeline.compute_octree([s], [segmentation.BASEMENT], g["unit_values"], g["sigmoid_slope"], ext,
-                                 [2, 2, 2], 5)
-    for (c_ref, r_ref), ol in zip(lv, sol.octrees_output):
-        np.testing.assert_array_equal(ol.grid_centers, c_ref)
-        zr = r_ref.fields[0]
-        assert np.abs(ol.outputs[0].scalar_field - zr).max() <= 1e-9 * np.abs(zr).max()
-        np.testing.assert_array_equal(ol.last_output_center.ids_block, r_ref.ids.astype(np.int32))
+                                 [2, 2, 2], 5, levels_surface=4)
+    _assert_levels_match(sol, lv, 1)
+
+
+def _assert_levels_match(sol, lv, n_series, tol=1e-9):
+    """Octree levels of compute_model against the oracle's: identical centres,
+    exported fields (centres, then corners on surface levels) within ``tol``
+    of max|Z|, identical lithology ids and squeezed masks."""
+    assert len(sol.octrees_output) == len(lv)
+    for L, ol in zip(lv, sol.octrees_output):
+        np.testing.assert_array_equal(ol.grid_centers, L.centres)
+        for i in range(n_series):
+            zr = L.exported_field(i)
+            z = ol.outputs[i].scalar_field
+            assert z.shape == zr.shape
+            assert np.abs(z - zr).max() <= tol * np.abs(zr).max()
+        np.testing.assert_array_equal(ol.last_output_center.ids_block, L.result.ids.astype(np.int32))
+        np.testing.assert_array_equal(ol.last_output_center.mask_matrix.astype(bool), L.result.masks)
 
 
 def test_compute_model_mixed_anticline():
@@ -314,17 +327,85 @@ def test_compute_model_three_series_octree_matches_oracle():
     og = m.interpolation_input.grid.octree_grid
     rel = [int(r) for r in m.data_descriptor.stack_structure.masking_descriptor]
     lv = pipeline.compute_octree(ss, rel, m.interpolation_input.unit_values, m.options.sigmoid_slope,
-                                 og.orthogonal_extent, og.regular_grid_shape, 4)
-    for (c_ref, r_ref), ol in zip(lv, sol.octrees_output):
-        np.testing.assert_array_equal(ol.grid_centers, c_ref)
-        for i in range(len(ss)):
-            zr = r_ref.fields[i]
-            assert np.abs(ol.outputs[i].scalar_field - zr).max() <= 1e-9 * np.abs(zr).max()
-        np.testing.assert_array_equal(ol.last_output_center.ids_block, r_ref.ids.astype(np.int32))
-        np.testing.assert_array_equal(ol.last_output_center.mask_matrix.astype(bool), r_ref.masks)
+                                 og.orthogonal_extent, og.regular_grid_shape, 4, levels_surface=4)
+    _assert_levels_match(sol, lv, len(ss))
     _, isos = pipeline.solve_all(ss)
     iso_ref = np.concatenate(isos)
     np.testing.assert_allclose(sol.scalar_field_at_surface_points, iso_ref, rtol=1e-9, atol=0)
+
+
+def _golden_octree(name, dtype="float64"):
+    import gempy_gb300 as gg
+    from oracle import inputs
+    g = load_golden(name)
+    ii, opts, dd, ext = engine_inputs_from_golden(g)
+    sol = gg.compute_model(ii, opts, dd, config=gg.EngineConfig(dtype=dtype))
+    series, rels, fr = inputs.series_from_golden(g)
+    oc = g["octree"]
+    lv = pipeline.compute_octree(series, rels, g["unit_values"], g["sigmoid_slope"], ext, oc["base_resolution"],
+                                 oc["levels"], fault_relations=fr, levels_surface=oc.get("levels_surface", 4))
+    return g, sol, lv, series
+
+
+def test_compute_model_fault_model_pins():
+    """The one-fault model through compute_model: the reference's approval
+    file (test_example_models_I.py:56-68) under its own comparator, and every
+    octree level against the oracle (centres, fields of both series, lithology
+    ids, masks) -- the fault's block drives the strata's fault drift and the
+    refinement."""
+    g, sol, lv, series = _golden_octree("fault_model.json")
+    z = sol.octrees_output[-1].outputs[0].scalar_field
+    assert len(z) == 24624
+    approved = np.array(g["octree"]["approved_scalar_field_last_level"])
+    assert np.allclose(z[:: len(z) // 50], approved, rtol=1e-5, atol=1e-5)
+    _assert_levels_match(sol, lv, len(series))
+    from oracle import inputs
+    series, rels, fr = inputs.series_from_golden(g)
+    m = pipeline.Model(series, rels, g["unit_values"], g["sigmoid_slope"], fr)
+    np.testing.assert_allclose(sol.scalar_field_at_surface_points, np.concatenate(m.isos), rtol=1e-9, atol=1e-12)
+
+
+def test_compute_model_combination_model_matches_oracle():
+    """Fault + eroding unconformity + folded strata (three series, the fault
+    offsetting both): every octree level of compute_model against the oracle,
+    including the corner values the surface levels export."""
+    g, sol, lv, series = _golden_octree("combination_model.json")
+    _assert_levels_match(sol, lv, len(series))
+    assert len(sol.octrees_output[-1].outputs[0].scalar_field) == 9 * len(sol.octrees_output[-1].grid_centers)
+
+
+def test_compute_model_fault_model_mixed_matches_plain():
+    """The mixed form on the fault model: the same octree and ids as the FP64
+    form, fields within 1e-7 of it."""
+    _, mixed, _, _ = _golden_octree("fault_model.json", dtype="float32")
+    _, plain, _, _ = _golden_octree("fault_model.json", dtype="float64")
+    for a, b in zip(mixed.octrees_output, plain.octrees_output):
+        np.testing.assert_array_equal(a.grid_centers, b.grid_centers)
+        np.testing.assert_array_equal(a.last_output_center.ids_block, b.last_output_center.ids_block)
+        for i in range(2):
+            zb = b.outputs[i].scalar_field
+            assert np.abs(a.outputs[i].scalar_field - zb).max() <= 1e-7 * np.abs(zb).max()
+
+
+def test_compute_model_onlap_series_matches_oracle():
+    """An ONLAP series over an eroding one over the basement series: masks,
+    ids and fields against the oracle (segmentation.series_masks)."""
+    import gempy_gb300 as gg
+    from gempy_gb300 import synthetic
+    m = synthetic.folded_series(octree_levels=3)
+    ss = m.data_descriptor.stack_structure
+    rel = list(ss.masking_descriptor)
+    rel[0] = gg.StackRelationType.ONLAP
+    ss.masking_descriptor = rel
+    sol = gg.compute_model(m.interpolation_input, m.options, m.data_descriptor)
+    series = oracle_series_list(m)
+    og = m.interpolation_input.grid.octree_grid
+    lv = pipeline.compute_octree(series, [int(r) for r in rel], m.interpolation_input.unit_values,
+                                 m.options.sigmoid_slope, og.orthogonal_extent, og.regular_grid_shape, 3,
+                                 levels_surface=4)
+    _assert_levels_match(sol, lv, len(series))
+    masks = sol.octrees_output[-1].last_output_center.mask_matrix.astype(bool)
+    assert masks[0].any() and masks[1].any() and masks[2].any()
 
 
 def test_nan_input_reports_status_without_fault():
