@@ -123,7 +123,7 @@ SIGNATURES = [
                                        ctypes.c_void_p]),
     ("gk_eval", ctypes.c_int, [ctypes.POINTER(GkSystem), ctypes.c_void_p, ctypes.POINTER(GkPoints),
                                ctypes.c_int, ctypes.POINTER(GkSegment), ctypes.c_void_p, ctypes.c_void_p,
-                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     ("gk_combine_series", ctypes.c_int, [ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
                                          ctypes.c_void_p, c_int32_p, c_double_p, c_double_p, ctypes.c_void_p,
                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
@@ -159,6 +159,7 @@ SIGNATURES = [
                                    ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(GkAdam), ctypes.c_int32,
                                    ctypes.c_void_p]),
     ("gk_system_features", ctypes.c_int, [ctypes.POINTER(GkSystem), ctypes.c_void_p, ctypes.c_void_p]),
+    ("gk_set_wait_limit", ctypes.c_int, [ctypes.c_int64]),
     ("gk_version", ctypes.c_char_p, []),
     ("gk_launch_count", ctypes.c_uint64, []),
 ]

@@ -435,7 +435,6 @@ __global__ void __launch_bounds__(256) batch_prepare_kernel(const BatchDesc* __r
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 constexpr int kChunkPoints = 1024;  // points per (system, chunk) item, whatever the variant
-constexpr long long kWaitSpin = 4LL * 1000 * 1000;
 
 struct Cursor {
     int64_t k;   // index into this CTA's item list
@@ -445,7 +444,7 @@ struct Cursor {
 template <int kPPT, int kStage>
 __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchDesc* __restrict__ D, int n_sys,
                                                          const int64_t* __restrict__ chunk_prefix, double* field,
-                                                         double* values, int32_t* ids, int* err) {
+                                                         double* values, int32_t* ids, gk_info* infos) {
     static_assert(kChunkPoints % (256 * kPPT) == 0, "chunk is a whole number of passes");
     constexpr int kPasses = kChunkPoints / (256 * kPPT);
     extern __shared__ __align__(128) unsigned char smem[];
@@ -539,7 +538,8 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchDesc* __rest
             const int sg = (int)(consumed & 1);
             const uint32_t parity = (uint32_t)((consumed >> 1) & 1);
             bool ok = false;
-            for (long long i = 0; i < kWaitSpin && !ok; ++i) {
+            const long long cap = wait_cap(kCopySpin);
+            for (long long i = 0; i < cap && !ok; ++i) {
                 uint32_t r;
                 asm volatile(
                     "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, "
@@ -550,7 +550,7 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchDesc* __rest
                 ok = r != 0;
             }
             if (!ok) {
-                if (err) atomicExch(err, GK_ERR_TIMEOUT);
+                report(infos ? infos + s : nullptr, GK_ERR_TIMEOUT, -2);  // this realisation's status
                 s_fail = 1;
             }
             __syncthreads();
@@ -558,7 +558,7 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchDesc* __rest
                 // wait (bounded) for the copies still in flight, then leave
                 if (tid == 0) {
                     for (int64_t u = consumed; u < issued; ++u) {
-                        for (long long i = 0; i < kWaitSpin; ++i) {
+                        for (long long i = 0; i < kCopySpin; ++i) {
                             uint32_t r;
                             asm volatile(
                                 "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n "
@@ -657,6 +657,8 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchDesc* __rest
         }  // pass
     }
 }
+
+cudaError_t wait_cap_set_batch(long long v) { return set_wait_cap_here(v); }
 
 }  // namespace gk
 
@@ -825,14 +827,14 @@ extern "C" gk_status gk_batch_plan(const gk_batch* b, void* work, size_t work_by
 
 template <int PPT, int STAGE>
 static gk_status launch_batch_eval(const BatchDesc* D, int n, const int64_t* chunk_prefix, double* field,
-                                   double* values, int32_t* ids, int* err, int sms, cudaStream_t s) {
+                                   double* values, int32_t* ids, gk_info* infos, int sms, cudaStream_t s) {
     auto k = batch_eval_kernel<PPT, STAGE>;
     const size_t smem = 2 * (size_t)STAGE;
     GK_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int occ = 0;
     GK_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, 256, smem));
     if (occ < 1) occ = 1;
-    k<<<sms * occ, 256, smem, s>>>(D, n, chunk_prefix, field, values, ids, err);
+    k<<<sms * occ, 256, smem, s>>>(D, n, chunk_prefix, field, values, ids, infos);
     GK_LAUNCH_CHECK();
     return GK_OK;
 }
@@ -865,15 +867,15 @@ extern "C" gk_status gk_batch_run(const gk_batch* b, void* work, size_t work_byt
     const TuneVariant v = tune_variant(GK_TUNE_BATCH_EVAL);
     if (v.ppt == 4 && v.stage_kb == 32)
         return launch_batch_eval<4, 32 * 1024>(D, (int)n, (const int64_t*)(base + chunk_prefix), field, values, ids,
-                                               counters + 2, sms, s);
+                                               infos, sms, s);
     if (v.ppt == 2 && v.stage_kb == 32)
         return launch_batch_eval<2, 32 * 1024>(D, (int)n, (const int64_t*)(base + chunk_prefix), field, values, ids,
-                                               counters + 2, sms, s);
+                                               infos, sms, s);
     if (v.ppt == 4)
         return launch_batch_eval<4, 16 * 1024>(D, (int)n, (const int64_t*)(base + chunk_prefix), field, values, ids,
-                                               counters + 2, sms, s);
+                                               infos, sms, s);
     return launch_batch_eval<2, 16 * 1024>(D, (int)n, (const int64_t*)(base + chunk_prefix), field, values, ids,
-                                           counters + 2, sms, s);
+                                           infos, sms, s);
 }
 
 extern "C" gk_status gk_batch_results(const gk_batch* b, const void* work, size_t work_bytes, int32_t item,

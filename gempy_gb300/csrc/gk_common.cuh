@@ -46,9 +46,21 @@ constexpr double kGradEps = 1e-5;
 // the anticline approval file selects; it moves C'/r(0) by 105/4 * 1e-5 / a^3.
 constexpr double kDistEps2 = 1e-10;
 
-// Iteration cap of every inter-CTA spin wait: ~seconds at worst, then the
+// Default iteration caps of the spin waits: ~seconds at worst, then the
 // kernel records GK_ERR_TIMEOUT and returns instead of hanging the GPU.
-constexpr long long kSpinLimit = 20LL * 1000 * 1000;
+constexpr long long kSpinLimit = 20LL * 1000 * 1000;  // inter-CTA waits (grid barrier, block flags)
+constexpr long long kCopySpin = 4LL * 1000 * 1000;    // bulk-copy completion waits (mbarrier)
+
+// Cap in force for the waits of this module (each translation unit has its
+// own copy): negative selects the defaults above.  gk_set_wait_limit sets it
+// so tests can make the waits run out (0: give up before the first poll).
+// A CTA that gave up still waits for its bulk copies in flight with the
+// default cap before it exits.
+static __constant__ long long g_wait_cap = -1;
+__device__ __forceinline__ long long wait_cap(long long dflt) { return g_wait_cap < 0 ? dflt : g_wait_cap; }
+static inline cudaError_t set_wait_cap_here(long long v) {
+    return cudaMemcpyToSymbol(g_wait_cap, &v, sizeof(v));
+}
 
 __host__ __device__ inline int drift_count(int degree) {
     return degree == 1 ? 3 : (degree == 2 ? 9 : 0);
@@ -154,18 +166,18 @@ struct GridBarrier {
                 __threadfence();
                 atomicAdd(&bar[1], 1u);
             } else {
-                long long spins = 0;
-                while (true) {
-                    unsigned int g;
-                    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(g) : "l"(bar + 1) : "memory");
-                    if (g != gen) break;
-                    if (*abort) { s_ok = 0; break; }
-                    if (++spins > kSpinLimit) {
+                const long long cap = wait_cap(kSpinLimit);
+                for (long long spins = 0;; ++spins) {
+                    if (spins >= cap) {
                         *abort = 1;
                         report(info, GK_ERR_TIMEOUT, -1);
                         s_ok = 0;
                         break;
                     }
+                    unsigned int g;
+                    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(g) : "l"(bar + 1) : "memory");
+                    if (g != gen) break;
+                    if (*abort) { s_ok = 0; break; }
                 }
             }
             __threadfence();

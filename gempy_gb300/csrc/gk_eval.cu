@@ -162,9 +162,10 @@ __device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-constexpr long long kMbarSpin = 4LL * 1000 * 1000;
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    for (long long i = 0; i < kMbarSpin; ++i)
+// Bounded wait for a stage's bulk copy: the first wait on a stage uses the
+// module's cap (wait_cap), the drain before an early exit the default.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long cap) {
+    for (long long i = 0; i < cap; ++i)
         if (mbar_try(bar, parity)) return true;
     return false;
 }
@@ -190,7 +191,7 @@ struct EvalParams {
     double* grad;
     double* values;
     int32_t* ids;
-    int* err;          // device error word (timeouts), may be NULL
+    gk_info* info;     // device status word (timeouts), may be NULL
 };
 
 template <typename T> __device__ __forceinline__ T fast_r(T r2);
@@ -305,8 +306,8 @@ __global__ void __launch_bounds__(256) eval_kernel(const EvalParams P) {
         for (int t = 0; t < n_tiles; ++t, ++item) {
             const int s = (int)(item & 1);
             const uint32_t parity = (uint32_t)((item >> 1) & 1);
-            if (!mbar_wait(&mbar[s], parity)) {
-                if (P.err) atomicExch(P.err, GK_ERR_TIMEOUT);
+            if (!mbar_wait(&mbar[s], parity, wait_cap(kCopySpin))) {
+                report(P.info, GK_ERR_TIMEOUT, (int)blockIdx.x);
                 s_fail = 1;
             }
             __syncthreads();
@@ -403,7 +404,8 @@ __global__ void __launch_bounds__(256) eval_kernel(const EvalParams P) {
 drain:
     // a stage wait gave up: wait (bounded) for copies still in flight, then leave
     if (tid == 0) {
-        for (int64_t it = item; it < n_items && it < item + 2; ++it) mbar_wait(&mbar[it & 1], (uint32_t)((it >> 1) & 1));
+        for (int64_t it = item; it < n_items && it < item + 2; ++it)
+            mbar_wait(&mbar[it & 1], (uint32_t)((it >> 1) & 1), kCopySpin);
     }
     __syncthreads();
 }
@@ -490,8 +492,8 @@ __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const 
         for (int t = 0; t < n_tiles; ++t, ++item) {
             const int s = (int)(item & 1);
             const uint32_t parity = (uint32_t)((item >> 1) & 1);
-            if (!mbar_wait(&mbar[s], parity)) {
-                if (P.err) atomicExch(P.err, GK_ERR_TIMEOUT);
+            if (!mbar_wait(&mbar[s], parity, wait_cap(kCopySpin))) {
+                report(P.info, GK_ERR_TIMEOUT, (int)blockIdx.x);
                 s_fail = 1;
             }
             __syncthreads();
@@ -579,7 +581,8 @@ __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const 
     return;
 drain:
     if (tid == 0) {
-        for (int64_t it = item; it < n_items && it < item + 2; ++it) mbar_wait(&mbar[it & 1], (uint32_t)((it >> 1) & 1));
+        for (int64_t it = item; it < n_items && it < item + 2; ++it)
+            mbar_wait(&mbar[it & 1], (uint32_t)((it >> 1) & 1), kCopySpin);
     }
     __syncthreads();
 }
@@ -625,6 +628,8 @@ __global__ void combine_kernel(const CombineParams P) {
     if (P.out_values) P.out_values[i] = v;
     if (P.out_ids) P.out_ids[i] = id;
 }
+
+cudaError_t wait_cap_set_eval(long long v) { return set_wait_cap_here(v); }
 
 }  // namespace gk
 
@@ -739,7 +744,7 @@ static gk_status launch_eval_ff(EvalParams& P, const double* meta, cudaStream_t 
 
 extern "C" gk_status gk_eval(const gk_system* s, const void* model, const gk_points* pts, gk_prec prec,
                              const gk_segment* seg, double* field, double* grad, double* values, int32_t* ids,
-                             gk_stream stream) {
+                             gk_info* info, gk_stream stream) {
     gk_status st = gk_check_system(s);
     if (st != GK_OK) return st;
     if (model == nullptr || pts == nullptr) return GK_ERR_ARG;
@@ -783,7 +788,7 @@ extern "C" gk_status gk_eval(const gk_system* s, const void* model, const gk_poi
     P.grad = grad;
     P.values = values;
     P.ids = ids;
-    P.err = nullptr;
+    P.info = info;
     cudaStream_t cs = (cudaStream_t)stream;
     if (prec == GK_F64) {
         P.ori = m + L.ori64;

@@ -954,13 +954,13 @@ __global__ void __launch_bounds__(256) trsv_kernel(const T* __restrict__ A, int6
             }
         }
         if (lane == 0) {
-            long long spins = 0;
-            while (true) {
+            const long long cap = wait_cap(kSpinLimit);
+            for (long long spins = 0;; ++spins) {
+                if (spins >= cap) { report(info, GK_ERR_TIMEOUT, dep); break; }
                 int f;
                 asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(f) : "l"(flags + kFlagStride * dep)
                              : "memory");
                 if (f) break;
-                if (++spins > kSpinLimit) { report(info, GK_ERR_TIMEOUT, dep); break; }
                 if (spins > 64) __nanosleep(20);
             }
         }
@@ -1530,6 +1530,9 @@ __global__ void scatter_scale_kernel(const T* __restrict__ t, const int32_t* __r
     }
 }
 
+cudaError_t wait_cap_set_eval(long long v);
+cudaError_t wait_cap_set_batch(long long v);
+
 }  // namespace gk
 
 using namespace gk;
@@ -1752,3 +1755,11 @@ gk_status gk_internal_twolevel_apply_f64(int64_t n, const double* A, int64_t lda
     return twolevel_apply<double>(n, A, lda, perm, d, r, bs, v, z, t, work, wbytes, info, st);
 }
 size_t gk_internal_lu_ws_f64(int64_t n) { return lu_ws_bytes<double>(n); }
+
+extern "C" gk_status gk_set_wait_limit(int64_t spins) {
+    const long long v = spins < 0 ? -1 : (long long)spins;
+    if (set_wait_cap_here(v) != cudaSuccess) return GK_ERR_CUDA;
+    if (wait_cap_set_eval(v) != cudaSuccess) return GK_ERR_CUDA;
+    if (wait_cap_set_batch(v) != cudaSuccess) return GK_ERR_CUDA;
+    return GK_OK;
+}

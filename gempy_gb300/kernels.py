@@ -367,10 +367,11 @@ def make_segment(isovalues_sorted, unit_values, slope):
 
 
 def evaluate(series: DeviceSeries, model, pts: Points, prec=GK_F64, seg=None, gradient=False, want_field=True,
-             want_values=True, want_ids=False, out=None, fault_values=None):
+             want_values=True, want_ids=False, out=None, fault_values=None, info=None):
     """Field (gradient, soft values, block ids) of one series at ``pts``;
     ``fault_values`` (n_fault, n) holds the blocks of the faults that offset
-    the series at these points (required when it has fault drift)."""
+    the series at these points (required when it has fault drift); ``info``
+    an optional gk_info tensor (``new_info``) for device-side failures."""
     lib = _lib.load()
     n = pts.n
     if series.n_faults:
@@ -398,7 +399,7 @@ def evaluate(series: DeviceSeries, model, pts: Points, prec=GK_F64, seg=None, gr
         ids = torch.empty(n, dtype=torch.int32, device=dev)
     check("gk_eval", lib.gk_eval(ctypes.byref(series.sys), _ptr(model), ctypes.byref(pts.gk), prec,
                                  ctypes.byref(seg) if seg is not None else None, _ptr(field), _ptr(grad),
-                                 _ptr(values), _ptr(ids), _stream()))
+                                 _ptr(values), _ptr(ids), _ptr(info), _stream()))
     return field, grad, values, ids
 
 
@@ -450,3 +451,10 @@ def octree_refine(centres, corner_ids, spacing, refine_all=False):
                                                    _ptr(work), wb, _stream()))
     m = int(count.item())
     return children[:m]
+
+
+def set_wait_limit(spins):
+    """Iteration cap of the kernels' spin waits (``gk_set_wait_limit``): 0
+    makes them give up at once, None or a negative value restores the
+    defaults.  For tests of the failure paths."""
+    check("gk_set_wait_limit", _lib.load().gk_set_wait_limit(-1 if spins is None else int(spins)))

@@ -252,14 +252,17 @@ gk_status gk_eval_prepare(const gk_system* sys, const double* w, void* model,
                           gk_stream stream);
 
 /* Scalar field (times gi_res, the engine's reported scale), optional
- * gradient (n x 3), optional soft segmentation values and ids.  ``prec``
+ * gradient (n x 3), optional soft segmentation values and ids.  ``info``
+ * (may be NULL) receives GK_ERR_TIMEOUT if a wait for a staged record tile
+ * gives up (the outputs are then incomplete).  ``prec``
  * selects FP64, FP32 or float-float arithmetic (GK_FF: field only, cubic
  * kernel); outputs are always FP64 for field/values and int32 for ids.  Any
  * output pointer may be NULL.  ``seg`` may be NULL (no segmentation). */
 gk_status gk_eval(const gk_system* sys, const void* model,
                   const gk_points* pts, gk_prec prec,
                   const gk_segment* seg, double* field, double* grad,
-                  double* values, int32_t* ids, gk_stream stream);
+                  double* values, int32_t* ids, gk_info* info,
+                  gk_stream stream);
 
 /* Combination of series with the squeezed masks (ERODE / ONLAP / FAULT /
  * BASEMENT, ``gempy/core/data/structural_frame.py:326-330``; a FAULT series
@@ -440,6 +443,22 @@ gk_status gk_mlp_adam(int64_t n, float* master, uint16_t* params,
  * alignment, nugget levels, drift degree, point spacing, surface count. */
 gk_status gk_system_features(const gk_system* s, float* features,
                              gk_stream stream);
+
+/* ---------------- failure-path testing ---------------------------------- */
+
+/* Iteration cap of the kernels' spin waits, for tests of the failure paths
+ * (no reference counterpart: the reference has no device code).  The capped
+ * waits are the inter-CTA ones -- the grid barrier of the cooperative LU
+ * panel, the block flags of the triangular solves -- and each first wait on a
+ * bulk copy of the evaluation kernels (single-system and batched).  A wait
+ * that reaches its cap records GK_ERR_TIMEOUT in the call's gk_info (for
+ * gk_batch_run, in the realisation's) and its kernel returns early; a CTA
+ * that gave up first waits, with the default cap, for its copies still in
+ * flight.  ``spins`` 0 makes every capped wait give up before its first poll;
+ * a negative value restores the defaults (2e7 polls inter-CTA, 4e6 per copy).
+ * The network's tensor-core pass keeps its own fixed cap.  Applies to the
+ * current device; call it while no kernel of this library is running. */
+gk_status gk_set_wait_limit(int64_t spins);
 
 /* Library version string (HOST). */
 const char* gk_version(void);
