@@ -169,22 +169,36 @@ def reference_arm(args):
         t2 = time.perf_counter()
         return t1 - t0, (t2 - t1) / sample
 
-    for _ in range(max(0, min(args.warmup, 1))):
+    # every sample step is a full FP64 build + LU on the host cores (seconds each):
+    # at most 1 warm-up and 3 timed steps run, and the line reports what ran
+    n_warm = max(0, min(args.warmup, 1))
+    n_steps = max(1, min(args.steps, 3))
+    t_start = time.perf_counter()
+    for _ in range(n_warm):
         step()
     ts, te = [], []
-    for _ in range(max(1, min(args.steps, 2))):
+    for _ in range(n_steps):
         a, b = step()
         ts.append(a)
         te.append(b)
+    wall = time.perf_counter() - t_start
     t_solve, t_pt = float(np.mean(ts)), float(np.mean(te))
     t_step = t_solve + t_pt * n_total
     v = n_total / t_step
+    sample_ms = 1e3 * (t_solve + t_pt * sample)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "grid points/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_step, "higher_is_better": True,
+            "steps": n_steps, "warmup": n_warm, "ms_per_step": sample_ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "grid_points": n_total},
+            "requested": {"steps": args.steps, "warmup": args.warmup},
+            "extrapolated": True,
+            "value_basis": "value = grid_points / (build+LU seconds + per-point seconds x grid_points); "
+                           "ms_per_step is the measured sample step",
+            "sample_points": sample, "measured_steps": n_steps, "measured_seconds": wall,
+            "extrapolated_ms_per_workload_step": 1e3 * t_step,
             "solves_per_s": 1.0 / t_solve,
             "cpu_baseline": {"value": v, "unit": "grid points/s", "cores": cores, "kind": "port",
+                             "extrapolated": True, "sample_points": sample,
                              "sample": f"FP64 numpy/scipy oracle: full build+LU (N={s.size}) per step + "
                                        f"{sample}-point subsample of the 256^3 grid, extrapolated to "
                                        f"{n_total} points"},
@@ -445,6 +459,7 @@ def main():
                      "fp32_pipe_frac": achieved_tf * 168 / 20 / fp32_peak},
     }
     if not args.no_extra and rank == 0:
+        line["plain"] = plain_section()
         line["batch"] = batch_section(n_real=args.batch_realisations)
         line["octree"] = octree_section()
         line["learned"] = learned_section(args.learned_points, args.learned_config)
@@ -530,6 +545,54 @@ def batch_section(n_real=512, res=64, plain=True):
                              "note": "single-system FP64 kernels, one realisation after another"}
         out["speedup_vs_plain_fp64"] = ms_p / ms
         out["errors_vs_fp64"] = {"field_rel_max": err, "ids_mismatch_outside_band": mism}
+    return out
+
+
+def plain_section():
+    """Config 1: the plain horizontal model (2 surfaces x 10 points, 2
+    orientations, linear drift, 50^3 dense grid) through compute_model from
+    host inputs: plain FP64 and mixed on the GPU, and the FP64 oracle on the
+    host cores, all on the full grid."""
+    import torch
+    import gempy_gb300 as gg
+    from gempy_gb300 import synthetic
+    from oracle import kriging, segmentation
+    from oracle.inputs import series_from_engine_inputs
+    m = synthetic.plain_horizontal()
+    args_ = (m.interpolation_input, m.options, m.data_descriptor)
+    n_pts = m.interpolation_input.grid.dense_grid.n_points
+    out = {"workload": "2 horizontal surfaces x 10 points, 2 orientations, cubic, linear drift, 50^3 dense grid",
+           "grid_points": n_pts}
+    sols = {}
+    for name, dt in (("plain_fp64", "float64"), ("mixed", "float32")):
+        cfg = gg.EngineConfig(dtype=dt)
+        for _ in range(3):
+            gg.compute_model(*args_, config=cfg)
+        torch.cuda.synchronize()
+        reps = 10
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            sols[name] = gg.compute_model(*args_, config=cfg)
+        torch.cuda.synchronize()
+        dt_s = (time.perf_counter() - t0) / reps
+        out[name] = {"ms": 1e3 * dt_s, "points_per_s": n_pts / dt_s, "solves_per_s": 1.0 / dt_s}
+    (s,) = series_from_engine_inputs(*args_)
+    t0 = time.perf_counter()
+    w = kriging.solve(*kriging.build_system(s))
+    iso = kriging.isovalues(s, w)
+    z = kriging.evaluate(s, w, m.interpolation_input.grid.dense_grid.values)
+    segmentation.segment(z, iso, m.interpolation_input.unit_values, m.options.sigmoid_slope)
+    t_cpu = time.perf_counter() - t0
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    out["cpu_oracle"] = {"ms": 1e3 * t_cpu, "points_per_s": n_pts / t_cpu, "cores": cores, "extrapolated": False}
+    zp = np.asarray(sols["plain_fp64"].raw_arrays.scalar_field_matrix)[0]
+    zm = np.asarray(sols["mixed"].raw_arrays.scalar_field_matrix)[0]
+    out["errors"] = {"plain_vs_oracle_rel": float(np.abs(zp - z).max() / np.abs(z).max()),
+                     "mixed_vs_plain_rel": float(np.abs(zm - zp).max() / np.abs(zp).max()),
+                     "ids_identical": bool(np.array_equal(sols["plain_fp64"].raw_arrays.lith_block,
+                                                          sols["mixed"].raw_arrays.lith_block))}
+    out["speedup_vs_plain_fp64"] = out["plain_fp64"]["ms"] / out["mixed"]["ms"]
+    out["speedup_plain_gpu_vs_cpu_oracle"] = t_cpu * 1e3 / out["plain_fp64"]["ms"]
     return out
 
 
@@ -684,6 +747,7 @@ def cpu_baseline(m, sample=4096):
     t_step = (t1 - t0) + (t2 - t1) / sample * n_total
     cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
     return {"value": n_total / t_step, "unit": "grid points/s", "cores": cores, "kind": "port",
+            "extrapolated": True, "sample_points": sample,
             "sample": f"FP64 numpy/scipy oracle (BLAS threads = all {cores} cores): full build+LU "
                       f"(N={s.size}) + {sample}-point subsample of the grid, extrapolated to {n_total} points",
             "solve_s": t1 - t0, "eval_s_per_point": (t2 - t1) / sample}

@@ -573,7 +573,7 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchDesc* __rest
                 __syncthreads();
                 return;
             }
-            ff acc[kPPT];
+            ffacc acc[kPPT];
 #pragma unroll
             for (int p = 0; p < kPPT; ++p) acc[p] = {0.f, 0.f};
             const float* rec = reinterpret_cast<const float*>(stage[sg]);
@@ -589,14 +589,15 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchDesc* __rest
                         float dh[3], dl[3];
                         ff r2 = ff_dist2(X[p], ph, pl, dh, dl, eps2);
                         if (r2.h >= 1.f) continue;
-                        ff sr = ff_sqrt(r2);
-                        ff kk = ff_add_f(ff_mul_f(r2, 5.25f), -17.5f);
-                        kk = ff_horner(r2, kk, 26.25f);
-                        kk = ff_horner(sr, kk, -14.f);
-                        ff wh = ff_mul(wx, ff{-dh[0], -dl[0]});
-                        wh = ff_add(wh, ff_mul(wy, ff{-dh[1], -dl[1]}));
-                        wh = ff_add(wh, ff_mul(wz, ff{-dh[2], -dl[2]}));
-                        acc[p] = ff_add(acc[p], ff_mul(kk, wh));
+                        const ff sr = ff_sqrt(r2);
+                        const ff kk = ff_cubic_d1(r2, sr);
+                        const ff wh = ff_dot3(wx, wy, wz, ff{-dh[0], -dl[0]}, ff{-dh[1], -dl[1]},
+                                              ff{-dh[2], -dl[2]});
+                        ff_acc_fma(acc[p], kk, wh);
+                    }
+                    if ((qr & 7) == 7) {  // fold the low words back every 8 records
+#pragma unroll
+                        for (int p = 0; p < kPPT; ++p) ff_acc_norm(acc[p]);
                     }
                 }
             } else {
@@ -611,17 +612,17 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchDesc* __rest
                         float dh[3], dl[3];
                         ff r2 = ff_dist2(X[p], ph, pl, dh, dl, eps2);
                         if (r2.h >= 1.f) continue;
-                        ff sr = ff_sqrt(r2);
-                        ff cc = ff_add_f(ff_mul_f(r2, 0.75f), -3.5f);
-                        cc = ff_horner(r2, cc, 8.75f);
-                        cc = ff_horner(sr, cc, -7.f);
-                        cc = ff_horner(r2, cc, 1.f);
-                        acc[p] = ff_add(acc[p], ff_mul(cc, W));
+                        const ff sr = ff_sqrt(r2);
+                        ff_acc_fma(acc[p], ff_cubic_C(r2, sr), W);
+                    }
+                    if ((qr & 7) == 7) {  // fold the low words back every 8 records
+#pragma unroll
+                        for (int p = 0; p < kPPT; ++p) ff_acc_norm(acc[p]);
                     }
                 }
             }
 #pragma unroll
-            for (int p = 0; p < kPPT; ++p) Z[p] += ff_to_double(acc[p]);
+            for (int p = 0; p < kPPT; ++p) Z[p] += ff_acc_to_double(acc[p]);
             __syncthreads();
             consumed++;
             issue_next();

@@ -499,7 +499,7 @@ __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const 
             __syncthreads();
             if (s_fail) goto drain;
             {
-                ff acc[PPT];
+                ffacc acc[PPT];
 #pragma unroll
                 for (int p = 0; p < PPT; ++p) acc[p] = {0.f, 0.f};
                 const float* rec = reinterpret_cast<const float*>(stage[s]);
@@ -515,15 +515,16 @@ __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const 
                             float dh[3], dl[3];
                             ff r2 = ff_dist2(X[p], ph, pl, dh, dl, eps2);
                             if (r2.h >= 1.f) continue;  // beyond the range: C'/r = 0
-                            ff sr = ff_sqrt(r2);
-                            ff k = ff_add_f(ff_mul_f(r2, 5.25f), -17.5f);
-                            k = ff_horner(r2, k, 26.25f);
-                            k = ff_horner(sr, k, -14.f);
+                            const ff sr = ff_sqrt(r2);
+                            const ff k = ff_cubic_d1(r2, sr);
                             // h = x_o - x = -(dh + dl)
-                            ff wh = ff_mul(wx, ff{-dh[0], -dl[0]});
-                            wh = ff_add(wh, ff_mul(wy, ff{-dh[1], -dl[1]}));
-                            wh = ff_add(wh, ff_mul(wz, ff{-dh[2], -dl[2]}));
-                            acc[p] = ff_add(acc[p], ff_mul(k, wh));
+                            const ff wh = ff_dot3(wx, wy, wz, ff{-dh[0], -dl[0]}, ff{-dh[1], -dl[1]},
+                                                  ff{-dh[2], -dl[2]});
+                            ff_acc_fma(acc[p], k, wh);
+                        }
+                        if ((qr & 7) == 7) {  // fold the low words back every 8 records
+#pragma unroll
+                            for (int p = 0; p < PPT; ++p) ff_acc_norm(acc[p]);
                         }
                     }
                 } else {
@@ -538,17 +539,17 @@ __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const 
                             float dh[3], dl[3];
                             ff r2 = ff_dist2(X[p], ph, pl, dh, dl, eps2);
                             if (r2.h >= 1.f) continue;  // beyond the range: C = 0
-                            ff sr = ff_sqrt(r2);
-                            ff c = ff_add_f(ff_mul_f(r2, 0.75f), -3.5f);
-                            c = ff_horner(r2, c, 8.75f);
-                            c = ff_horner(sr, c, -7.f);
-                            c = ff_horner(r2, c, 1.f);
-                            acc[p] = ff_add(acc[p], ff_mul(c, W));
+                            const ff sr = ff_sqrt(r2);
+                            ff_acc_fma(acc[p], ff_cubic_C(r2, sr), W);
+                        }
+                        if ((qr & 7) == 7) {  // fold the low words back every 8 records
+#pragma unroll
+                            for (int p = 0; p < PPT; ++p) ff_acc_norm(acc[p]);
                         }
                     }
                 }
 #pragma unroll
-                for (int p = 0; p < PPT; ++p) Z[p] += ff_to_double(acc[p]);
+                for (int p = 0; p < PPT; ++p) Z[p] += ff_acc_to_double(acc[p]);
             }
             __syncthreads();
             if (item + 2 < n_items) issue(item + 2);

@@ -79,6 +79,79 @@ __device__ __forceinline__ ff ff_sqrt(ff a) {
 
 __device__ __forceinline__ double ff_to_double(ff a) { return (double)a.h + (double)a.l; }
 
+// ---------------------------------------------------------------------------
+// Cubic covariance in float-float, as polynomials of s = r / a (0 <= s < 1):
+//   C(s)         = 1 + s^2 (-7 + s (8.75 + s^2 (-3.5 + 0.75 s^2)))
+//   a^2 C'(r)/r  = -14 + s (26.25 + s^2 (-17.5 + 5.25 s^2))
+// In every Horner step c + x t of these two polynomials |x t| <= |c| holds on
+// 0 <= s <= 1 (each inner polynomial is monotone on [0, 1]; the bounds are
+// 0.75 <= 3.5, 3.5 <= 8.75, 6 <= 7, 1 - C(s) <= 1 and 5.25 <= 17.5,
+// 17.5 <= 26.25, 14 <= 14), so Fast2Sum(c, x t) is exact and replaces TwoSum.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ ff ff_horner_dom(ff x, ff t, float c) {
+    ff p = two_prod(x.h, t.h);
+    float e = __fmaf_rn(x.h, t.l, __fmaf_rn(x.l, t.h, p.l));
+    ff s = fast_two_sum(c, p.h);
+    return fast_two_sum(s.h, s.l + e);
+}
+
+// c + m x with |m x| <= |c| (the innermost step; m a float constant)
+__device__ __forceinline__ ff ff_lin_dom(ff x, float m, float c) {
+    ff p = two_prod(x.h, m);
+    float e = __fmaf_rn(x.l, m, p.l);
+    ff s = fast_two_sum(c, p.h);
+    return fast_two_sum(s.h, s.l + e);
+}
+
+__device__ __forceinline__ ff ff_cubic_C(ff s2, ff s) {
+    ff c = ff_lin_dom(s2, 0.75f, -3.5f);
+    c = ff_horner_dom(s2, c, 8.75f);
+    c = ff_horner_dom(s, c, -7.f);
+    return ff_horner_dom(s2, c, 1.f);
+}
+
+__device__ __forceinline__ ff ff_cubic_d1(ff s2, ff s) {
+    ff k = ff_lin_dom(s2, 5.25f, -17.5f);
+    k = ff_horner_dom(s2, k, 26.25f);
+    return ff_horner_dom(s, k, -14.f);
+}
+
+// Accumulator of float-float products: the high word is a running sum kept
+// exact by TwoSum, the low word collects the rounding errors in FP32 and is
+// folded back into the high word every few terms (ff_acc_norm), so it stays
+// within a few ulps of the high word's error and adds ~eps^2-level error.
+struct ffacc {
+    float h, l;
+};
+
+__device__ __forceinline__ void ff_acc_fma(ffacc& a, ff x, ff y) {
+    ff p = two_prod(x.h, y.h);
+    float e = __fmaf_rn(x.h, y.l, __fmaf_rn(x.l, y.h, p.l));
+    ff s = two_sum(a.h, p.h);
+    a.h = s.h;
+    a.l += s.l + e;
+}
+
+__device__ __forceinline__ void ff_acc_norm(ffacc& a) {
+    ff s = two_sum(a.h, a.l);
+    a.h = s.h;
+    a.l = s.l;
+}
+
+__device__ __forceinline__ double ff_acc_to_double(const ffacc& a) { return (double)a.h + (double)a.l; }
+
+// w . h for float-float 3-vectors: exact products and a TwoSum chain on the
+// high words, the low-order terms added in FP32.
+__device__ __forceinline__ ff ff_dot3(ff wx, ff wy, ff wz, ff hx, ff hy, ff hz) {
+    ff p0 = two_prod(wx.h, hx.h), p1 = two_prod(wy.h, hy.h), p2 = two_prod(wz.h, hz.h);
+    float e = __fmaf_rn(wx.h, hx.l, __fmaf_rn(wx.l, hx.h, p0.l));
+    e += __fmaf_rn(wy.h, hy.l, __fmaf_rn(wy.l, hy.h, p1.l));
+    e += __fmaf_rn(wz.h, hz.l, __fmaf_rn(wz.l, hz.h, p2.l));
+    ff s1 = two_sum(p0.h, p1.h);
+    ff s2 = two_sum(s1.h, p2.h);
+    return fast_two_sum(s2.h, s1.l + s2.l + e);
+}
+
 __device__ __forceinline__ ff ff_from_double(double x) {
     float h = (float)x;
     return {h, (float)(x - (double)h)};
