@@ -589,8 +589,8 @@ def plain_section():
     zm = np.asarray(sols["mixed"].raw_arrays.scalar_field_matrix)[0]
     out["errors"] = {"plain_vs_oracle_rel": float(np.abs(zp - z).max() / np.abs(z).max()),
                      "mixed_vs_plain_rel": float(np.abs(zm - zp).max() / np.abs(zp).max()),
-                     "ids_identical": bool(np.array_equal(sols["plain_fp64"].raw_arrays.lith_block,
-                                                          sols["mixed"].raw_arrays.lith_block))}
+                     "ids_identical": bool(np.array_equal(np.rint(sols["plain_fp64"].raw_arrays.lith_block),
+                                                          np.rint(sols["mixed"].raw_arrays.lith_block)))}
     out["speedup_vs_plain_fp64"] = out["plain_fp64"]["ms"] / out["mixed"]["ms"]
     out["speedup_plain_gpu_vs_cpu_oracle"] = t_cpu * 1e3 / out["plain_fp64"]["ms"]
     return out

@@ -534,6 +534,9 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchDesc* __rest
             ff_point(xd, inv_a, q, X[p]);
             Z[p] = 0.0;
         }
+        bool all_exact = true;
+#pragma unroll
+        for (int p = 0; p < kPPT; ++p) all_exact = all_exact && X[p].exact;
         for (int t = 0; t < nt; ++t) {
             const int sg = (int)(consumed & 1);
             const uint32_t parity = (uint32_t)((consumed >> 1) & 1);
@@ -577,50 +580,10 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchDesc* __rest
 #pragma unroll
             for (int p = 0; p < kPPT; ++p) acc[p] = {0.f, 0.f};
             const float* rec = reinterpret_cast<const float*>(stage[sg]);
-            if (t < to) {
-                const int nr = min(rec_ori, d.n_ori - t * rec_ori);
-                for (int qr = 0; qr < nr; ++qr) {
-                    const float4* R4 = reinterpret_cast<const float4*>(rec + 16 * qr);
-                    const float4 a0 = R4[0], a1 = R4[1], a2 = R4[2];
-                    const float ph[3] = {a0.x, a0.z, a1.x}, pl[3] = {a0.y, a0.w, a1.y};
-                    const ff wx = {a1.z, a1.w}, wy = {a2.x, a2.y}, wz = {a2.z, a2.w};
-#pragma unroll
-                    for (int p = 0; p < kPPT; ++p) {
-                        float dh[3], dl[3];
-                        ff r2 = ff_dist2(X[p], ph, pl, dh, dl, eps2);
-                        if (r2.h >= 1.f) continue;
-                        const ff sr = ff_sqrt(r2);
-                        const ff kk = ff_cubic_d1(r2, sr);
-                        const ff wh = ff_dot3(wx, wy, wz, ff{-dh[0], -dl[0]}, ff{-dh[1], -dl[1]},
-                                              ff{-dh[2], -dl[2]});
-                        ff_acc_fma(acc[p], kk, wh);
-                    }
-                    if ((qr & 7) == 7) {  // fold the low words back every 8 records
-#pragma unroll
-                        for (int p = 0; p < kPPT; ++p) ff_acc_norm(acc[p]);
-                    }
-                }
-            } else {
-                const int nr = min(rec_sp, d.n_sp - (t - to) * rec_sp);
-                for (int qr = 0; qr < nr; ++qr) {
-                    const float4* R4 = reinterpret_cast<const float4*>(rec + 8 * qr);
-                    const float4 a0 = R4[0], a1 = R4[1];
-                    const float ph[3] = {a0.x, a0.z, a1.x}, pl[3] = {a0.y, a0.w, a1.y};
-                    const ff W = {a1.z, a1.w};
-#pragma unroll
-                    for (int p = 0; p < kPPT; ++p) {
-                        float dh[3], dl[3];
-                        ff r2 = ff_dist2(X[p], ph, pl, dh, dl, eps2);
-                        if (r2.h >= 1.f) continue;
-                        const ff sr = ff_sqrt(r2);
-                        ff_acc_fma(acc[p], ff_cubic_C(r2, sr), W);
-                    }
-                    if ((qr & 7) == 7) {  // fold the low words back every 8 records
-#pragma unroll
-                        for (int p = 0; p < kPPT; ++p) ff_acc_norm(acc[p]);
-                    }
-                }
-            }
+            const bool ori = t < to;
+            const int nr = ori ? min(rec_ori, d.n_ori - t * rec_ori) : min(rec_sp, d.n_sp - (t - to) * rec_sp);
+            if (all_exact) ff_tile<kPPT, true>(rec, ori, nr, X, eps2, acc);
+            else ff_tile<kPPT, false>(rec, ori, nr, X, eps2, acc);
 #pragma unroll
             for (int p = 0; p < kPPT; ++p) Z[p] += ff_acc_to_double(acc[p]);
             __syncthreads();

@@ -69,12 +69,14 @@ __device__ __forceinline__ ff ff_horner(ff x, ff t, float c) {
 
 // sqrt of a non-negative float-float: one Newton correction of rsqrt-based
 // sqrt (the 2-ulp start squares to ~2^-44 relative error).
+// The result is left unnormalised (|lo| within a few ulps of hi): every user
+// reads it through exact products and sums.
 __device__ __forceinline__ ff ff_sqrt(ff a) {
     if (a.h <= 0.f) return {0.f, 0.f};
     float y = rsqrtf(a.h);
     float s = a.h * y;
     float e = __fmaf_rn(-s, s, a.h) + a.l;
-    return fast_two_sum(s, e * 0.5f * y);
+    return {s, e * 0.5f * y};
 }
 
 __device__ __forceinline__ double ff_to_double(ff a) { return (double)a.h + (double)a.l; }
@@ -88,11 +90,16 @@ __device__ __forceinline__ double ff_to_double(ff a) { return (double)a.h + (dou
 // 0.75 <= 3.5, 3.5 <= 8.75, 6 <= 7, 1 - C(s) <= 1 and 5.25 <= 17.5,
 // 17.5 <= 26.25, 14 <= 14), so Fast2Sum(c, x t) is exact and replaces TwoSum.
 // ---------------------------------------------------------------------------
+// The steps leave their result unnormalised (lo = exact Fast2Sum error plus
+// the product's low-order terms, within a few ulps of hi); the next step
+// reads both words through exact products.  The polynomial's variable (s^2,
+// s) is normalised, so the dropped product of the two low words stays at the
+// eps^2 level.
 __device__ __forceinline__ ff ff_horner_dom(ff x, ff t, float c) {
     ff p = two_prod(x.h, t.h);
     float e = __fmaf_rn(x.h, t.l, __fmaf_rn(x.l, t.h, p.l));
     ff s = fast_two_sum(c, p.h);
-    return fast_two_sum(s.h, s.l + e);
+    return {s.h, s.l + e};
 }
 
 // c + m x with |m x| <= |c| (the innermost step; m a float constant)
@@ -100,7 +107,7 @@ __device__ __forceinline__ ff ff_lin_dom(ff x, float m, float c) {
     ff p = two_prod(x.h, m);
     float e = __fmaf_rn(x.l, m, p.l);
     ff s = fast_two_sum(c, p.h);
-    return fast_two_sum(s.h, s.l + e);
+    return {s.h, s.l + e};
 }
 
 __device__ __forceinline__ ff ff_cubic_C(ff s2, ff s) {
@@ -149,12 +156,7 @@ __device__ __forceinline__ ff ff_dot3(ff wx, ff wy, ff wz, ff hx, ff hy, ff hz) 
     e += __fmaf_rn(wz.h, hz.l, __fmaf_rn(wz.l, hz.h, p2.l));
     ff s1 = two_sum(p0.h, p1.h);
     ff s2 = two_sum(s1.h, p2.h);
-    return fast_two_sum(s2.h, s1.l + s2.l + e);
-}
-
-__device__ __forceinline__ ff ff_from_double(double x) {
-    float h = (float)x;
-    return {h, (float)(x - (double)h)};
+    return {s2.h, s1.l + s2.l + e};   // unnormalised, read through exact products
 }
 
 // ---------------------------------------------------------------------------
@@ -194,12 +196,16 @@ __device__ __forceinline__ void ff_point(const double* xd, double inv_a, double 
 
 // r^2 + eps2 of d = x - p as float-float (eps2 is the distance regulariser
 // in the scaled frame, kDistEps2 / range^2); d_k = dh_k + dl_k with dh_k exact
-// when the split is exact, else recovered with a two-sum.
+// when the split is exact (EXACT: every point of the caller is), else
+// recovered with a two-sum.  The result is normalised: it is the variable of
+// the covariance polynomials, and an unnormalised variable's low word would
+// enter every Horner step (emulated: 3e-12 instead of 1e-13 per term).
+template <bool EXACT>
 __device__ __forceinline__ ff ff_dist2(const PointFF& X, const float* ph, const float* pl, float* dh, float* dl,
                                        float eps2) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        if (X.exact) {
+        if (EXACT) {
             dh[k] = X.h[k] - ph[k];
             dl[k] = X.l[k] - pl[k];
         } else {
@@ -216,6 +222,61 @@ __device__ __forceinline__ ff ff_dist2(const PointFF& X, const float* ph, const 
     low = __fmaf_rn(dl[1], 2.f * dh[1] + dl[1], low);
     low = __fmaf_rn(dl[2], 2.f * dh[2] + dl[2], low);
     return fast_two_sum(s2.h, low);
+}
+
+// One staged tile of float-float records against PPT points: orientation
+// records (16 floats: x, y, z hi/lo, then w_x, w_y, w_z hi/lo) add
+// C'/r(|x - x_o|) (w . (x_o - x)), surface-point records (8 floats: x, y, z
+// hi/lo, alpha hi/lo) add alpha C(|x - p|); coordinates are scaled by 1/range.
+// EXACT: every point's split is exact (the common case).
+template <int PPT, bool EXACT>
+__device__ __forceinline__ void ff_tile(const float* __restrict__ rec, bool orientation, int nr,
+                                        const PointFF (&X)[PPT], float eps2, ffacc (&acc)[PPT]) {
+    if (orientation) {
+        for (int qr = 0; qr < nr; ++qr) {
+            const float4* R4 = reinterpret_cast<const float4*>(rec + 16 * qr);
+            const float4 a0 = R4[0], a1 = R4[1], a2 = R4[2];
+            const float ph[3] = {a0.x, a0.z, a1.x}, pl[3] = {a0.y, a0.w, a1.y};
+            const ff wx = {a1.z, a1.w}, wy = {a2.x, a2.y}, wz = {a2.z, a2.w};
+#pragma unroll
+            for (int p = 0; p < PPT; ++p) {
+                float dh[3], dl[3];
+                const ff r2 = ff_dist2<EXACT>(X[p], ph, pl, dh, dl, eps2);
+                if (r2.h >= 1.f) continue;  // beyond the range: C'/r = 0
+                const ff k = ff_cubic_d1(r2, ff_sqrt(r2));
+                // h = x_o - x = -(dh + dl)
+                const ff wh = ff_dot3(wx, wy, wz, ff{-dh[0], -dl[0]}, ff{-dh[1], -dl[1]}, ff{-dh[2], -dl[2]});
+                ff_acc_fma(acc[p], k, wh);
+            }
+            if ((qr & 7) == 7) {  // fold the low words back every 8 records
+#pragma unroll
+                for (int p = 0; p < PPT; ++p) ff_acc_norm(acc[p]);
+            }
+        }
+    } else {
+        for (int qr = 0; qr < nr; ++qr) {
+            const float4* R4 = reinterpret_cast<const float4*>(rec + 8 * qr);
+            const float4 a0 = R4[0], a1 = R4[1];
+            const float ph[3] = {a0.x, a0.z, a1.x}, pl[3] = {a0.y, a0.w, a1.y};
+            const ff W = {a1.z, a1.w};
+#pragma unroll
+            for (int p = 0; p < PPT; ++p) {
+                float dh[3], dl[3];
+                const ff r2 = ff_dist2<EXACT>(X[p], ph, pl, dh, dl, eps2);
+                if (r2.h >= 1.f) continue;  // beyond the range: C = 0
+                ff_acc_fma(acc[p], ff_cubic_C(r2, ff_sqrt(r2)), W);
+            }
+            if ((qr & 7) == 7) {
+#pragma unroll
+                for (int p = 0; p < PPT; ++p) ff_acc_norm(acc[p]);
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ ff ff_from_double(double x) {
+    float h = (float)x;
+    return {h, (float)(x - (double)h)};
 }
 
 }  // namespace gk
