@@ -20,6 +20,7 @@ GK_MAX_SURFACES = 32
 GK_MAX_FAULTS = 16
 GK_TIE_TOL = 1e-9
 GK_NOALLOC_MAX_N = 1024
+GK_CTA_MAX_N = 4096
 GK_TUNE_EVAL_FF, GK_TUNE_EVAL_F32, GK_TUNE_BATCH_EVAL = 0, 1, 2
 TUNABLES = {"eval_ff": GK_TUNE_EVAL_FF, "eval_f32": GK_TUNE_EVAL_F32, "batch_eval": GK_TUNE_BATCH_EVAL}
 
@@ -74,6 +75,22 @@ class GkBatch(ctypes.Structure):
                 ("ref_index", ctypes.c_void_p), ("rest_index", ctypes.c_void_p)]
 
 
+GK_CTA_MAX_JOBS = 16
+
+
+class GkSeriesEval(ctypes.Structure):
+    _fields_ = [("sys", ctypes.POINTER(GkSystem)), ("model", ctypes.c_void_p), ("seg", GkSegment),
+                ("relation", ctypes.c_int32), ("n_faults", ctypes.c_int32),
+                ("faults", ctypes.c_int32 * GK_MAX_FAULTS), ("min_iso", ctypes.c_double),
+                ("max_iso", ctypes.c_double)]
+
+
+class GkCtaJob(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64), ("K", ctypes.c_void_p), ("ldk", ctypes.c_int64), ("b", ctypes.c_void_p),
+                ("x", ctypes.c_void_p), ("work", ctypes.c_void_p), ("work_bytes", ctypes.c_size_t),
+                ("info", ctypes.c_void_p)]
+
+
 GK_MLP_HIDDEN = 256
 GK_MLP_MAX_IN = 64
 GK_MLP_MAX_OUT = 16
@@ -112,6 +129,12 @@ SIGNATURES = [
     ("gk_solve_mixed_noalloc", ctypes.c_int, [ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                               ctypes.c_void_p, ctypes.c_double, ctypes.c_int32, ctypes.c_void_p,
                                               ctypes.c_void_p]),
+    ("gk_solve_mixed_cta_workspace_bytes", ctypes.c_size_t, [ctypes.c_int64, ctypes.c_int64]),
+    ("gk_solve_mixed_cta", ctypes.c_int, [ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.c_double, ctypes.c_int32, ctypes.c_void_p,
+                                          ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]),
+    ("gk_solve_mixed_cta_many", ctypes.c_int, [ctypes.c_int32, ctypes.POINTER(GkCtaJob), ctypes.c_double,
+                                               ctypes.c_int32, ctypes.c_void_p]),
     ("gk_solve_twolevel_workspace_bytes", ctypes.c_size_t, [ctypes.c_int64, ctypes.c_int]),
     ("gk_solve_twolevel", ctypes.c_int, [ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
@@ -124,6 +147,10 @@ SIGNATURES = [
     ("gk_eval", ctypes.c_int, [ctypes.POINTER(GkSystem), ctypes.c_void_p, ctypes.POINTER(GkPoints),
                                ctypes.c_int, ctypes.POINTER(GkSegment), ctypes.c_void_p, ctypes.c_void_p,
                                ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    ("gk_eval_series_set", ctypes.c_int, [ctypes.c_int32, ctypes.POINTER(GkSeriesEval), ctypes.POINTER(GkPoints),
+                                          ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_void_p]),
     ("gk_combine_series", ctypes.c_int, [ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
                                          ctypes.c_void_p, c_int32_p, c_double_p, c_double_p, ctypes.c_void_p,
                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),

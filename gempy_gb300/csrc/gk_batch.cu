@@ -164,18 +164,193 @@ __device__ void cta_gemv64(const double* K, int ld, int N, const double* x, cons
     __syncthreads();
 }
 
+// One system of the in-CTA mixed solve: K64 (FP64, read only), its FP32
+// equilibrated copy K32, the right-hand side b, the solution x and scratch.
+struct CtaSystem {
+    const double* K64;
+    int ld, N;
+    float* K32;
+    const double* b;
+    double* x;
+    double* dsc;
+    double* r;
+    double* w;
+    double* V;     // (restart + 1) x N
+    double* Z;     // restart x N
+    float* t32;
+};
+
+struct CtaSolveShared {
+    float Ds[kLNB][kLNB + 1];
+    double red[32];
+    float xs[kLNB];
+    int s_bad;
+    double H[(kBatchRestart + 1) * kBatchRestart];
+    double cs[kBatchRestart], sn[kBatchRestart], g[kBatchRestart + 1], yv[kBatchRestart];
+    double hcol[kBatchRestart + 2];
+};
+
+// The whole mixed solve of one system by the calling CTA: symmetric
+// equilibration, FP32 LU without pivoting, FGMRES(30) in FP64 preconditioned
+// by the FP32 factors with Givens rotations and convergence tests on the
+// device.  Returns the status, iteration count and final relative residual.
+__device__ void cta_mixed_solve(const CtaSystem& d, double tol, int max_iter, CtaSolveShared& sh, int& status_out,
+                                int& its_out, double& rel_out) {
+    auto& Ds = sh.Ds;
+    double* red = sh.red;
+    float* xs = sh.xs;
+    int& s_bad = sh.s_bad;
+    double* H = sh.H;
+    double* cs = sh.cs;
+    double* sn = sh.sn;
+    double* g = sh.g;
+    double* yv = sh.yv;
+    double* hcol = sh.hcol;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int N = d.N, ld = d.ld;
+    // equilibration and FP32 copy
+    {
+        const int lane = tid & 31, wid = tid >> 5;
+        for (int row = wid; row < N; row += nt >> 5) {
+            const double* k = d.K64 + (int64_t)row * ld;
+            double m = 0.0;
+            for (int j = lane; j < N; j += 32) m = fmax(m, fabs(k[j]));
+            for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+            if (lane == 0) d.dsc[row] = m > 0.0 ? 1.0 / sqrt(m) : 1.0;
+        }
+        __syncthreads();
+        for (int row = wid; row < N; row += nt >> 5) {
+            const double di = d.dsc[row];
+            const double* k = d.K64 + (int64_t)row * ld;
+            float* k32 = d.K32 + (int64_t)row * ld;
+            for (int j = lane; j < N; j += 32) k32[j] = (float)(di * k[j] * d.dsc[j]);
+        }
+        __syncthreads();
+    }
+    int status = GK_OK, its = 0;
+    double rel = 1.0;
+    if (!cta_lu_nopiv(d.K32, ld, N, Ds, &s_bad)) {
+        status = GK_ERR_SINGULAR;
+    } else {
+        // FGMRES(restart) in FP64
+        for (int i = tid; i < N; i += nt) d.x[i] = 0.0;
+        __syncthreads();
+        double bn = 0.0;
+        {
+            double s = 0.0;
+            for (int i = tid; i < N; i += nt) s += d.b[i] * d.b[i];
+            bn = sqrt(block_sum(s, red));
+        }
+        double prev = INFINITY;
+        status = GK_ERR_NOT_CONVERGED;
+        if (!(bn > 0.0)) { status = GK_OK; rel = 0.0; }
+        while (status == GK_ERR_NOT_CONVERGED && its < max_iter) {
+            cta_gemv64(d.K64, ld, N, d.x, d.b, d.r);
+            double s = 0.0;
+            for (int i = tid; i < N; i += nt) s += d.r[i] * d.r[i];
+            const double beta = sqrt(block_sum(s, red));
+            rel = beta / bn;
+            if (!(rel == rel)) { status = GK_ERR_NONFINITE; break; }
+            if (rel <= tol) { status = GK_OK; break; }
+            if (rel > 0.98 * prev) break;
+            prev = rel;
+            for (int i = tid; i < N; i += nt) d.V[i] = d.r[i] / beta;
+            if (tid == 0) { for (int q = 0; q <= kBatchRestart; ++q) g[q] = 0.0; g[0] = beta; }
+            __syncthreads();
+            int j = 0;
+            bool done = false;
+            for (; j < kBatchRestart && its < max_iter; ++j, ++its) {
+                const double* vj = d.V + (int64_t)j * N;
+                double* zj = d.Z + (int64_t)j * N;
+                for (int i = tid; i < N; i += nt) d.t32[i] = (float)(d.dsc[i] * vj[i]);
+                __syncthreads();
+                cta_lu_solve(d.K32, ld, N, d.t32, xs);
+                for (int i = tid; i < N; i += nt) zj[i] = d.dsc[i] * (double)d.t32[i];
+                __syncthreads();
+                cta_gemv64(d.K64, ld, N, zj, nullptr, d.w);
+                // CGS2: warp w computes the dot products c = w, w + 16, ...
+                for (int pass = 0; pass < 2; ++pass) {
+                    {
+                        const int lane = tid & 31, wid = tid >> 5;
+                        for (int c = wid; c <= j; c += nt >> 5) {
+                            const double* vc = d.V + (int64_t)c * N;
+                            double sd = 0.0;
+                            for (int i = lane; i < N; i += 32) sd = fma(vc[i], d.w[i], sd);
+                            for (int o = 16; o > 0; o >>= 1) sd += __shfl_down_sync(0xffffffffu, sd, o);
+                            if (lane == 0) {
+                                yv[c] = sd;
+                                hcol[c] = (pass == 0 ? 0.0 : hcol[c]) + sd;
+                            }
+                        }
+                    }
+                    __syncthreads();
+                    for (int i = tid; i < N; i += nt) {
+                        double v = d.w[i];
+                        for (int c = 0; c <= j; ++c) v -= d.V[(int64_t)c * N + i] * yv[c];
+                        d.w[i] = v;
+                    }
+                    __syncthreads();
+                }
+                double sn2 = 0.0;
+                for (int i = tid; i < N; i += nt) sn2 += d.w[i] * d.w[i];
+                const double hn = sqrt(block_sum(sn2, red));
+                if (hn > 0.0)
+                    for (int i = tid; i < N; i += nt) d.V[(int64_t)(j + 1) * N + i] = d.w[i] / hn;
+                if (tid == 0) {
+                    hcol[j + 1] = hn;
+                    for (int i = 0; i < j; ++i) {
+                        double t = cs[i] * hcol[i] + sn[i] * hcol[i + 1];
+                        hcol[i + 1] = -sn[i] * hcol[i] + cs[i] * hcol[i + 1];
+                        hcol[i] = t;
+                    }
+                    double den = hypot(hcol[j], hcol[j + 1]);
+                    cs[j] = den > 0 ? hcol[j] / den : 1.0;
+                    sn[j] = den > 0 ? hcol[j + 1] / den : 0.0;
+                    hcol[j] = den;
+                    g[j + 1] = -sn[j] * g[j];
+                    g[j] = cs[j] * g[j];
+                    for (int i = 0; i <= j; ++i) H[i * kBatchRestart + j] = hcol[i];
+                    red[31] = (fabs(g[j + 1]) <= tol * bn || hn == 0.0) ? 1.0 : 0.0;
+                }
+                __syncthreads();
+                if (red[31] != 0.0) { ++j; ++its; done = true; break; }
+            }
+            (void)done;
+            if (tid == 0) {
+                for (int i = j - 1; i >= 0; --i) {
+                    double t = g[i];
+                    for (int q = i + 1; q < j; ++q) t -= H[i * kBatchRestart + q] * yv[q];
+                    yv[i] = H[i * kBatchRestart + i] != 0.0 ? t / H[i * kBatchRestart + i] : 0.0;
+                }
+            }
+            __syncthreads();
+            for (int i = tid; i < N; i += nt) {
+                double v = d.x[i];
+                for (int c = 0; c < j; ++c) v += d.Z[(int64_t)c * N + i] * yv[c];
+                d.x[i] = v;
+            }
+            __syncthreads();
+        }
+        if (status == GK_ERR_NOT_CONVERGED) {
+            cta_gemv64(d.K64, ld, N, d.x, d.b, d.r);
+            double s = 0.0;
+            for (int i = tid; i < N; i += nt) s += d.r[i] * d.r[i];
+            rel = sqrt(block_sum(s, red)) / bn;
+            if (rel <= tol) status = GK_OK;
+        }
+    }
+    status_out = status;
+    its_out = its;
+    rel_out = rel;
+}
+
 __global__ void __launch_bounds__(kSolveThreads) batch_solve_kernel(const BatchDesc* __restrict__ D, int n_sys,
                                                                     const int32_t* __restrict__ order,
                                                                     int* counter, double tol, int max_iter,
                                                                     gk_info* infos) {
-    __shared__ float Ds[kLNB][kLNB + 1];
-    __shared__ double red[32];
-    __shared__ float xs[kLNB];
-    __shared__ int s_sys, s_bad;
-    __shared__ double H[(kBatchRestart + 1) * kBatchRestart];
-    __shared__ double cs[kBatchRestart], sn[kBatchRestart], g[kBatchRestart + 1], yv[kBatchRestart];
-    __shared__ double hcol[kBatchRestart + 2];
-    const int tid = threadIdx.x, nt = blockDim.x;
+    __shared__ CtaSolveShared sh;
+    __shared__ int s_sys;
+    const int tid = threadIdx.x;
     while (true) {
         if (tid == 0) {
             int k = atomicAdd(counter, 1);
@@ -184,139 +359,11 @@ __global__ void __launch_bounds__(kSolveThreads) batch_solve_kernel(const BatchD
         __syncthreads();
         const int sys = s_sys;
         if (sys < 0) return;
-        const BatchDesc& d = D[sys];
-        const int N = d.N, ld = d.ld;
-        // equilibration and FP32 copy
-        {
-            const int lane = tid & 31, wid = tid >> 5;
-            for (int row = wid; row < N; row += nt >> 5) {
-                const double* k = d.K64 + (int64_t)row * ld;
-                double m = 0.0;
-                for (int j = lane; j < N; j += 32) m = fmax(m, fabs(k[j]));
-                for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
-                if (lane == 0) d.dsc[row] = m > 0.0 ? 1.0 / sqrt(m) : 1.0;
-            }
-            __syncthreads();
-            for (int row = wid; row < N; row += nt >> 5) {
-                const double di = d.dsc[row];
-                const double* k = d.K64 + (int64_t)row * ld;
-                float* k32 = d.K32 + (int64_t)row * ld;
-                for (int j = lane; j < N; j += 32) k32[j] = (float)(di * k[j] * d.dsc[j]);
-            }
-            __syncthreads();
-        }
-        int status = GK_OK, its = 0;
-        double rel = 1.0;
-        if (!cta_lu_nopiv(d.K32, ld, N, Ds, &s_bad)) {
-            status = GK_ERR_SINGULAR;
-        } else {
-            // FGMRES(restart) in FP64
-            for (int i = tid; i < N; i += nt) d.x[i] = 0.0;
-            __syncthreads();
-            double bn = 0.0;
-            {
-                double s = 0.0;
-                for (int i = tid; i < N; i += nt) s += d.b[i] * d.b[i];
-                bn = sqrt(block_sum(s, red));
-            }
-            double prev = INFINITY;
-            status = GK_ERR_NOT_CONVERGED;
-            if (!(bn > 0.0)) { status = GK_OK; rel = 0.0; }
-            while (status == GK_ERR_NOT_CONVERGED && its < max_iter) {
-                cta_gemv64(d.K64, ld, N, d.x, d.b, d.r);
-                double s = 0.0;
-                for (int i = tid; i < N; i += nt) s += d.r[i] * d.r[i];
-                const double beta = sqrt(block_sum(s, red));
-                rel = beta / bn;
-                if (!(rel == rel)) { status = GK_ERR_NONFINITE; break; }
-                if (rel <= tol) { status = GK_OK; break; }
-                if (rel > 0.98 * prev) break;
-                prev = rel;
-                for (int i = tid; i < N; i += nt) d.V[i] = d.r[i] / beta;
-                if (tid == 0) { for (int q = 0; q <= kBatchRestart; ++q) g[q] = 0.0; g[0] = beta; }
-                __syncthreads();
-                int j = 0;
-                bool done = false;
-                for (; j < kBatchRestart && its < max_iter; ++j, ++its) {
-                    const double* vj = d.V + (int64_t)j * N;
-                    double* zj = d.Z + (int64_t)j * N;
-                    for (int i = tid; i < N; i += nt) d.t32[i] = (float)(d.dsc[i] * vj[i]);
-                    __syncthreads();
-                    cta_lu_solve(d.K32, ld, N, d.t32, xs);
-                    for (int i = tid; i < N; i += nt) zj[i] = d.dsc[i] * (double)d.t32[i];
-                    __syncthreads();
-                    cta_gemv64(d.K64, ld, N, zj, nullptr, d.w);
-                    // CGS2: warp w computes the dot products c = w, w + 16, ...
-                    for (int pass = 0; pass < 2; ++pass) {
-                        {
-                            const int lane = tid & 31, wid = tid >> 5;
-                            for (int c = wid; c <= j; c += nt >> 5) {
-                                const double* vc = d.V + (int64_t)c * N;
-                                double sd = 0.0;
-                                for (int i = lane; i < N; i += 32) sd = fma(vc[i], d.w[i], sd);
-                                for (int o = 16; o > 0; o >>= 1) sd += __shfl_down_sync(0xffffffffu, sd, o);
-                                if (lane == 0) {
-                                    yv[c] = sd;
-                                    hcol[c] = (pass == 0 ? 0.0 : hcol[c]) + sd;
-                                }
-                            }
-                        }
-                        __syncthreads();
-                        for (int i = tid; i < N; i += nt) {
-                            double v = d.w[i];
-                            for (int c = 0; c <= j; ++c) v -= d.V[(int64_t)c * N + i] * yv[c];
-                            d.w[i] = v;
-                        }
-                        __syncthreads();
-                    }
-                    double sn2 = 0.0;
-                    for (int i = tid; i < N; i += nt) sn2 += d.w[i] * d.w[i];
-                    const double hn = sqrt(block_sum(sn2, red));
-                    if (hn > 0.0)
-                        for (int i = tid; i < N; i += nt) d.V[(int64_t)(j + 1) * N + i] = d.w[i] / hn;
-                    if (tid == 0) {
-                        hcol[j + 1] = hn;
-                        for (int i = 0; i < j; ++i) {
-                            double t = cs[i] * hcol[i] + sn[i] * hcol[i + 1];
-                            hcol[i + 1] = -sn[i] * hcol[i] + cs[i] * hcol[i + 1];
-                            hcol[i] = t;
-                        }
-                        double den = hypot(hcol[j], hcol[j + 1]);
-                        cs[j] = den > 0 ? hcol[j] / den : 1.0;
-                        sn[j] = den > 0 ? hcol[j + 1] / den : 0.0;
-                        hcol[j] = den;
-                        g[j + 1] = -sn[j] * g[j];
-                        g[j] = cs[j] * g[j];
-                        for (int i = 0; i <= j; ++i) H[i * kBatchRestart + j] = hcol[i];
-                        red[31] = (fabs(g[j + 1]) <= tol * bn || hn == 0.0) ? 1.0 : 0.0;
-                    }
-                    __syncthreads();
-                    if (red[31] != 0.0) { ++j; ++its; done = true; break; }
-                }
-                (void)done;
-                if (tid == 0) {
-                    for (int i = j - 1; i >= 0; --i) {
-                        double t = g[i];
-                        for (int q = i + 1; q < j; ++q) t -= H[i * kBatchRestart + q] * yv[q];
-                        yv[i] = H[i * kBatchRestart + i] != 0.0 ? t / H[i * kBatchRestart + i] : 0.0;
-                    }
-                }
-                __syncthreads();
-                for (int i = tid; i < N; i += nt) {
-                    double v = d.x[i];
-                    for (int c = 0; c < j; ++c) v += d.Z[(int64_t)c * N + i] * yv[c];
-                    d.x[i] = v;
-                }
-                __syncthreads();
-            }
-            if (status == GK_ERR_NOT_CONVERGED) {
-                cta_gemv64(d.K64, ld, N, d.x, d.b, d.r);
-                double s = 0.0;
-                for (int i = tid; i < N; i += nt) s += d.r[i] * d.r[i];
-                rel = sqrt(block_sum(s, red)) / bn;
-                if (rel <= tol) status = GK_OK;
-            }
-        }
+        const BatchDesc& bd = D[sys];
+        const CtaSystem d{bd.K64, bd.ld, bd.N, bd.K32, bd.b, bd.x, bd.dsc, bd.r, bd.w, bd.V, bd.Z, bd.t32};
+        int status, its;
+        double rel;
+        cta_mixed_solve(d, tol, max_iter, sh, status, its, rel);
         if (tid == 0 && infos != nullptr) {
             infos[sys].status = status;
             infos[sys].where = 0;
@@ -325,6 +372,29 @@ __global__ void __launch_bounds__(kSolveThreads) batch_solve_kernel(const BatchD
             infos[sys].residual = rel;
         }
         __syncthreads();
+    }
+}
+
+// Independent systems, one CTA each (systems passed by value).
+constexpr int kCtaJobs = GK_CTA_MAX_JOBS;
+struct CtaJobs {
+    CtaSystem sys[kCtaJobs];
+    gk_info* info[kCtaJobs];
+};
+
+__global__ void __launch_bounds__(kSolveThreads) mixed_cta_kernel(const __grid_constant__ CtaJobs jobs, double tol,
+                                                                  int max_iter) {
+    __shared__ CtaSolveShared sh;
+    int status, its;
+    double rel;
+    cta_mixed_solve(jobs.sys[blockIdx.x], tol, max_iter, sh, status, its, rel);
+    gk_info* info = jobs.info[blockIdx.x];
+    if (threadIdx.x == 0 && info != nullptr) {
+        info->status = status;
+        info->where = 0;
+        info->iterations = its;
+        info->pivoted = 0;
+        info->residual = rel;
     }
 }
 
@@ -534,9 +604,13 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchDesc* __rest
             ff_point(xd, inv_a, q, X[p]);
             Z[p] = 0.0;
         }
-        bool all_exact = true;
+        bool all_exact = true, act[kPPT], any_act = false;
 #pragma unroll
-        for (int p = 0; p < kPPT; ++p) all_exact = all_exact && X[p].exact;
+        for (int p = 0; p < kPPT; ++p) {
+            act[p] = pid[p] < d.n_points;
+            all_exact = all_exact && (X[p].exact || !act[p]);
+            any_act = any_act || act[p];
+        }
         for (int t = 0; t < nt; ++t) {
             const int sg = (int)(consumed & 1);
             const uint32_t parity = (uint32_t)((consumed >> 1) & 1);
@@ -582,8 +656,12 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchDesc* __rest
             const float* rec = reinterpret_cast<const float*>(stage[sg]);
             const bool ori = t < to;
             const int nr = ori ? min(rec_ori, d.n_ori - t * rec_ori) : min(rec_sp, d.n_sp - (t - to) * rec_sp);
-            if (all_exact) ff_tile<kPPT, true>(rec, ori, nr, X, eps2, acc);
-            else ff_tile<kPPT, false>(rec, ori, nr, X, eps2, acc);
+            if (!any_act) {
+            } else if (all_exact) {
+                ff_tile<kPPT, true>(rec, ori, nr, X, act, eps2, acc);
+            } else {
+                ff_tile<kPPT, false>(rec, ori, nr, X, act, eps2, acc);
+            }
 #pragma unroll
             for (int p = 0; p < kPPT; ++p) Z[p] += ff_acc_to_double(acc[p]);
             __syncthreads();
@@ -794,10 +872,11 @@ static gk_status launch_batch_eval(const BatchDesc* D, int n, const int64_t* chu
                                    double* values, int32_t* ids, gk_info* infos, int sms, cudaStream_t s) {
     auto k = batch_eval_kernel<PPT, STAGE>;
     const size_t smem = 2 * (size_t)STAGE;
-    GK_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int occ = 0;
-    GK_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, 256, smem));
-    if (occ < 1) occ = 1;
+    int occ = 1;
+    {
+        const gk_status st = cached_occupancy((const void*)k, 256, smem, occ);
+        if (st != GK_OK) return st;
+    }
     k<<<sms * occ, 256, smem, s>>>(D, n, chunk_prefix, field, values, ids, infos);
     GK_LAUNCH_CHECK();
     return GK_OK;
@@ -859,4 +938,61 @@ extern "C" gk_status gk_batch_results(const gk_batch* b, const void* work, size_
         GK_CUDA_TRY(cudaMemcpyAsync(isovalues, d.iso + GK_MAX_SURFACES, d.n_surf * sizeof(double),
                                     cudaMemcpyDeviceToDevice, s));
     return GK_OK;
+}
+
+// ---------------------------------------------------------------------------
+// single-system mixed solve in one CTA
+// ---------------------------------------------------------------------------
+static size_t cta_ws_layout(int64_t n, int64_t ld, size_t* off) {
+    size_t o = 0;
+    off[0] = o; o += al256((size_t)n * ld * sizeof(float));                     // K32
+    off[1] = o; o += al256((size_t)n * sizeof(double));                          // dsc
+    off[2] = o; o += al256((size_t)n * sizeof(double));                          // r
+    off[3] = o; o += al256((size_t)n * sizeof(double));                          // w
+    off[4] = o; o += al256((size_t)(kBatchRestart + 1) * n * sizeof(double));    // V
+    off[5] = o; o += al256((size_t)kBatchRestart * n * sizeof(double));          // Z
+    off[6] = o; o += al256((size_t)n * sizeof(float));                           // t32
+    return o;
+}
+
+extern "C" size_t gk_solve_mixed_cta_workspace_bytes(int64_t n, int64_t ldk) {
+    if (n < 1 || n > GK_CTA_MAX_N || ldk < n) return 0;
+    size_t off[7];
+    return cta_ws_layout(n, ldk, off);
+}
+
+static gk_status cta_job(const gk_cta_job& j, CtaSystem& d) {
+    if (j.n < 1 || j.K == nullptr || j.b == nullptr || j.x == nullptr || j.ldk < j.n) return GK_ERR_ARG;
+    if (j.n > GK_CTA_MAX_N) return GK_ERR_SIZE;
+    size_t off[7];
+    const size_t need = cta_ws_layout(j.n, j.ldk, off);
+    if (j.work == nullptr || j.work_bytes < need) return GK_ERR_SIZE;
+    char* w = (char*)j.work;
+    d = CtaSystem{j.K, (int)j.ldk, (int)j.n, (float*)(w + off[0]), j.b, j.x, (double*)(w + off[1]),
+                  (double*)(w + off[2]), (double*)(w + off[3]), (double*)(w + off[4]), (double*)(w + off[5]),
+                  (float*)(w + off[6])};
+    return GK_OK;
+}
+
+extern "C" gk_status gk_solve_mixed_cta_many(int32_t n_jobs, const gk_cta_job* jobs, double tol, int32_t max_iter,
+                                             gk_stream stream) {
+    if (n_jobs < 1 || jobs == nullptr || max_iter < 1 || !(tol > 0.0)) return GK_ERR_ARG;
+    if (n_jobs > kCtaJobs) return GK_ERR_SIZE;
+    CtaJobs J;
+    memset(&J, 0, sizeof(J));
+    for (int i = 0; i < n_jobs; ++i) {
+        gk_status st = cta_job(jobs[i], J.sys[i]);
+        if (st != GK_OK) return st;
+        J.info[i] = jobs[i].info;
+    }
+    mixed_cta_kernel<<<n_jobs, kSolveThreads, 0, (cudaStream_t)stream>>>(J, tol, max_iter);
+    GK_LAUNCH_CHECK();
+    return GK_OK;
+}
+
+extern "C" gk_status gk_solve_mixed_cta(int64_t n, const double* K, int64_t ldk, const double* b, double* x,
+                                        double tol, int32_t max_iter, void* work, size_t work_bytes, gk_info* info,
+                                        gk_stream stream) {
+    gk_cta_job j{n, K, ldk, b, x, work, work_bytes, info};
+    return gk_solve_mixed_cta_many(1, &j, tol, max_iter, stream);
 }

@@ -6,6 +6,9 @@
 #include <stdint.h>
 
 #include <atomic>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 #include "../../include/gempy_gb300.h"
 
@@ -188,10 +191,81 @@ struct GridBarrier {
 };
 
 inline int device_sm_count() {
+    static std::atomic<int> cache[64];
     int dev = 0, n = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return kSMs;
-    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return kSMs;
-    return n > 0 ? n : kSMs;
+    if (dev >= 0 && dev < 64 && (n = cache[dev].load(std::memory_order_relaxed)) > 0) return n;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) return kSMs;
+    if (dev >= 0 && dev < 64) cache[dev].store(n, std::memory_order_relaxed);
+    return n;
+}
+
+// Resident CTAs per SM of ``kernel`` at ``threads`` threads and ``smem`` bytes
+// of dynamic shared memory; computed once per (kernel, threads, smem, device)
+// and cached, so launches of small point sets do not pay the runtime queries
+// each time.  The kernel's dynamic shared-memory limit is only ever raised
+// (to the largest size requested so far on the device), so every cached
+// configuration stays launchable.
+inline gk_status cached_occupancy(const void* kernel, int threads, size_t smem, int& occ) {
+    static std::mutex mu;
+    static std::map<std::tuple<const void*, int, size_t, int>, int> table;
+    static std::map<std::pair<const void*, int>, size_t> limit;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return GK_ERR_CUDA;
+    const auto key = std::make_tuple(kernel, threads, smem, dev);
+    std::lock_guard<std::mutex> g(mu);
+    auto it = table.find(key);
+    if (it != table.end()) {
+        occ = it->second;
+        return GK_OK;
+    }
+    size_t& lim = limit[std::make_pair(kernel, dev)];
+    if (smem > lim) {
+        if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+            return GK_ERR_CUDA;
+        lim = smem;
+    }
+    int o = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kernel, threads, smem) != cudaSuccess) return GK_ERR_CUDA;
+    occ = o < 1 ? 1 : o;
+    table[key] = occ;
+    return GK_OK;
+}
+
+// Whether clusters of `size` CTAs of `kernel` (threads, smem bytes of dynamic
+// shared memory each) can be scheduled on the device; cached.  Sizes above 8
+// are opted into on the kernel first.  Call after cached_occupancy with the
+// same smem, which raises the kernel's shared-memory limit.
+inline bool cached_cluster_fits(const void* kernel, int threads, size_t smem, int size) {
+    static std::mutex mu;
+    static std::map<std::tuple<const void*, int, size_t, int, int>, bool> table;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    const auto key = std::make_tuple(kernel, threads, smem, size, dev);
+    std::lock_guard<std::mutex> g(mu);
+    auto it = table.find(key);
+    if (it != table.end()) return it->second;
+    bool ok = true;
+    if (size > 8 && cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
+        ok = false;
+    if (ok) {
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = (unsigned)size;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.gridDim = dim3((unsigned)size);
+        cfg.blockDim = dim3((unsigned)threads);
+        cfg.dynamicSmemBytes = smem;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int nc = 0;
+        ok = cudaOccupancyMaxActiveClusters(&nc, kernel, &cfg) == cudaSuccess && nc > 0;
+    }
+    if (!ok) (void)cudaGetLastError();
+    table[key] = ok;
+    return ok;
 }
 
 }  // namespace gk

@@ -12,6 +12,9 @@
 // Grid coordinates of regular grids are generated in the kernel.  In FP32 mode
 // the per-tile partial sums are FP32 and are added into FP64 accumulators once
 // per tile; the drift, the segmentation thresholds and the outputs are FP64.
+#include <cooperative_groups.h>
+
+#include <algorithm>
 #include <cstring>
 
 #include "gk_common.cuh"
@@ -178,13 +181,13 @@ struct EvalParams {
     const double* xyz;
     int n_ori, n_sp, n_drift, degree, kernel, n_fault;
     double range;
-    const double* fault_values;  // n_fault x fault_ld
-    int64_t fault_ld;
+    const double* fault_rows[GK_MAX_FAULTS];  // block of each offsetting fault at the points
     const void* ori;   // packed records in T
     const void* sp;
     const double* mu;
     int tiles_ori, tiles_sp, rec_ori, rec_sp;  // records per tile
     int stage_bytes;
+    int split;         // CTAs of one cluster sharing a chunk of points (1: no cluster)
     int has_seg;
     gk_segment seg;
     double* field;
@@ -214,7 +217,7 @@ template <> __device__ __forceinline__ float sigm<float>(double t) {
 // Fault-drift contribution at point i: sum_f nu_f F_f(x_i).
 __device__ __forceinline__ double fault_term(const EvalParams& P, int64_t i) {
     double z = 0.0;
-    for (int f = 0; f < P.n_fault; ++f) z += P.mu[kFaultSlot + f] * P.fault_values[f * P.fault_ld + i];
+    for (int f = 0; f < P.n_fault; ++f) z += P.mu[kFaultSlot + f] * P.fault_rows[f][i];
     return z;
 }
 
@@ -227,27 +230,124 @@ __device__ __forceinline__ int32_t block_id(const gk_segment& S, double z) {
     return (int32_t)rint(v);
 }
 
-template <typename T, int PPT, bool GRAD>
+__device__ __forceinline__ void point_coords(const EvalParams& P, int64_t q, double* xd) {
+    if (P.kind == 0) {
+        const int64_t nyz = (int64_t)P.dims[1] * P.dims[2];
+        const int64_t ix = q / nyz, rem = q - ix * nyz;
+        const int64_t iy = rem / P.dims[2], iz = rem - iy * P.dims[2];
+        xd[0] = P.origin[0] + (double)ix * P.spacing[0];
+        xd[1] = P.origin[1] + (double)iy * P.spacing[1];
+        xd[2] = P.origin[2] + (double)iz * P.spacing[2];
+    } else {
+        xd[0] = P.xyz[3 * q];
+        xd[1] = P.xyz[3 * q + 1];
+        xd[2] = P.xyz[3 * q + 2];
+    }
+}
+
+// Outputs of point i from the covariance sums z (and gradient sums g, or
+// NULL): drift, fault drift, field, gradient, sigmoid segmentation and ids.
+// Ts is the type the sigmoid is computed in.
+template <typename Ts>
+__device__ __forceinline__ void finish_point(const EvalParams& P, int64_t i, const double* xd, double z,
+                                             const double* g) {
+    const double* mu = P.mu;
+    const double X = xd[0], Y = xd[1], Zc = xd[2];
+    if (P.n_drift >= 3) z += mu[0] * X + mu[1] * Y + mu[2] * Zc;
+    if (P.n_drift >= 9)
+        z += mu[3] * X * X + mu[4] * Y * Y + mu[5] * Zc * Zc + mu[6] * X * Y + mu[7] * X * Zc + mu[8] * Y * Zc;
+    if (P.n_fault) z += fault_term(P, i);
+    if (P.field) P.field[i] = z;
+    if (g != nullptr && P.grad) {
+        double gx = g[0], gy = g[1], gz = g[2];
+        if (P.n_drift >= 3) { gx += mu[0]; gy += mu[1]; gz += mu[2]; }
+        if (P.n_drift >= 9) {
+            gx += 2.0 * mu[3] * X + mu[6] * Y + mu[7] * Zc;
+            gy += 2.0 * mu[4] * Y + mu[6] * X + mu[8] * Zc;
+            gz += 2.0 * mu[5] * Zc + mu[7] * X + mu[8] * Y;
+        }
+        P.grad[3 * i] = gx;
+        P.grad[3 * i + 1] = gy;
+        P.grad[3 * i + 2] = gz;
+    }
+    if (P.has_seg) {
+        double v = P.seg.unit_values[0];
+        for (int k = 0; k < P.seg.n_surf; ++k)
+            v += (P.seg.unit_values[k + 1] - P.seg.unit_values[k]) *
+                 (double)sigm<Ts>(P.seg.slope * (P.seg.isovalues[k] - z));
+        if (P.values) P.values[i] = v;
+        if (P.ids) P.ids[i] = block_id(P.seg, z);
+    }
+}
+
+// Record split.  When the chunks of points would fill less than half of the
+// GPU, `split` CTAs of one thread-block cluster share each chunk: rank r
+// streams record tiles r, r + split, r + 2 split, ... and leaves its partial
+// sums in shared memory (`red`, NV values per point slot).  Past a cluster
+// barrier every CTA adds the partials of all ranks in rank order through
+// distributed shared memory -- the result does not depend on scheduling -- and
+// finishes its share of the chunk's points; a second barrier keeps the
+// partials alive until every rank has read them.  A CTA whose copy wait gave
+// up sets the abort word of every CTA of its cluster before the first barrier,
+// so the whole cluster passes the same barriers and stops together.
+namespace cg = cooperative_groups;
+
+template <typename Ts, int NV>
+__device__ __forceinline__ bool split_finish(const EvalParams& P, int64_t chunk, int64_t chunk_pts, int rank,
+                                             double* red, int* s_abort, bool failed) {
+    cg::cluster_group cl = cg::this_cluster();
+    if (failed && threadIdx.x == 0)
+        for (int r = 0; r < P.split; ++r) *cl.map_shared_rank(s_abort, r) = 1;
+    cl.sync();
+    const bool aborted = *(volatile int*)s_abort != 0;
+    if (!aborted) {
+        for (int64_t f = (int64_t)rank * blockDim.x + threadIdx.x; f < chunk_pts; f += (int64_t)P.split * blockDim.x) {
+            const int64_t i = chunk * chunk_pts + f;
+            if (i >= P.n) continue;
+            double v[NV];
+#pragma unroll
+            for (int c = 0; c < NV; ++c) v[c] = 0.0;
+            for (int r = 0; r < P.split; ++r) {
+                const double* rr = cl.map_shared_rank(red, r);
+#pragma unroll
+                for (int c = 0; c < NV; ++c) v[c] += rr[c * chunk_pts + f];
+            }
+            double xd[3];
+            point_coords(P, i, xd);
+            finish_point<Ts>(P, i, xd, v[0], NV == 4 ? v + 1 : nullptr);
+        }
+    }
+    cl.sync();
+    return aborted;
+}
+
+template <typename T, int PPT, bool GRAD, bool SPLIT>
 __global__ void __launch_bounds__(256) eval_kernel(const EvalParams P) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t mbar[2];
-    __shared__ int s_fail;
+    __shared__ int s_fail, s_abort;
     const int tid = threadIdx.x;
+    const int split = SPLIT ? P.split : 1;
     unsigned char* stage[2] = {smem, smem + P.stage_bytes};
     if (tid == 0) {
         mbar_init(&mbar[0], 1);
         mbar_init(&mbar[1], 1);
         mbar_fence_init();
         s_fail = 0;
+        s_abort = 0;
     }
     __syncthreads();
+    if (SPLIT) cg::this_cluster().sync();  // abort words initialised before any peer can set one
 
     const Cov<T> cv = Cov<T>::make(P.kernel, P.range);
     const int64_t chunk_pts = (int64_t)blockDim.x * PPT;
     const int64_t n_chunks = (P.n + chunk_pts - 1) / chunk_pts;
     const int n_tiles = P.tiles_ori + P.tiles_sp;
-    const int64_t my_chunks = n_chunks > blockIdx.x ? (n_chunks - 1 - blockIdx.x) / gridDim.x + 1 : 0;
-    const int64_t n_items = my_chunks * n_tiles;
+    const int rank = SPLIT ? (int)cg::this_cluster().block_rank() : 0;
+    const int64_t group = blockIdx.x / split, n_groups = gridDim.x / split;
+    const int my_tiles = n_tiles > rank ? (n_tiles - 1 - rank) / split + 1 : 0;
+    const int64_t my_chunks = n_chunks > group ? (n_chunks - 1 - group) / n_groups + 1 : 0;
+    const int64_t n_items = my_chunks * my_tiles;
 
     auto tile_src = [&](int t, uint32_t& bytes) -> const void* {
         if (t < P.tiles_ori) {
@@ -265,7 +365,7 @@ __global__ void __launch_bounds__(256) eval_kernel(const EvalParams P) {
     auto issue = [&](int64_t item) {
         if (tid != 0) return;
         int s = (int)(item & 1);
-        int t = (int)(item % n_tiles);
+        int t = rank + (int)(item % my_tiles) * split;
         uint32_t bytes;
         const void* src = tile_src(t, bytes);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -277,33 +377,27 @@ __global__ void __launch_bounds__(256) eval_kernel(const EvalParams P) {
 
     int64_t item = 0;
     for (int64_t lc = 0; lc < my_chunks; ++lc) {
-        const int64_t chunk = blockIdx.x + lc * gridDim.x;
+        const int64_t chunk = group + lc * n_groups;
         T x[PPT][3];
         double xd[PPT][3];
         int64_t pid[PPT];
+        bool act[PPT];   // slots past the end of the point list compute nothing
 #pragma unroll
         for (int p = 0; p < PPT; ++p) {
             pid[p] = chunk * chunk_pts + tid + (int64_t)p * blockDim.x;
-            int64_t q = pid[p] < P.n ? pid[p] : P.n - 1;
-            if (P.kind == 0) {
-                int64_t nyz = (int64_t)P.dims[1] * P.dims[2];
-                int64_t ix = q / nyz, rem = q - ix * nyz;
-                int64_t iy = rem / P.dims[2], iz = rem - iy * P.dims[2];
-                xd[p][0] = P.origin[0] + (double)ix * P.spacing[0];
-                xd[p][1] = P.origin[1] + (double)iy * P.spacing[1];
-                xd[p][2] = P.origin[2] + (double)iz * P.spacing[2];
-            } else {
-                xd[p][0] = P.xyz[3 * q];
-                xd[p][1] = P.xyz[3 * q + 1];
-                xd[p][2] = P.xyz[3 * q + 2];
-            }
+            act[p] = pid[p] < P.n;
+            point_coords(P, act[p] ? pid[p] : P.n - 1, xd[p]);
             for (int k = 0; k < 3; ++k) x[p][k] = (T)xd[p][k];
         }
         double Z[PPT], G[PPT][3];
 #pragma unroll
-        for (int p = 0; p < PPT; ++p) { Z[p] = 0.0; G[p][0] = G[p][1] = G[p][2] = 0.0; }
+        for (int p = 0; p < PPT; ++p) {
+            Z[p] = 0.0;
+            G[p][0] = G[p][1] = G[p][2] = 0.0;
+        }
 
-        for (int t = 0; t < n_tiles; ++t, ++item) {
+        for (int k = 0; k < my_tiles; ++k, ++item) {
+            const int t = rank + k * split;
             const int s = (int)(item & 1);
             const uint32_t parity = (uint32_t)((item >> 1) & 1);
             if (!mbar_wait(&mbar[s], parity, wait_cap(kCopySpin))) {
@@ -311,7 +405,10 @@ __global__ void __launch_bounds__(256) eval_kernel(const EvalParams P) {
                 s_fail = 1;
             }
             __syncthreads();
-            if (s_fail) goto drain;
+            if (s_fail) {
+                if (!SPLIT) goto drain;
+                break;  // the cluster learns of it at the next barrier
+            }
             {
                 T zt[PPT], gt[PPT][3];
 #pragma unroll
@@ -324,6 +421,7 @@ __global__ void __launch_bounds__(256) eval_kernel(const EvalParams P) {
                         const T wx = rec[8 * q + 3], wy = rec[8 * q + 4], wz = rec[8 * q + 5];
 #pragma unroll
                         for (int p = 0; p < PPT; ++p) {
+                            if (!act[p]) continue;
                             const T hx = ox - x[p][0], hy = oy - x[p][1], hz = oz - x[p][2];
                             const T r = fast_r<T>(hx * hx + hy * hy + hz * hz + (T)kDistEps2);
                             const T k1 = cv.d1_r(r);
@@ -345,6 +443,7 @@ __global__ void __launch_bounds__(256) eval_kernel(const EvalParams P) {
                         const T px = rec[4 * q], py = rec[4 * q + 1], pz = rec[4 * q + 2], al = rec[4 * q + 3];
 #pragma unroll
                         for (int p = 0; p < PPT; ++p) {
+                            if (!act[p]) continue;
                             const T hx = x[p][0] - px, hy = x[p][1] - py, hz = x[p][2] - pz;
                             const T r = fast_r<T>(hx * hx + hy * hy + hz * hz + (T)kDistEps2);
                             zt[p] += al * cv.C(r);
@@ -366,94 +465,67 @@ __global__ void __launch_bounds__(256) eval_kernel(const EvalParams P) {
             __syncthreads();  // stage s fully consumed
             if (item + 2 < n_items) issue(item + 2);
         }
-        // epilogue: drift, outputs, segmentation
+        if (SPLIT) {
+            constexpr int NV = GRAD ? 4 : 1;
+            double* red = reinterpret_cast<double*>(smem + 2 * (size_t)P.stage_bytes);
 #pragma unroll
-        for (int p = 0; p < PPT; ++p) {
-            if (pid[p] >= P.n) continue;
-            const double* mu = P.mu;
-            const double X = xd[p][0], Y = xd[p][1], Zc = xd[p][2];
-            double z = Z[p];
-            if (P.n_drift >= 3) z += mu[0] * X + mu[1] * Y + mu[2] * Zc;
-            if (P.n_drift >= 9)
-                z += mu[3] * X * X + mu[4] * Y * Y + mu[5] * Zc * Zc + mu[6] * X * Y + mu[7] * X * Zc + mu[8] * Y * Zc;
-            if (P.n_fault) z += fault_term(P, pid[p]);
-            if (P.field) P.field[pid[p]] = z;
-            if (GRAD && P.grad) {
-                double gx = G[p][0], gy = G[p][1], gz = G[p][2];
-                if (P.n_drift >= 3) { gx += mu[0]; gy += mu[1]; gz += mu[2]; }
-                if (P.n_drift >= 9) {
-                    gx += 2.0 * mu[3] * X + mu[6] * Y + mu[7] * Zc;
-                    gy += 2.0 * mu[4] * Y + mu[6] * X + mu[8] * Zc;
-                    gz += 2.0 * mu[5] * Zc + mu[7] * X + mu[8] * Y;
-                }
-                P.grad[3 * pid[p]] = gx;
-                P.grad[3 * pid[p] + 1] = gy;
-                P.grad[3 * pid[p] + 2] = gz;
+            for (int p = 0; p < PPT; ++p) {
+                const int64_t f = tid + (int64_t)p * blockDim.x;
+                red[f] = Z[p];
+                if (GRAD) for (int c = 0; c < 3; ++c) red[(c + 1) * chunk_pts + f] = G[p][c];
             }
-            if (P.has_seg) {
-                double v = P.seg.unit_values[0];
-                for (int k = 0; k < P.seg.n_surf; ++k)
-                    v += (P.seg.unit_values[k + 1] - P.seg.unit_values[k]) *
-                         (double)sigm<T>(P.seg.slope * (P.seg.isovalues[k] - z));
-                if (P.values) P.values[pid[p]] = v;
-                if (P.ids) P.ids[pid[p]] = block_id(P.seg, z);
-            }
+            if (split_finish<T, NV>(P, chunk, chunk_pts, rank, red, &s_abort, s_fail != 0)) goto drain;
+        } else {
+#pragma unroll
+            for (int p = 0; p < PPT; ++p)
+                if (act[p]) finish_point<T>(P, pid[p], xd[p], Z[p], GRAD ? G[p] : nullptr);
         }
     }
     return;
 drain:
-    // a stage wait gave up: wait (bounded) for copies still in flight, then leave
-    if (tid == 0) {
+    // a copy wait gave up (here or in the cluster): wait, bounded, for the
+    // copies still in flight, then leave
+    if (tid == 0)
         for (int64_t it = item; it < n_items && it < item + 2; ++it)
             mbar_wait(&mbar[it & 1], (uint32_t)((it >> 1) & 1), kCopySpin);
-    }
     __syncthreads();
 }
 
 // ---------------------------------------------------------------------------
 // float-float evaluation (cubic kernel, field only)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void point_coords(const EvalParams& P, int64_t q, double* xd) {
-    if (P.kind == 0) {
-        const int64_t nyz = (int64_t)P.dims[1] * P.dims[2];
-        const int64_t ix = q / nyz, rem = q - ix * nyz;
-        const int64_t iy = rem / P.dims[2], iz = rem - iy * P.dims[2];
-        xd[0] = P.origin[0] + (double)ix * P.spacing[0];
-        xd[1] = P.origin[1] + (double)iy * P.spacing[1];
-        xd[2] = P.origin[2] + (double)iz * P.spacing[2];
-    } else {
-        xd[0] = P.xyz[3 * q];
-        xd[1] = P.xyz[3 * q + 1];
-        xd[2] = P.xyz[3 * q + 2];
-    }
-}
-
-template <int PPT>
+template <int PPT, bool SPLIT>
 __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const double* __restrict__ meta) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t mbar[2];
-    __shared__ int s_fail;
+    __shared__ int s_fail, s_abort;
     const int tid = threadIdx.x;
+    const int split = SPLIT ? P.split : 1;
     unsigned char* stage[2] = {smem, smem + P.stage_bytes};
     if (tid == 0) {
         mbar_init(&mbar[0], 1);
         mbar_init(&mbar[1], 1);
         mbar_fence_init();
         s_fail = 0;
+        s_abort = 0;
     }
     __syncthreads();
+    if (SPLIT) cg::this_cluster().sync();  // abort words initialised before any peer can set one
     const double q = meta[0], inv_a = meta[2];
     const float eps2 = (float)(kDistEps2 * inv_a * inv_a);
     const int64_t chunk_pts = (int64_t)blockDim.x * PPT;
     const int64_t n_chunks = (P.n + chunk_pts - 1) / chunk_pts;
     const int n_tiles = P.tiles_ori + P.tiles_sp;
-    const int64_t my_chunks = n_chunks > blockIdx.x ? (n_chunks - 1 - blockIdx.x) / gridDim.x + 1 : 0;
-    const int64_t n_items = my_chunks * n_tiles;
+    const int rank = SPLIT ? (int)cg::this_cluster().block_rank() : 0;
+    const int64_t group = blockIdx.x / split, n_groups = gridDim.x / split;
+    const int my_tiles = n_tiles > rank ? (n_tiles - 1 - rank) / split + 1 : 0;
+    const int64_t my_chunks = n_chunks > group ? (n_chunks - 1 - group) / n_groups + 1 : 0;
+    const int64_t n_items = my_chunks * my_tiles;
 
     auto issue = [&](int64_t item) {
         if (tid != 0) return;
         int s = (int)(item & 1);
-        int t = (int)(item % n_tiles);
+        int t = rank + (int)(item % my_tiles) * split;
         const void* src;
         uint32_t bytes;
         if (t < P.tiles_ori) {
@@ -476,23 +548,25 @@ __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const 
 
     int64_t item = 0;
     for (int64_t lc = 0; lc < my_chunks; ++lc) {
-        const int64_t chunk = blockIdx.x + lc * gridDim.x;
+        const int64_t chunk = group + lc * n_groups;
         PointFF X[PPT];
+        bool all_exact = true, act[PPT], any_act = false;
 #pragma unroll
         for (int p = 0; p < PPT; ++p) {
             const int64_t pidp = chunk * chunk_pts + tid + (int64_t)p * blockDim.x;
+            act[p] = pidp < P.n;
             double xd[3];
-            point_coords(P, pidp < P.n ? pidp : P.n - 1, xd);
+            point_coords(P, act[p] ? pidp : P.n - 1, xd);
             ff_point(xd, inv_a, q, X[p]);
+            all_exact = all_exact && (X[p].exact || !act[p]);
+            any_act = any_act || act[p];
         }
-        bool all_exact = true;
-#pragma unroll
-        for (int p = 0; p < PPT; ++p) all_exact = all_exact && X[p].exact;
         double Z[PPT];
 #pragma unroll
         for (int p = 0; p < PPT; ++p) Z[p] = 0.0;
 
-        for (int t = 0; t < n_tiles; ++t, ++item) {
+        for (int k = 0; k < my_tiles; ++k, ++item) {
+            const int t = rank + k * split;
             const int s = (int)(item & 1);
             const uint32_t parity = (uint32_t)((item >> 1) & 1);
             if (!mbar_wait(&mbar[s], parity, wait_cap(kCopySpin))) {
@@ -500,7 +574,10 @@ __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const 
                 s_fail = 1;
             }
             __syncthreads();
-            if (s_fail) goto drain;
+            if (s_fail) {
+                if (!SPLIT) goto drain;
+                break;  // the cluster learns of it at the next barrier
+            }
             {
                 ffacc acc[PPT];
 #pragma unroll
@@ -509,45 +586,39 @@ __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const 
                 const bool ori = t < P.tiles_ori;
                 const int nr = ori ? min(P.rec_ori, P.n_ori - t * P.rec_ori)
                                    : min(P.rec_sp, P.n_sp - (t - P.tiles_ori) * P.rec_sp);
-                if (all_exact) ff_tile<PPT, true>(rec, ori, nr, X, eps2, acc);
-                else ff_tile<PPT, false>(rec, ori, nr, X, eps2, acc);
+                if (!any_act) {
+                } else if (all_exact) {
+                    ff_tile<PPT, true>(rec, ori, nr, X, act, eps2, acc);
+                } else {
+                    ff_tile<PPT, false>(rec, ori, nr, X, act, eps2, acc);
+                }
 #pragma unroll
                 for (int p = 0; p < PPT; ++p) Z[p] += ff_acc_to_double(acc[p]);
             }
             __syncthreads();
             if (item + 2 < n_items) issue(item + 2);
         }
+        if (SPLIT) {
+            double* red = reinterpret_cast<double*>(smem + 2 * (size_t)P.stage_bytes);
 #pragma unroll
-        for (int p = 0; p < PPT; ++p) {
-            const int64_t pidp = chunk * chunk_pts + tid + (int64_t)p * blockDim.x;
-            if (pidp >= P.n) continue;
-            double xd[3];
-            point_coords(P, pidp, xd);
-            const double* mu = P.mu;
-            const double Xx = xd[0], Yy = xd[1], Zc = xd[2];
-            double z = Z[p];
-            if (P.n_drift >= 3) z += mu[0] * Xx + mu[1] * Yy + mu[2] * Zc;
-            if (P.n_drift >= 9)
-                z += mu[3] * Xx * Xx + mu[4] * Yy * Yy + mu[5] * Zc * Zc + mu[6] * Xx * Yy + mu[7] * Xx * Zc +
-                     mu[8] * Yy * Zc;
-            if (P.n_fault) z += fault_term(P, pidp);
-            if (P.field) P.field[pidp] = z;
-            if (P.has_seg) {
-                double v = P.seg.unit_values[0];
-                for (int k = 0; k < P.seg.n_surf; ++k)
-                    v += (P.seg.unit_values[k + 1] - P.seg.unit_values[k]) *
-                         (double)sigm<float>(P.seg.slope * (P.seg.isovalues[k] - z));
-                if (P.values) P.values[pidp] = v;
-                if (P.ids) P.ids[pidp] = block_id(P.seg, z);
+            for (int p = 0; p < PPT; ++p) red[tid + p * blockDim.x] = Z[p];
+            if (split_finish<float, 1>(P, chunk, chunk_pts, rank, red, &s_abort, s_fail != 0)) goto drain;
+        } else {
+#pragma unroll
+            for (int p = 0; p < PPT; ++p) {
+                if (!act[p]) continue;
+                const int64_t pidp = chunk * chunk_pts + tid + (int64_t)p * blockDim.x;
+                double xd[3];
+                point_coords(P, pidp, xd);
+                finish_point<float>(P, pidp, xd, Z[p], nullptr);
             }
         }
     }
     return;
 drain:
-    if (tid == 0) {
+    if (tid == 0)
         for (int64_t it = item; it < n_items && it < item + 2; ++it)
             mbar_wait(&mbar[it & 1], (uint32_t)((it >> 1) & 1), kCopySpin);
-    }
     __syncthreads();
 }
 
@@ -654,61 +725,98 @@ extern "C" gk_status gk_eval_prepare(const gk_system* s, const double* w, void* 
     return GK_OK;
 }
 
-template <typename T, int PPT, bool GRAD>
-static gk_status launch_eval(EvalParams& P, cudaStream_t st, int stage_kb = 32) {
-    const int stage_bytes = stage_kb * 1024;
-    P.stage_bytes = stage_bytes;
-    P.rec_ori = stage_bytes / (8 * sizeof(T));
-    P.rec_sp = stage_bytes / (4 * sizeof(T));
-    P.tiles_ori = (P.n_ori + P.rec_ori - 1) / P.rec_ori;
-    P.tiles_sp = (P.n_sp + P.rec_sp - 1) / P.rec_sp;
-    auto k = eval_kernel<T, PPT, GRAD>;
-    size_t smem = 2 * (size_t)stage_bytes;
-    GK_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int occ = 0;
-    GK_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, 256, smem));
-    if (occ < 1) occ = 1;
-    const int64_t chunk_pts = 256LL * PPT;
-    int64_t n_chunks = (P.n + chunk_pts - 1) / chunk_pts;
-    int64_t grid = (int64_t)occ * device_sm_count();
-    if (grid > n_chunks) grid = n_chunks;
-    if (grid < 1) grid = 1;
-    if (P.tiles_ori + P.tiles_sp == 0) {
-        // no covariance records: a zero-length record set still needs the drift epilogue
-        P.tiles_sp = 0;
+// Record tiles of `rec_bytes_ori` / `rec_bytes_sp` bytes per record, at most
+// `stage_bytes` bytes per tile; split > 1 cuts the records into about `split`
+// tiles of each kind so every rank of a cluster streams about one of each.
+static void plan_tiles(EvalParams& P, int stage_bytes, int rec_bytes_ori, int rec_bytes_sp, int split) {
+    int ro = stage_bytes / rec_bytes_ori, rs = stage_bytes / rec_bytes_sp;
+    if (split > 1) {
+        ro = std::min(ro, std::max(1, (P.n_ori + split - 1) / split));
+        rs = std::min(rs, std::max(1, (P.n_sp + split - 1) / split));
+        stage_bytes = (std::max(ro * rec_bytes_ori, rs * rec_bytes_sp) + 127) & ~127;
     }
-    k<<<(unsigned)grid, 256, smem, st>>>(P);
+    P.stage_bytes = stage_bytes;
+    P.rec_ori = ro;
+    P.rec_sp = rs;
+    P.tiles_ori = (P.n_ori + ro - 1) / ro;
+    P.tiles_sp = (P.n_sp + rs - 1) / rs;
+    P.split = split;
+}
+
+constexpr int kMaxSplit = 16;          // cluster sizes above 8 are opted into per kernel
+constexpr int kMinSplitRecords = 48;   // records per rank below which a split does not pay
+
+// Launches `kernel` over the chunks of P or, when the chunks alone would fill
+// less than half of the GPU, `split_kernel` with the records split over a
+// cluster of up to kMaxSplit CTAs per chunk.
+template <typename Kernel, typename... Args>
+static gk_status launch_chunks(Kernel kernel, Kernel split_kernel, EvalParams& P, int ppt, int stage_kb,
+                               int rec_bytes_ori, int rec_bytes_sp, int nv, cudaStream_t st, Args... args) {
+    const int64_t chunk_pts = 256LL * ppt;
+    const int64_t n_chunks = (P.n + chunk_pts - 1) / chunk_pts;
+    const int sms = device_sm_count();
+    const int n_rec = P.n_ori + P.n_sp;
+    int occ = 1;
+    plan_tiles(P, stage_kb * 1024, rec_bytes_ori, rec_bytes_sp, 1);
+    size_t smem = 2 * (size_t)P.stage_bytes;
+    gk_status rc = cached_occupancy((const void*)kernel, 256, smem, occ);
+    if (rc != GK_OK) return rc;
+    int split = 1;
+    while (split < kMaxSplit && n_chunks * (2 * split) <= (int64_t)occ * sms &&
+           n_rec >= 2 * split * kMinSplitRecords)
+        split *= 2;
+    for (; split > 1; split /= 2) {
+        plan_tiles(P, stage_kb * 1024, rec_bytes_ori, rec_bytes_sp, split);
+        smem = 2 * (size_t)P.stage_bytes + (size_t)chunk_pts * nv * sizeof(double);
+        int occ_s = 1;
+        if (cached_occupancy((const void*)split_kernel, 256, smem, occ_s) != GK_OK) return GK_ERR_CUDA;
+        if (cached_cluster_fits((const void*)split_kernel, 256, smem, split)) break;
+    }
+    if (split == 1) {
+        plan_tiles(P, stage_kb * 1024, rec_bytes_ori, rec_bytes_sp, 1);
+        smem = 2 * (size_t)P.stage_bytes;
+        int64_t grid = std::min<int64_t>((int64_t)occ * sms, n_chunks);
+        if (grid < 1) grid = 1;
+        kernel<<<(unsigned)grid, 256, smem, st>>>(P, args...);
+        GK_LAUNCH_CHECK();
+        return GK_OK;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)split;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3((unsigned)(n_chunks * split));
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (cudaLaunchKernelEx(&cfg, split_kernel, P, args...) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return GK_ERR_CUDA;
+    }
     GK_LAUNCH_CHECK();
     return GK_OK;
+}
+
+template <typename T, int PPT, bool GRAD>
+static gk_status launch_eval(EvalParams& P, cudaStream_t st, int stage_kb = 32) {
+    return launch_chunks(eval_kernel<T, PPT, GRAD, false>, eval_kernel<T, PPT, GRAD, true>, P, PPT, stage_kb,
+                         (int)(8 * sizeof(T)), (int)(4 * sizeof(T)), GRAD ? 4 : 1, st);
 }
 
 template <int PPT>
 static gk_status launch_eval_ff(EvalParams& P, const double* meta, cudaStream_t st, int stage_kb) {
-    const int stage_bytes = stage_kb * 1024;
-    P.stage_bytes = stage_bytes;
-    P.rec_ori = stage_bytes / (16 * sizeof(float));
-    P.rec_sp = stage_bytes / (8 * sizeof(float));
-    P.tiles_ori = (P.n_ori + P.rec_ori - 1) / P.rec_ori;
-    P.tiles_sp = (P.n_sp + P.rec_sp - 1) / P.rec_sp;
-    auto k = eval_ff_kernel<PPT>;
-    size_t smem = 2 * (size_t)stage_bytes;
-    GK_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int occ = 0;
-    GK_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, 256, smem));
-    if (occ < 1) occ = 1;
-    const int64_t chunk_pts = 256LL * PPT;
-    int64_t n_chunks = (P.n + chunk_pts - 1) / chunk_pts;
-    int64_t grid = (int64_t)occ * device_sm_count();
-    if (grid > n_chunks) grid = n_chunks;
-    if (grid < 1) grid = 1;
-    k<<<(unsigned)grid, 256, smem, st>>>(P, meta);
-    GK_LAUNCH_CHECK();
-    return GK_OK;
+    return launch_chunks(eval_ff_kernel<PPT, false>, eval_ff_kernel<PPT, true>, P, PPT, stage_kb,
+                         (int)(16 * sizeof(float)), (int)(8 * sizeof(float)), 1, st, meta);
 }
 
-extern "C" gk_status gk_eval(const gk_system* s, const void* model, const gk_points* pts, gk_prec prec,
-                             const gk_segment* seg, double* field, double* grad, double* values, int32_t* ids,
-                             gk_info* info, gk_stream stream) {
+// gk_eval with the offsetting faults' blocks given as row pointers.
+static gk_status eval_impl(const gk_system* s, const void* model, const gk_points* pts,
+                           const double* const* fault_rows, gk_prec prec, const gk_segment* seg, double* field,
+                           double* grad, double* values, int32_t* ids, gk_info* info, gk_stream stream) {
     gk_status st = gk_check_system(s);
     if (st != GK_OK) return st;
     if (model == nullptr || pts == nullptr) return GK_ERR_ARG;
@@ -723,7 +831,9 @@ extern "C" gk_status gk_eval(const gk_system* s, const void* model, const gk_poi
     if (seg != nullptr && (seg->n_surf < 0 || seg->n_surf > GK_MAX_SURFACES)) return GK_ERR_SIZE;
     if ((values || ids) && seg == nullptr) return GK_ERR_ARG;
     if (s->n_ori + s->n_sp == 0) return GK_ERR_ARG;
-    if (s->n_fault > 0 && (pts->fault_values == nullptr || pts->fault_ld < pts->n)) return GK_ERR_ARG;
+    if (s->n_fault > 0 && fault_rows == nullptr) return GK_ERR_ARG;
+    for (int f = 0; f < s->n_fault; ++f)
+        if (fault_rows[f] == nullptr) return GK_ERR_ARG;
     ModelLayout L = model_layout(s->n_ori, s->n_sp);
     const char* m = (const char*)model;
     EvalParams P;
@@ -743,8 +853,7 @@ extern "C" gk_status gk_eval(const gk_system* s, const void* model, const gk_poi
     P.kernel = s->kernel;
     P.range = s->range;
     P.n_fault = s->n_fault;
-    P.fault_values = pts->fault_values;
-    P.fault_ld = pts->fault_ld;
+    for (int f = 0; f < s->n_fault; ++f) P.fault_rows[f] = fault_rows[f];
     P.mu = (const double*)(m + L.mu64);
     P.has_seg = seg != nullptr;
     if (seg) P.seg = *seg;
@@ -776,6 +885,50 @@ extern "C" gk_status gk_eval(const gk_system* s, const void* model, const gk_poi
                           : launch_eval_ff<4>(P, (const double*)(m + L.ffmeta), cs, v.stage_kb);
     }
     return GK_ERR_ARG;
+}
+
+extern "C" gk_status gk_eval(const gk_system* s, const void* model, const gk_points* pts, gk_prec prec,
+                             const gk_segment* seg, double* field, double* grad, double* values, int32_t* ids,
+                             gk_info* info, gk_stream stream) {
+    if (s == nullptr || pts == nullptr) return GK_ERR_ARG;
+    const double* rows[GK_MAX_FAULTS] = {nullptr};
+    if (s->n_fault > 0) {
+        if (s->n_fault > GK_MAX_FAULTS) return GK_ERR_SIZE;
+        if (pts->fault_values == nullptr || pts->fault_ld < pts->n) return GK_ERR_ARG;
+        for (int f = 0; f < s->n_fault; ++f) rows[f] = pts->fault_values + (int64_t)f * pts->fault_ld;
+    }
+    return eval_impl(s, model, pts, rows, prec, seg, field, grad, values, ids, info, stream);
+}
+
+extern "C" gk_status gk_eval_series_set(int32_t n_series, const gk_series_eval* series, const gk_points* pts,
+                                        gk_prec prec, double* fields, double* values, int32_t* ids, double* block,
+                                        int32_t* lith_ids, uint8_t* masks, gk_info* info, gk_stream stream) {
+    if (n_series < 1 || n_series > GK_MAX_SURFACES || series == nullptr || pts == nullptr) return GK_ERR_ARG;
+    if (fields == nullptr || values == nullptr || ids == nullptr) return GK_ERR_ARG;
+    const int64_t n = pts->n;
+    if (n < 0) return GK_ERR_ARG;
+    if (n == 0) return GK_OK;
+    int32_t rel[GK_MAX_SURFACES];
+    double mn[GK_MAX_SURFACES], mx[GK_MAX_SURFACES];
+    for (int i = 0; i < n_series; ++i) {
+        const gk_series_eval& e = series[i];
+        if (e.sys == nullptr) return GK_ERR_ARG;
+        if (e.n_faults != e.sys->n_fault) return GK_ERR_ARG;
+        const double* rows[GK_MAX_FAULTS] = {nullptr};
+        for (int f = 0; f < e.n_faults; ++f) {
+            const int j = e.faults[f];
+            if (j < 0 || j >= i) return GK_ERR_ARG;  // a fault offsets younger series only
+            rows[f] = values + (int64_t)j * n;
+        }
+        gk_status st = eval_impl(e.sys, e.model, pts, rows, prec, &e.seg, fields + (int64_t)i * n, nullptr,
+                                 values + (int64_t)i * n, ids + (int64_t)i * n, info, stream);
+        if (st != GK_OK) return st;
+        rel[i] = e.relation;
+        mn[i] = e.min_iso;
+        mx[i] = e.max_iso;
+    }
+    if (block == nullptr && lith_ids == nullptr && masks == nullptr) return GK_OK;
+    return gk_combine_series(n_series, n, fields, values, ids, rel, mn, mx, block, lith_ids, masks, stream);
 }
 
 extern "C" gk_status gk_combine_series(int32_t n_series, int64_t n, const double* fields, const double* values,

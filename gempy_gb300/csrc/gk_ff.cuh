@@ -172,7 +172,7 @@ __device__ __forceinline__ double ff_quantum(const unsigned int* maxbits) {
 }
 
 __device__ __forceinline__ void ff_split(double u, double q, float& h, float& l) {
-    double hi = rint(u / q) * q;
+    double hi = rint(u * (1.0 / q)) * q;   // q is a power of two: u * (1/q) == u / q exactly
     h = (float)hi;
     l = (float)(u - hi);
 }
@@ -183,11 +183,11 @@ struct PointFF {
 };
 
 __device__ __forceinline__ void ff_point(const double* xd, double inv_a, double q, PointFF& P) {
-    const double lim = ldexp(q, 23);
+    const double lim = ldexp(q, 23), inv_q = 1.0 / q;   // q a power of two: exact inverse
     P.exact = true;
     for (int k = 0; k < 3; ++k) {
         double u = xd[k] * inv_a;
-        double hi = rint(u / q) * q;
+        double hi = rint(u * inv_q) * q;
         P.h[k] = (float)hi;
         P.l[k] = (float)(u - hi);
         if (fabs(hi) > lim) P.exact = false;
@@ -231,7 +231,8 @@ __device__ __forceinline__ ff ff_dist2(const PointFF& X, const float* ph, const 
 // EXACT: every point's split is exact (the common case).
 template <int PPT, bool EXACT>
 __device__ __forceinline__ void ff_tile(const float* __restrict__ rec, bool orientation, int nr,
-                                        const PointFF (&X)[PPT], float eps2, ffacc (&acc)[PPT]) {
+                                        const PointFF (&X)[PPT], const bool (&act)[PPT], float eps2,
+                                        ffacc (&acc)[PPT]) {
     if (orientation) {
         for (int qr = 0; qr < nr; ++qr) {
             const float4* R4 = reinterpret_cast<const float4*>(rec + 16 * qr);
@@ -240,6 +241,7 @@ __device__ __forceinline__ void ff_tile(const float* __restrict__ rec, bool orie
             const ff wx = {a1.z, a1.w}, wy = {a2.x, a2.y}, wz = {a2.z, a2.w};
 #pragma unroll
             for (int p = 0; p < PPT; ++p) {
+                if (!act[p]) continue;  // a slot past the end of the point list
                 float dh[3], dl[3];
                 const ff r2 = ff_dist2<EXACT>(X[p], ph, pl, dh, dl, eps2);
                 if (r2.h >= 1.f) continue;  // beyond the range: C'/r = 0
@@ -261,6 +263,7 @@ __device__ __forceinline__ void ff_tile(const float* __restrict__ rec, bool orie
             const ff W = {a1.z, a1.w};
 #pragma unroll
             for (int p = 0; p < PPT; ++p) {
+                if (!act[p]) continue;
                 float dh[3], dl[3];
                 const ff r2 = ff_dist2<EXACT>(X[p], ph, pl, dh, dl, eps2);
                 if (r2.h >= 1.f) continue;  // beyond the range: C = 0

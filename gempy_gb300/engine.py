@@ -110,11 +110,35 @@ def _solve_learned(dev_s, cost_model, tol, x0=None):
 
 
 def _split(interpolation_input, options, data_descriptor, device):
+    """Per-series DeviceSeries.  All series' inputs go to the device in two
+    copies -- one FP64 buffer (points, nuggets, orientations, reference
+    points), one int32 buffer (reference/rest indices) -- and each series
+    holds views into them."""
     ss = data_descriptor.stack_structure
     pps = np.asarray(data_descriptor.tensors_structure.number_of_points_per_surface, dtype=np.int64)
     sp = interpolation_input.surface_points
     ori = interpolation_input.orientations
     ko = options.kernel_options
+    spc = np.asarray(sp.sp_coords, dtype=np.float64).reshape(-1, 3)
+    nsp = np.asarray(sp.nugget_effect_scalar, dtype=np.float64).ravel()
+    dpos = np.asarray(ori.dip_positions, dtype=np.float64).reshape(-1, 3)
+    dgr = np.asarray(ori.dip_gradients, dtype=np.float64).reshape(-1, 3)
+    ngr = np.asarray(ori.nugget_effect_grad, dtype=np.float64).ravel()
+    starts = np.concatenate([[0], np.cumsum(pps)[:-1]]).astype(np.int64) if len(pps) else np.zeros(0, np.int64)
+    refp = spc[starts]
+    parts = [spc.ravel(), nsp, dpos.ravel(), dgr.ravel(), ngr, refp.ravel()]
+    offs = np.concatenate([[0], np.cumsum([len(a) for a in parts])])
+    f64 = torch.as_tensor(np.concatenate(parts)).to(device)
+    g_sp, g_nsp, g_dpos, g_dgr, g_ngr, g_ref = (f64[offs[i]:offs[i + 1]] for i in range(6))
+    g_sp, g_dpos, g_dgr, g_ref = g_sp.view(-1, 3), g_dpos.view(-1, 3), g_dgr.view(-1, 3), g_ref.view(-1, 3)
+    idx_parts, s_off = [], 0
+    for i in range(ss.n_stacks):
+        n_s = int(ss.number_of_surfaces_per_stack[i])
+        ref, rest = K.ref_rest_indices(pps[s_off:s_off + n_s])
+        idx_parts += [ref, rest]
+        s_off += n_s
+    ilen = np.concatenate([[0], np.cumsum([len(a) for a in idx_parts])])
+    i32 = torch.as_tensor(np.concatenate(idx_parts).astype(np.int32) if idx_parts else np.zeros(0, np.int32)).to(device)
     p_off = o_off = s_off = 0
     out = []
     for i in range(ss.n_stacks):
@@ -122,11 +146,12 @@ def _split(interpolation_input, options, data_descriptor, device):
         n_o = int(ss.number_of_orientations_per_stack[i])
         n_s = int(ss.number_of_surfaces_per_stack[i])
         dev = K.DeviceSeries(
-            ori.dip_positions[o_off:o_off + n_o], ori.dip_gradients[o_off:o_off + n_o],
-            ori.nugget_effect_grad[o_off:o_off + n_o],
-            sp.sp_coords[p_off:p_off + n_p], sp.nugget_effect_scalar[p_off:p_off + n_p],
-            pps[s_off:s_off + n_s], range=ko.range, c_o=ko.c_o, uni_degree=ko.uni_degree,
-            kernel=ko.kernel_function, i_res=ko.i_res, gi_res=ko.gi_res, device=device)
+            g_dpos[o_off:o_off + n_o], g_dgr[o_off:o_off + n_o], g_ngr[o_off:o_off + n_o],
+            g_sp[p_off:p_off + n_p], g_nsp[p_off:p_off + n_p], pps[s_off:s_off + n_s],
+            range=ko.range, c_o=ko.c_o, uni_degree=ko.uni_degree, kernel=ko.kernel_function, i_res=ko.i_res,
+            gi_res=ko.gi_res, device=device,
+            ref_index=i32[ilen[2 * i]:ilen[2 * i + 1]], rest_index=i32[ilen[2 * i + 1]:ilen[2 * i + 2]],
+            ref_points=g_ref[s_off:s_off + n_s])
         faults = ss.fault_sources(i) if hasattr(ss, "fault_sources") else []
         out.append((dev, s_off, n_s, ss.masking_descriptor[i], faults))
         p_off += n_p
@@ -146,10 +171,12 @@ class _Evaluation:
     masks: torch.Tensor           # (n_series, n) squeezed masks
     fault_rows: List[int]         # series that are FAULT stacks
 
-    def refinement_ids(self):
-        """Id sets whose change across a voxel's corners refines it: the
-        lithology, then each fault series' block."""
-        return torch.stack([self.lith_ids] + [self.ids[i] for i in self.fault_rows])
+    def refinement_ids(self, a, b):
+        """Id sets of points a..b-1 whose change across a voxel's corners
+        refines it: the lithology, then each fault series' block."""
+        if not self.fault_rows:
+            return self.lith_ids[a:b].view(1, -1)
+        return torch.stack([self.lith_ids[a:b]] + [self.ids[i, a:b] for i in self.fault_rows])
 
     def slice(self, a, b):
         return _Evaluation(self.fields[:, a:b], self.values[:, a:b], self.ids[:, a:b],
@@ -174,63 +201,263 @@ class _Evaluator:
             vals.append(v)
         return vals
 
+    def _set(self):
+        if getattr(self, "_series_set", None) is None:
+            self._series_set = K.SeriesSet([
+                (s.dev, s.model, s.seg, int(s.relation), s.faults,
+                 float(np.min(s.iso)) if len(s.iso) else 0.0, float(np.max(s.iso)) if len(s.iso) else 0.0)
+                for s in self.series])
+            self._frows = [k for k, s in enumerate(self.series) if int(s.relation) == int(StackRelationType.FAULT)]
+        return self._series_set
+
     def run(self, pts: K.Points, gradient=False) -> _Evaluation:
-        fields, values, ids, grads = [], [], [], []
-        for s in self.series:
-            fv = torch.stack([values[j] for j in s.faults]) if s.faults else None
-            f, _, v, i = K.evaluate(s.dev, s.model, pts, self.prec, seg=s.seg, want_ids=True, fault_values=fv)
+        """Every series at ``pts`` and their combination: one library call
+        (gk_eval_series_set); gradients, when asked for, in FP64 per series."""
+        F, V, I, cv, ci, masks = self._set().evaluate(pts, self.prec)
+        grads = []
+        for k, s in enumerate(self.series):
             g = None
             if gradient:   # gradients in FP64 (the float-float kernel computes the field only)
+                fv = V[s.faults] if s.faults else None
                 _, g, _, _ = K.evaluate(s.dev, s.model, pts, GK_F64 if self.prec == GK_FF else self.prec,
                                         gradient=True, want_field=False, fault_values=fv)
-            fields.append(f)
-            values.append(v)
-            ids.append(i)
             grads.append(g)
-        F, V, I = torch.stack(fields), torch.stack(values), torch.stack(ids)
-        rel = [int(s.relation) for s in self.series]
-        mn = [float(np.min(s.iso)) if len(s.iso) else 0.0 for s in self.series]
-        mx = [float(np.max(s.iso)) if len(s.iso) else 0.0 for s in self.series]
-        cv, ci, masks = K.combine(F, V, I, rel, mn, mx)
-        frows = [k for k, s in enumerate(self.series) if int(s.relation) == int(StackRelationType.FAULT)]
-        return _Evaluation(F, V, I, grads, cv, ci, masks, frows)
+        return _Evaluation(F, V, I, grads, cv, ci, masks, self._frows)
 
 
-def _np(t, keep):
-    if t is None:
-        return None
-    return t if keep else t.cpu().numpy()
-
-
-def _outputs(ev: _Evaluation, series, keep):
+def _outputs(ev: _Evaluation, series):
     outs = []
     for i, s in enumerate(series):
         g = ev.grads[i]
-        ef = ExportedFields(scalar_field=_np(ev.fields[i], keep),
-                            gx_field=_np(g[:, 0], keep) if g is not None else None,
-                            gy_field=_np(g[:, 1], keep) if g is not None else None,
-                            gz_field=_np(g[:, 2], keep) if g is not None else None,
+        ef = ExportedFields(scalar_field=ev.fields[i],
+                            gx_field=g[:, 0] if g is not None else None,
+                            gy_field=g[:, 1] if g is not None else None,
+                            gz_field=g[:, 2] if g is not None else None,
                             scalar_field_at_surface_points=s.iso)
-        outs.append(InterpOutput(ef, _np(ev.values[i], keep), weights=_np(s.weights, keep),
-                                 mask=_np(ev.masks[i], keep)))
+        outs.append(InterpOutput(ef, ev.values[i], weights=s.weights, mask=ev.masks[i]))
     return outs
 
 
-def _combined(ev: _Evaluation, keep):
-    return CombinedOutput(ExportedFields(scalar_field=_np(ev.fields[-1], keep)), _np(ev.block, keep),
-                          _np(ev.lith_ids, keep), _np(ev.masks, keep))
+def _combined(ev: _Evaluation):
+    return CombinedOutput(ExportedFields(scalar_field=ev.fields[-1]), ev.block, ev.lith_ids, ev.masks)
+
+
+_NP_DTYPE = {torch.float64: np.float64, torch.float32: np.float32, torch.int32: np.int32,
+             torch.uint8: np.uint8, torch.int64: np.int64, torch.bool: np.bool_}
+
+
+def _tensor_slots(obj):
+    """(container, key, tensor) for every CUDA tensor reachable in obj."""
+    slots = []
+
+    def visit(o):
+        if isinstance(o, list):
+            for i, v in enumerate(o):
+                if isinstance(v, torch.Tensor):
+                    slots.append((o, i, v))
+                else:
+                    visit(v)
+            return
+        d = getattr(o, "__dict__", None)
+        if d is None:
+            return
+        for k, v in list(d.items()):
+            if isinstance(v, torch.Tensor):
+                slots.append((o, k, v))
+            elif isinstance(v, list) or hasattr(v, "__dict__"):
+                visit(v)
+
+    visit(obj)
+    return slots
+
+
+class _HostStager:
+    """Moves result tensors to host numpy arrays with few, overlapped copies,
+    made on a side stream (into page-locked memory from PyTorch's caching
+    host allocator) while the compute stream goes on.
+
+    * ``push(t)`` copies the bytes of a contiguous device tensor;
+      ``host(t)`` is then its numpy copy.
+    * ``stage(obj)`` copies every device tensor reachable from ``obj``: the
+      tensors are views of a few allocations, each copied whole once, and each
+      tensor becomes a numpy view of its copy (same offset, shape and strides).
+
+    ``finish`` waits for the copies, then ``host`` answers and staged objects
+    hold numpy arrays."""
+
+    def __init__(self):
+        self.stream = torch.cuda.Stream()
+        self.jobs = []
+        self.hosts = {}        # device storage address -> page-locked copy of the whole storage
+        self.pushed = {}       # id(tensor) -> (tensor, page-locked copy of its bytes)
+        self.pending = []
+
+    def _copy(self, dev_bytes, nbytes):
+        pinned = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+        self.pending.append((dev_bytes, pinned))
+        return pinned
+
+    def _launch(self):
+        if not self.pending:
+            return
+        self.stream.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(self.stream):
+            for dev, pinned in self.pending:
+                pinned.copy_(dev, non_blocking=True)
+        for dev, _ in self.pending:
+            dev.record_stream(self.stream)
+        self.pending = []
+
+    def push(self, *tensors):
+        for t in tensors:
+            if t is None or id(t) in self.pushed:
+                continue
+            if not t.is_contiguous():
+                raise ValueError("push() copies contiguous tensors")
+            self.pushed[id(t)] = (t, self._copy(t.view(-1).view(torch.uint8), t.numel() * t.element_size()))
+        self._launch()
+
+    def host(self, t):
+        if t is None:
+            return None
+        _, pinned = self.pushed[id(t)]
+        return pinned.numpy().view(_NP_DTYPE[t.dtype]).reshape(tuple(t.shape))
+
+    def stage(self, obj):
+        slots = _tensor_slots(obj)
+        if not slots:
+            return
+        meta = []
+        for _, _, t in slots:
+            st = t.untyped_storage()
+            ptr = st.data_ptr()
+            if ptr not in self.hosts:
+                dev = torch.empty(0, dtype=torch.uint8, device=t.device).set_(st)
+                self.hosts[ptr] = self._copy(dev, st.nbytes())
+            meta.append((ptr, t.storage_offset() * t.element_size(), t.dtype, tuple(t.shape),
+                         tuple(x * t.element_size() for x in t.stride())))
+        self._launch()
+        self.jobs.append((slots, meta))
+
+    def finish(self):
+        self.stream.synchronize()
+        hosts = {ptr: pinned.numpy() for ptr, pinned in self.hosts.items()}
+        for slots, meta in self.jobs:
+            for (obj, k, _), (ptr, off, dt, shape, strides) in zip(slots, meta):
+                arr = np.ndarray(shape, dtype=_NP_DTYPE[dt], buffer=hosts[ptr], offset=off, strides=strides)
+                if isinstance(obj, list):
+                    obj[k] = arr
+                else:
+                    setattr(obj, k, arr)
+        self.jobs.clear()
+        self.hosts.clear()
+
+
+@dataclass
+class _LevelRecord:
+    """What one octree level left on the device: its point buffer
+    ([centres; 8 corners each] or the centres alone), the series-set buffer
+    of its evaluation and the per-series gradients."""
+    pts: torch.Tensor
+    n: int
+    spacing: np.ndarray
+    surface: bool
+    buffer: torch.Tensor
+    layout: tuple
+    grads: list
+
+
+def _level_output(rec: _LevelRecord, ev: "_Evaluator", series, pts, buffer, grads):
+    """The OctreeLevel of a record from its arrays (device tensors, or their
+    host copies: the same layout either way)."""
+    n = rec.n
+    F, V, I, B, L, M = ev._set().views(buffer, rec.layout)
+    e = _Evaluation(F, V, I, grads, B, L, M, ev._frows)
+    ec = e.slice(0, n)
+    outs = _outputs(e if rec.surface else ec, series)
+    corners_out = _combined(e.slice(n, 9 * n)) if rec.surface else None
+    return OctreeLevel(pts[:n], rec.spacing.copy(), outs, _combined(ec), corners_out,
+                       pts[n:] if rec.surface else None)
+
+
+CTA_MAX_N = 4096   # mixed-form series up to this size are solved by one thread block
+
+
+def _solve_one(dev_s, cfg, mixed, cost_model, interpolation_input, si, device):
+    if mixed and cost_model is not None and dev_s.N >= cfg.learned_min_n:
+        return _solve_learned(dev_s, cost_model, cfg.learned_tol,
+                              _warm_start(interpolation_input, si, dev_s.N, device)) + (False,)
+    if mixed and dev_s.N <= CTA_MAX_N:
+        return K.solve_mixed_cta(dev_s, tol=cfg.solver_tol, max_iter=cfg.solver_max_iter) + (True,)
+    if mixed:
+        return K.solve_mixed(dev_s, tol=cfg.solver_tol, max_iter=cfg.solver_max_iter) + (False,)
+    return K.solve_plain(dev_s) + (False,)
 
 
 def _solve_series(interpolation_input, options, data_descriptor, device, cfg, mixed):
+    """Per series: fault blocks, solve, packed model and FP64 isovalues.  The
+    isovalues and solver statuses of all series are read back together with
+    one synchronisation, except where a later series' fault drift needs a
+    fault series' isovalues first."""
     ko = options.kernel_options
     uv = np.asarray(interpolation_input.unit_values, dtype=np.float64)
-    series = []
+    series, pending = [], []
     cost_model = None
     conds = []
     ev = _Evaluator(series, GK_F64, options.sigmoid_slope)
+
+    def finalize():
+        if not pending:
+            return
+        # one copy: every pending series' status word (24 bytes) and isovalues
+        packed = torch.cat([p["info"].view(torch.uint8) for p in pending] +
+                           [p["iso"].contiguous().view(torch.uint8) for p in pending]).cpu().numpy()
+        nb = 24 * len(pending)
+        infos = list(np.frombuffer(packed[:nb].tobytes(), dtype=K.INFO_DTYPE))
+        isos = packed[nb:].view(np.float64)
+        o = 0
+        for p, inf in zip(pending, infos):
+            n_s = p["n_s"]
+            iso = isos[o:o + n_s]
+            o += n_s
+            if p["cta"] and int(inf["status"]) != 0:
+                # the one-block solve met a zero pivot or stalled: the full solver
+                # (partial-pivoting fallback) takes over
+                w, info = K.solve_mixed(p["dev"], tol=cfg.solver_tol, max_iter=cfg.solver_max_iter)
+                p["w"], p["info"] = w, info
+                p["model"] = K.prepare(p["dev"], w)
+                iso = _isovalues(p["dev"], p["model"]).cpu().numpy()
+                inf = K.read_info(info)
+            order = np.argsort(-iso, kind="stable")
+            sr = _Series(p["dev"], iso, order, p["uv"], p["rel"], p["w"], p["info"], p["faults"])
+            sr.info_host = inf
+            sr.model = p["model"]
+            sr.set_slope(options.sigmoid_slope)
+            series.append(sr)
+        pending.clear()
+
+    group = []   # small series of the mixed form, solved together in one launch
+
+    def add_pending(dev_s, w, info, cta, s_off, n_s, rel, faults):
+        model = K.prepare(dev_s, w)
+        iso_t = _isovalues(dev_s, model) if n_s else torch.zeros(0, dtype=torch.float64, device=device)
+        pending.append({"dev": dev_s, "w": w, "info": info, "model": model, "iso": iso_t, "n_s": n_s,
+                        "uv": uv[s_off:s_off + n_s + 1], "rel": rel, "faults": faults, "cta": cta})
+
+    def flush_group():
+        if not group:
+            return
+        res = K.solve_mixed_cta_many([(g["K"], g["b"]) for g in group], tol=cfg.solver_tol,
+                                     max_iter=cfg.solver_max_iter)
+        for g, (w, info) in zip(group, res):
+            add_pending(g["dev"], w, info, True, *g["meta"])
+        group.clear()
+
     for si, (dev_s, s_off, n_s, rel, faults) in enumerate(_split(interpolation_input, options, data_descriptor,
                                                                   device)):
         if faults:
+            flush_group()
+            finalize()   # the fault series' isovalues are needed on the host
             # the fault blocks at this series' surface points are its fault-drift functions
             vals = ev.series_values(K.Points(xyz=dev_s.sp_coords), si)
             dev_s.set_fault_blocks(torch.stack([vals[j] for j in faults]))
@@ -238,41 +465,44 @@ def _solve_series(interpolation_input, options, data_descriptor, device, cfg, mi
             Kc, _ = K.build(dev_s, GK_F64)
             conds.append(K.condition_number(Kc))
             del Kc
-        if mixed and cfg.learned_min_n > 0 and dev_s.N >= cfg.learned_min_n:
-            if cost_model is None:
-                cost_model = _load_cost_model(cfg.learned_model, device)
-        if mixed and cost_model is not None and dev_s.N >= cfg.learned_min_n:
-            w, info = _solve_learned(dev_s, cost_model, cfg.learned_tol,
-                                     _warm_start(interpolation_input, si, dev_s.N, device))
-        elif mixed:
-            w, info = K.solve_mixed(dev_s, tol=cfg.solver_tol, max_iter=cfg.solver_max_iter)
-        else:
-            w, info = K.solve_plain(dev_s)
-        model = K.prepare(dev_s, w)
-        # ---- 3: isovalues at the reference points, FP64
-        if n_s:
-            starts = torch.as_tensor(np.concatenate([[0], np.cumsum(dev_s.points_per_surface)[:-1]])).to(device)
-            fv = dev_s.fault_sp[:, starts] if dev_s.n_faults else None
-            iso_t, _, _, _ = K.evaluate(dev_s, model, K.Points(xyz=dev_s.ref_points), GK_F64, fault_values=fv)
-            iso = iso_t.cpu().numpy()
-        else:
-            iso = np.zeros(0)
-        order = np.argsort(-iso, kind="stable")
-        s = _Series(dev_s, iso, order, uv[s_off:s_off + n_s + 1], rel, w, info, faults)
-        s.model = model
-        s.set_slope(options.sigmoid_slope)
-        series.append(s)
+        if mixed and cfg.learned_min_n > 0 and dev_s.N >= cfg.learned_min_n and cost_model is None:
+            cost_model = _load_cost_model(cfg.learned_model, device)
+        learned = mixed and cost_model is not None and dev_s.N >= cfg.learned_min_n
+        if mixed and not learned and dev_s.N <= CTA_MAX_N:
+            Kd, b = K.build(dev_s, GK_F64)
+            group.append({"dev": dev_s, "K": Kd, "b": b, "meta": (s_off, n_s, rel, faults)})
+            continue
+        flush_group()
+        w, info, cta = _solve_one(dev_s, cfg, mixed, cost_model, interpolation_input, si, device)
+        add_pending(dev_s, w, info, cta, s_off, n_s, rel, faults)
+    flush_group()
+    finalize()
     if conds:
         # the engine reports one number on the options; with several series, the largest
         ko.condition_number = float(max(conds))
     return series
 
 
+def _isovalues(dev_s, model):
+    """FP64 field at each surface's reference point (device tensor)."""
+    fv = None
+    if dev_s.n_faults:
+        starts = torch.as_tensor(np.concatenate([[0], np.cumsum(dev_s.points_per_surface)[:-1]])).to(dev_s.device)
+        fv = dev_s.fault_sp[:, starts]
+    iso_t, _, _, _ = K.evaluate(dev_s, model, K.Points(xyz=dev_s.ref_points), GK_F64, fault_values=fv)
+    return iso_t
+
+
 def compute_model(interpolation_input, options, data_descriptor, geophysics_input=None,
                   config: Optional[EngineConfig] = None) -> Solutions:
-    cfg = config or EngineConfig()
     if not torch.cuda.is_available():
         raise RuntimeError("gempy_gb300.compute_model needs a CUDA device (there is no CPU fallback)")
+    with K.on_current_stream():
+        return _compute_model(interpolation_input, options, data_descriptor, geophysics_input, config)
+
+
+def _compute_model(interpolation_input, options, data_descriptor, geophysics_input, config) -> Solutions:
+    cfg = config or EngineConfig()
     device = torch.device("cuda")
     mixed = str(cfg.dtype) in ("float32", "mixed")
     ko = options.kernel_options
@@ -291,15 +521,18 @@ def compute_model(interpolation_input, options, data_descriptor, geophysics_inpu
         timings["solve_s"] = time.perf_counter() - t0
 
     ev = _Evaluator(series, prec, options.sigmoid_slope)
-    keep = cfg.keep_on_device
     grid = interpolation_input.grid
     eo = options.evaluation_options
     want_grad = bool(eo.compute_scalar_gradient)
 
     # ---- 4a: octree levels.  Centres and (where needed) corners are one
     # point set: [centres; 8 corners per centre], evaluated once per series.
+    # The loop only launches work and reads the size of the next level; each
+    # level's two buffers go to the host while the next level computes, and
+    # the output objects are built once, after the loop.
     t1 = time.perf_counter()
-    octrees = []
+    stager = None if cfg.keep_on_device else _HostStager()
+    records = []
     n_levels = int(eo.number_octree_levels)
     min_level = int(eo.octree_min_level)
     levels_surface = int(getattr(eo, "number_octree_levels_surface", getattr(eo, "_number_octree_levels_surface", 0)))
@@ -307,6 +540,7 @@ def compute_model(interpolation_input, options, data_descriptor, geophysics_inpu
         og = grid.octree_grid
         centres = torch.as_tensor(og.values).to(device)
         d = np.array(og.dxdydz, dtype=np.float64)
+        ss = ev._set()
         for level in range(n_levels):
             n = centres.shape[0]
             last = level == n_levels - 1
@@ -316,20 +550,23 @@ def compute_model(interpolation_input, options, data_descriptor, geophysics_inpu
             if need_corners:
                 pts_xyz = torch.empty((9 * n, 3), dtype=torch.float64, device=device)
                 pts_xyz[:n] = centres
-                pts_xyz[n:] = K.octree_corners(centres, d)
+                K.octree_corners(centres, d, out=pts_xyz[n:])
             else:
-                pts_xyz = centres
-            e = ev.run(K.Points(xyz=pts_xyz), gradient=want_grad)
-            ec = e.slice(0, n)
-            outs = _outputs(e if surface else ec, series, keep)
-            corners_out = _combined(e.slice(n, 9 * n), keep) if surface else None
-            octrees.append(OctreeLevel(_np(centres, keep), d.copy(), outs, _combined(ec, keep), corners_out,
-                                       _np(pts_xyz[n:], keep) if surface else None))
+                pts_xyz = centres.contiguous()
+            pts = K.Points(xyz=pts_xyz)
+            e = ev.run(pts, gradient=want_grad)
+            buf, offs, sizes, _ = ss.last_buffer
+            records.append(_LevelRecord(pts_xyz, n, d.copy(), surface, buf, (offs, sizes, pts.n), e.grads))
+            if stager is not None:
+                stager.push(pts_xyz, buf, *e.grads)   # copied while the next level computes
             if last:
                 break
-            corner_ids = None if refine_all else e.slice(n, 9 * n).refinement_ids()
+            corner_ids = None if refine_all else e.refinement_ids(n, 9 * n)
             centres = K.octree_refine(centres, corner_ids, d, refine_all=refine_all)
             d = d / 2.0
+            if cfg.timings:
+                torch.cuda.synchronize()
+                timings.setdefault("levels_s", []).append(time.perf_counter() - t1)
             if centres.shape[0] == 0:
                 break
     if cfg.timings:
@@ -341,24 +578,37 @@ def compute_model(interpolation_input, options, data_descriptor, geophysics_inpu
     t2 = time.perf_counter()
     if grid.dense_grid is not None:
         e = ev.run(K.Points.regular(grid.dense_grid), gradient=want_grad)
-        raw.lith_block = _np(e.block, keep)
-        raw.scalar_field_matrix = _np(e.fields, keep)
-        raw.mask_matrix_squeezed = _np(e.masks, keep)
-        raw.block_matrix = _np(e.values, keep)
+        raw.lith_block = e.block
+        raw.scalar_field_matrix = e.fields
+        raw.mask_matrix_squeezed = e.masks
+        raw.block_matrix = e.values
     if grid.custom_grid is not None:
         pts = torch.as_tensor(grid.custom_grid.values).to(device)
         e = ev.run(K.Points(xyz=pts))
-        raw.custom = _np(e.block, keep)
+        raw.custom = e.block
     if cfg.timings:
         torch.cuda.synchronize()
         timings["grids_s"] = time.perf_counter() - t2
-        timings["total_s"] = time.perf_counter() - t0
 
+    octrees = [] if stager is not None else [_level_output(r, ev, series, r.pts, r.buffer, r.grads)
+                                             for r in records]
     root = RootOutput([InterpOutput(ExportedFields(scalar_field=None, scalar_field_at_surface_points=s.iso),
-                                    None, weights=_np(s.weights, keep)) for s in series])
+                                    None, weights=s.weights) for s in series])
     sfsp = [float(v) for s in series for v in s.iso]
     sol = Solutions(octrees_output=octrees, root_output=root, raw_arrays=raw,
                     scalar_field_at_surface_points=sfsp, _ordered_elements=[s.order for s in series],
                     block_solution_type=options.block_solutions_type, timings=timings,
-                    solver_info=[K.read_info(s.solve_info) for s in series])
+                    solver_info=[s.info_host for s in series])
+    if cfg.timings:
+        torch.cuda.synchronize()
+        t3 = time.perf_counter()
+    if stager is not None:
+        stager.stage(sol.root_output)     # the octree levels are already on their way
+        stager.stage(sol.raw_arrays)
+        stager.finish()
+        sol.octrees_output = [_level_output(r, ev, series, stager.host(r.pts), stager.host(r.buffer),
+                                            [stager.host(g) for g in r.grads]) for r in records]
+    if cfg.timings:
+        timings["transfer_s"] = time.perf_counter() - t3
+        timings["total_s"] = time.perf_counter() - t0
     return sol

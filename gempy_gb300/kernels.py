@@ -4,7 +4,9 @@ Device memory, streams and host<->device copies come from PyTorch (plumbing
 only); every computation is a call into ``libgempy_gb300.so``.  Tensors passed
 in must be CUDA tensors; nothing here runs on the CPU.
 """
+import contextlib
 import ctypes
+import threading
 from dataclasses import dataclass
 
 import numpy as np
@@ -17,10 +19,34 @@ INFO_DTYPE = np.dtype([("status", "<i4"), ("where", "<i4"), ("iterations", "<i4"
                        ("residual", "<f8")])
 
 
+_tuned = False
+
+
+_local = threading.local()
+
+
 def _stream():
-    from . import autotune
-    autotune.ensure_applied()
+    global _tuned
+    if not _tuned:
+        from . import autotune
+        autotune.ensure_applied()
+        _tuned = True
+    h = getattr(_local, "stream", None)
+    if h is not None:
+        return h
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+@contextlib.contextmanager
+def on_current_stream():
+    """Within the block every library call of this thread goes to the stream
+    that is current on entry (looked up once instead of per call)."""
+    prev = getattr(_local, "stream", None)
+    _local.stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    try:
+        yield
+    finally:
+        _local.stream = prev
 
 
 def _ptr(t):
@@ -62,27 +88,44 @@ class DeviceSeries:
     """One series' inputs resident on the GPU, with its ``gk_system``."""
 
     def __init__(self, dip_positions, dip_gradients, nugget_grad, sp_coords, nugget_sp, points_per_surface,
-                 range, c_o, uni_degree=1, kernel="cubic", i_res=4.0, gi_res=2.0, device="cuda"):
+                 range, c_o, uni_degree=1, kernel="cubic", i_res=4.0, gi_res=2.0, device="cuda",
+                 ref_index=None, rest_index=None, ref_points=None):
+        """Inputs are numpy arrays (uploaded here) or CUDA tensors already on
+        ``device`` (used as they are); ``ref_index``/``rest_index``/``ref_points``
+        may be given precomputed (device tensors) to avoid further uploads."""
         dev = torch.device(device)
-        f64 = lambda a: torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64)).to(dev)
+
+        def f64(a, shape=None):
+            if isinstance(a, torch.Tensor):
+                t = a.to(device=dev, dtype=torch.float64)
+            else:
+                t = torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64)).to(dev)
+            t = t.reshape(shape) if shape is not None else t
+            return t.contiguous()
+
         self.points_per_surface = np.asarray(points_per_surface, dtype=np.int64)
-        ref, rest = ref_rest_indices(self.points_per_surface)
-        self.dip_positions = f64(np.reshape(dip_positions, (-1, 3)))
-        self.dip_gradients = f64(np.reshape(dip_gradients, (-1, 3)))
+        self.dip_positions = f64(dip_positions, (-1, 3))
+        self.dip_gradients = f64(dip_gradients, (-1, 3))
         self.nugget_grad = f64(nugget_grad)
-        self.sp_coords = f64(np.reshape(sp_coords, (-1, 3)))
+        self.sp_coords = f64(sp_coords, (-1, 3))
         self.nugget_sp = f64(nugget_sp)
-        self.ref_index = torch.as_tensor(ref).to(dev)
-        self.rest_index = torch.as_tensor(rest).to(dev)
-        starts = np.concatenate([[0], np.cumsum(self.points_per_surface)[:-1]]).astype(np.int64)
-        self.ref_points = self.sp_coords[torch.as_tensor(starts).to(dev)].contiguous() \
-            if len(starts) else self.sp_coords[:0]
+        if ref_index is None or rest_index is None:
+            ref, rest = ref_rest_indices(self.points_per_surface)
+            ref_index, rest_index = torch.as_tensor(ref).to(dev), torch.as_tensor(rest).to(dev)
+        self.ref_index = ref_index
+        self.rest_index = rest_index
+        n_iface = int(ref_index.shape[0])
+        if ref_points is None:
+            starts = np.concatenate([[0], np.cumsum(self.points_per_surface)[:-1]]).astype(np.int64)
+            ref_points = self.sp_coords[torch.as_tensor(starts).to(dev)].contiguous() \
+                if len(starts) else self.sp_coords[:0]
+        self.ref_points = ref_points
         self.device = dev
         self.sys = GkSystem()
         s = self.sys
         s.n_ori = int(self.dip_positions.shape[0])
         s.n_sp = int(self.sp_coords.shape[0])
-        s.n_iface = int(len(ref))
+        s.n_iface = n_iface
         s.uni_degree = int(uni_degree)
         s.kernel = kernel_id(kernel)
         s.range, s.c_o, s.i_res, s.gi_res = float(range), float(c_o), float(i_res), float(gi_res)
@@ -199,6 +242,49 @@ def solve_mixed(series: DeviceSeries, tol=1e-12, max_iter=30, K=None, b=None):
     check("gk_solve_mixed", lib.gk_solve_mixed(n, _ptr(K), K.stride(0), _ptr(b), _ptr(x), float(tol),
                                                int(max_iter), _ptr(work), wb, _ptr(info), _stream()))
     return x, info
+
+
+def solve_mixed_cta(series: DeviceSeries, tol=1e-12, max_iter=60, K=None, b=None):
+    """The mixed solve of a small system (N <= GK_CTA_MAX_N) in one thread
+    block: one launch, no host synchronisation; (x, info)."""
+    lib = _lib.load()
+    if K is None:
+        K, b = build(series, GK_F64)
+    n = K.shape[0]
+    wb = lib.gk_solve_mixed_cta_workspace_bytes(n, K.stride(0))
+    if wb == 0:
+        raise ValueError(f"system of {n} unknowns is above GK_CTA_MAX_N")
+    work = torch.empty(wb, dtype=torch.uint8, device=K.device)
+    x = torch.empty(n, dtype=torch.float64, device=K.device)
+    info = new_info(K.device)
+    check("gk_solve_mixed_cta", lib.gk_solve_mixed_cta(n, _ptr(K), K.stride(0), _ptr(b), _ptr(x), float(tol),
+                                                       int(max_iter), _ptr(work), wb, _ptr(info), _stream()))
+    return x, info
+
+
+def solve_mixed_cta_many(systems, tol=1e-12, max_iter=60):
+    """Small independent systems ``[(K, b), ...]`` solved in one launch (one
+    thread block each, ``gk_solve_mixed_cta_many``); [(x, info), ...]."""
+    lib = _lib.load()
+    out, jobs, keep = [], [], []
+    for K, b in systems:
+        n = K.shape[0]
+        wb = lib.gk_solve_mixed_cta_workspace_bytes(n, K.stride(0))
+        if wb == 0:
+            raise ValueError(f"system of {n} unknowns is above GK_CTA_MAX_N")
+        work = torch.empty(wb, dtype=torch.uint8, device=K.device)
+        x = torch.empty(n, dtype=torch.float64, device=K.device)
+        info = new_info(K.device)
+        jobs.append(_lib.GkCtaJob(n, K.data_ptr(), K.stride(0), b.data_ptr(), x.data_ptr(), work.data_ptr(), wb,
+                                  info.data_ptr()))
+        keep.append(work)
+        out.append((x, info))
+    for c0 in range(0, len(jobs), _lib.GK_CTA_MAX_JOBS):
+        chunk = jobs[c0:c0 + _lib.GK_CTA_MAX_JOBS]
+        arr = (_lib.GkCtaJob * len(chunk))(*chunk)
+        check("gk_solve_mixed_cta_many", lib.gk_solve_mixed_cta_many(len(chunk), arr, float(tol), int(max_iter),
+                                                                     _stream()))
+    return out
 
 
 def gemv(K, x):
@@ -396,11 +482,92 @@ def evaluate(series: DeviceSeries, model, pts: Points, prec=GK_F64, seg=None, gr
         if values is None:
             values = torch.empty(n, dtype=torch.float64, device=dev)
     if seg is not None and want_ids:
-        ids = torch.empty(n, dtype=torch.int32, device=dev)
+        ids = o.get("ids")
+        if ids is None:
+            ids = torch.empty(n, dtype=torch.int32, device=dev)
     check("gk_eval", lib.gk_eval(ctypes.byref(series.sys), _ptr(model), ctypes.byref(pts.gk), prec,
                                  ctypes.byref(seg) if seg is not None else None, _ptr(field), _ptr(grad),
                                  _ptr(values), _ptr(ids), _ptr(info), _stream()))
     return field, grad, values, ids
+
+
+class SeriesSet:
+    """The series of one model prepared for ``gk_eval_series_set``: one
+    ``gk_series_eval`` per series (system, packed model, segmentation,
+    relation, fault sources, extreme isovalues), built once and reused for
+    every point set."""
+
+    def __init__(self, items):
+        """items: (DeviceSeries, model, GkSegment, relation, fault_sources, min_iso, max_iso) per series."""
+        n = len(items)
+        if not 1 <= n <= _lib.GK_MAX_SURFACES:
+            raise ValueError("1 .. GK_MAX_SURFACES series")
+        self.items = items
+        self.arr = (_lib.GkSeriesEval * n)()
+        for i, (ds, model, seg, rel, faults, mn, mx) in enumerate(items):
+            e = self.arr[i]
+            e.sys = ctypes.pointer(ds.sys)
+            e.model = model.data_ptr()
+            e.seg = seg
+            e.relation = int(rel)
+            e.n_faults = len(faults)
+            for f, j in enumerate(faults):
+                e.faults[f] = int(j)
+            e.min_iso, e.max_iso = float(mn), float(mx)
+        self.n = n
+        self.device = items[0][0].device
+
+    def set_slope(self, slope):
+        for i in range(self.n):
+            self.arr[i].seg.slope = float(slope)
+
+    def evaluate(self, pts: Points, prec, combine=True, info=None):
+        """fields, values, ids (n_series x n), block, lith ids, masks."""
+        lib = _lib.load()
+        n, dev, ns = pts.n, self.device, self.n
+        # one allocation, carved into the outputs (8-byte aligned pieces)
+        sizes = [8 * ns * n, 8 * ns * n, 4 * ns * n] + ([8 * n, 4 * n, ns * n] if combine else [])
+        offs = [0]
+        for b in sizes:
+            offs.append(offs[-1] + (b + 255) // 256 * 256)
+        buf = torch.empty(offs[-1], dtype=torch.uint8, device=dev)
+        piece = lambda i, dt, shape: buf[offs[i]:offs[i] + sizes[i]].view(dt).view(shape)
+        F = piece(0, torch.float64, (ns, n))
+        V = piece(1, torch.float64, (ns, n))
+        I = piece(2, torch.int32, (ns, n))
+        B = L = M = None
+        if combine:
+            B = piece(3, torch.float64, (n,))
+            L = piece(4, torch.int32, (n,))
+            M = piece(5, torch.uint8, (ns, n))
+        check("gk_eval_series_set", lib.gk_eval_series_set(self.n, self.arr, ctypes.byref(pts.gk), prec, _ptr(F),
+                                                           _ptr(V), _ptr(I), _ptr(B), _ptr(L), _ptr(M),
+                                                           _ptr(info), _stream()))
+        self.last_buffer = (buf, offs, sizes, n)
+        return F, V, I, B, L, M
+
+    def views(self, buffer, layout):
+        """fields, values, ids, block, lith ids, masks as views of ``buffer``
+        (a torch tensor or numpy array of bytes laid out like the buffer of an
+        earlier ``evaluate``; ``layout`` = (offsets, sizes, n) of that call)."""
+        offs, sizes, n = layout
+        ns = self.n
+        torch_buf = isinstance(buffer, torch.Tensor)
+
+        def piece(i, dt, shape):
+            b = buffer[offs[i]:offs[i] + sizes[i]]
+            if torch_buf:
+                return b.view(dt).view(shape)
+            return b.view(_NP_OF[dt]).reshape(shape)
+        out = [piece(0, torch.float64, (ns, n)), piece(1, torch.float64, (ns, n)), piece(2, torch.int32, (ns, n))]
+        if len(sizes) > 3:
+            out += [piece(3, torch.float64, (n,)), piece(4, torch.int32, (n,)), piece(5, torch.uint8, (ns, n))]
+        else:
+            out += [None, None, None]
+        return tuple(out)
+
+
+_NP_OF = {torch.float64: np.float64, torch.int32: np.int32, torch.uint8: np.uint8}
 
 
 def combine(fields, values, ids, relations, min_iso, max_iso, want_masks=True):
@@ -421,10 +588,12 @@ def combine(fields, values, ids, relations, min_iso, max_iso, want_masks=True):
     return out_v, out_i, masks
 
 
-def octree_corners(centres, spacing):
+def octree_corners(centres, spacing, out=None):
+    """The 8 corners of every voxel (8n x 3), into ``out`` when given."""
     lib = _lib.load()
     n = centres.shape[0]
-    out = torch.empty((8 * n, 3), dtype=torch.float64, device=centres.device)
+    if out is None:
+        out = torch.empty((8 * n, 3), dtype=torch.float64, device=centres.device)
     sp = (ctypes.c_double * 3)(*[float(v) for v in spacing])
     check("gk_octree_corners", lib.gk_octree_corners(n, _ptr(centres), sp, _ptr(out), _stream()))
     return out
@@ -441,10 +610,13 @@ def octree_refine(centres, corner_ids, spacing, refine_all=False):
         corner_ids = corner_ids.reshape(-1, 8 * n).contiguous() if n else corner_ids
         n_sets = int(corner_ids.shape[0]) if n else 1
     dev = centres.device
-    children = torch.empty((8 * n, 3), dtype=torch.float64, device=dev)
-    count = torch.zeros(1, dtype=torch.int64, device=dev)
     wb = lib.gk_octree_workspace_bytes(n)
-    work = torch.empty(max(wb, 8), dtype=torch.uint8, device=dev)
+    # one allocation: children (8n x 3 FP64), the count (written by the scan), workspace
+    cb = 8 * n * 3 * 8
+    buf = torch.empty(cb + 256 + max(wb, 8), dtype=torch.uint8, device=dev)
+    children = buf[:cb].view(torch.float64).view(8 * n, 3)
+    count = buf[cb:cb + 8].view(torch.int64)
+    work = buf[cb + 256:]
     sp = (ctypes.c_double * 3)(*[float(v) for v in spacing])
     check("gk_octree_refine", lib.gk_octree_refine(n, _ptr(centres), _ptr(corner_ids), n_sets,
                                                    int(bool(refine_all)), sp, _ptr(children), _ptr(count),

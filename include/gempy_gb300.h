@@ -192,6 +192,44 @@ gk_status gk_solve_mixed(int64_t n, const double* K, int64_t ldk,
                          int32_t max_iter, void* work, size_t work_bytes,
                          gk_info* info, gk_stream stream);
 
+/* Single-CTA form of gk_solve_mixed for small systems (n <= GK_CTA_MAX_N),
+ * e.g. the series of an octree model (no reference counterpart beyond the
+ * FP64 solve it replaces): one thread block equilibrates K, factors an FP32
+ * copy without pivoting and runs FGMRES(30) in FP64 on the FP64 K with the
+ * Givens rotations and convergence tests on the device, so the call queues one
+ * launch and never synchronises the host.  A zero or non-finite pivot is
+ * reported as GK_ERR_SINGULAR (the caller then uses gk_solve_mixed, which
+ * refactors with partial pivoting).  FGMRES stops at
+ * ||b - K x||_2 <= tol ||b||_2, at ``max_iter`` steps or when a restart cycle
+ * gains less than 2 %; ``info`` (written by the kernel, may be NULL) reports
+ * status, iterations and the residual.  ``work``:
+ * gk_solve_mixed_cta_workspace_bytes(n, ldk) bytes (K's FP32 copy with the
+ * same leading dimension, Krylov vectors). */
+#define GK_CTA_MAX_N 4096
+size_t gk_solve_mixed_cta_workspace_bytes(int64_t n, int64_t ldk);
+gk_status gk_solve_mixed_cta(int64_t n, const double* K, int64_t ldk,
+                             const double* b, double* x, double tol,
+                             int32_t max_iter, void* work, size_t work_bytes,
+                             gk_info* info, gk_stream stream);
+
+/* Up to GK_CTA_MAX_JOBS independent systems (the series of one model) solved
+ * as gk_solve_mixed_cta in one launch, one thread block each.  ``jobs`` is a
+ * HOST array; each job's arguments mean what gk_solve_mixed_cta's do. */
+#define GK_CTA_MAX_JOBS 16
+typedef struct gk_cta_job {
+    int64_t n;
+    const double* K;
+    int64_t ldk;
+    const double* b;
+    double* x;
+    void* work;
+    size_t work_bytes;
+    gk_info* info;
+} gk_cta_job;
+gk_status gk_solve_mixed_cta_many(int32_t n_jobs, const gk_cta_job* jobs,
+                                  double tol, int32_t max_iter,
+                                  gk_stream stream);
+
 /* FGMRES on the FP64 system K x = b preconditioned by a two-level
  * "block-Jacobi plus low-rank" operator, for systems too large for an LU
  * preconditioner (no reference counterpart beyond the FP64 solve it
@@ -263,6 +301,29 @@ gk_status gk_eval(const gk_system* sys, const void* model,
                   const gk_segment* seg, double* field, double* grad,
                   double* values, int32_t* ids, gk_info* info,
                   gk_stream stream);
+
+/* Every series of a model at one point set, in stack order, then their
+ * combination (the engine's evaluation of all stacks at a grid, reached from
+ * ``compute_API.py:68-73``): series i is evaluated as by gk_eval with its
+ * segmentation, the soft values of the FAULT series listed in ``faults``
+ * serving as its fault blocks (each must be an older series), into row i of
+ * ``fields``, ``values`` and ``ids`` (n_series x n); then gk_combine_series
+ * writes ``block``, ``lith_ids`` and ``masks`` (any may be NULL: no
+ * combination).  ``series`` is a HOST array. */
+typedef struct gk_series_eval {
+    const gk_system* sys;       /* HOST                                      */
+    const void* model;          /* packed model (gk_eval_prepare)           */
+    gk_segment seg;
+    int32_t relation;           /* 1 ERODE, 2 ONLAP, 3 FAULT, 4 BASEMENT     */
+    int32_t n_faults;           /* == sys->n_fault                           */
+    int32_t faults[GK_MAX_FAULTS];  /* indices of the offsetting series     */
+    double min_iso, max_iso;    /* the series' extreme isovalues             */
+} gk_series_eval;
+gk_status gk_eval_series_set(int32_t n_series, const gk_series_eval* series,
+                             const gk_points* pts, gk_prec prec,
+                             double* fields, double* values, int32_t* ids,
+                             double* block, int32_t* lith_ids,
+                             uint8_t* masks, gk_info* info, gk_stream stream);
 
 /* Combination of series with the squeezed masks (ERODE / ONLAP / FAULT /
  * BASEMENT, ``gempy/core/data/structural_frame.py:326-330``; a FAULT series

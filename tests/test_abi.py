@@ -80,6 +80,8 @@ int main(void) {
   printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(gk_info), sizeof(gk_system), sizeof(gk_points),
          sizeof(gk_segment), sizeof(gk_mlp), sizeof(gk_adam), offsetof(gk_mlp, params), offsetof(gk_system, range),
          offsetof(gk_system, fault_sp), offsetof(gk_points, fault_values), offsetof(gk_points, fault_ld));
+  printf("%zu %zu %zu %zu\\n", sizeof(gk_series_eval), offsetof(gk_series_eval, min_iso), sizeof(gk_cta_job),
+         offsetof(gk_cta_job, info));
   return 0;
 }
 """)
@@ -89,7 +91,9 @@ int main(void) {
     want = [ctypes.sizeof(_lib.GkInfo), ctypes.sizeof(_lib.GkSystem), ctypes.sizeof(_lib.GkPoints),
             ctypes.sizeof(_lib.GkSegment), ctypes.sizeof(_lib.GkMlp), ctypes.sizeof(_lib.GkAdam),
             _lib.GkMlp.params.offset, _lib.GkSystem.range.offset, _lib.GkSystem.fault_sp.offset,
-            _lib.GkPoints.fault_values.offset, _lib.GkPoints.fault_ld.offset]
+            _lib.GkPoints.fault_values.offset, _lib.GkPoints.fault_ld.offset,
+            ctypes.sizeof(_lib.GkSeriesEval), _lib.GkSeriesEval.min_iso.offset, ctypes.sizeof(_lib.GkCtaJob),
+            _lib.GkCtaJob.info.offset]
     assert got == want
 
 

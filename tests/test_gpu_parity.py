@@ -201,6 +201,39 @@ def test_eval_ff_precision_workload_subsample():
     assert e_32 > 1e-6   # documents why the mixed form evaluates in float-float
 
 
+@pytest.mark.parametrize("n", [1, 5, 257, 3000, 20000])
+def test_eval_record_split_small_point_sets(n):
+    """Point sets too small to fill the GPU share each chunk of points among
+    the CTAs of a cluster (records split, partials added in rank order): every
+    precision still matches the oracle, and two runs agree bit for bit.  The
+    series has 5500 records, enough for every split size."""
+    from gempy_gb300 import kernels as K
+    from gempy_gb300 import synthetic
+    m = synthetic.precision(resolution=(8, 8, 8))
+    (s,) = oracle_series_list(m)
+    w = kriging.solve(*kriging.build_system(s))
+    rng = np.random.default_rng(n)
+    x = rng.uniform(-0.5, 0.5, (n, 3))
+    x[0] = s.sp_coords[0]
+    Zr, Gr = kriging.evaluate(s, w, x, gradient=True)
+    scale_z, scale_g = np.abs(Zr).max(), np.abs(Gr).max()
+    Z, G = _eval_gpu(s, w, x, K.GK_F64, gradient=True)
+    assert np.abs(Z - Zr).max() <= 1e-9 * scale_z
+    assert np.abs(G - Gr).max() <= 1e-9 * scale_g
+    (Z64,) = _eval_gpu(s, w, x, K.GK_F64)
+    assert np.abs(Z64 - Zr).max() <= 1e-9 * scale_z
+    (Zff,) = _eval_gpu(s, w, x, K.GK_FF)
+    assert np.abs(Zff - Zr).max() <= 1e-9 * scale_z
+    (Zff2,) = _eval_gpu(s, w, x, K.GK_FF)
+    np.testing.assert_array_equal(Zff, Zff2)
+    alpha = kriging.point_coefficients(s, w)
+    cancel = (s.c_o * s.gi_res * (np.abs(alpha).sum() + np.abs(w[:3 * s.n_o]).sum() * 14 / s.range) / scale_z)
+    Z32, G32 = _eval_gpu(s, w, x, K.GK_F32, gradient=True)
+    assert np.abs(Z32 - Zr).max() <= 1e-6 * cancel * scale_z
+    (Z32n,) = _eval_gpu(s, w, x, K.GK_F32)
+    assert np.abs(Z32n - Zr).max() <= 1e-6 * cancel * scale_z
+
+
 @pytest.mark.parametrize("case", ["anticline", "random_deg2_cubic", "random_deg0_exp"])
 def test_eval_f32_field_and_gradient_bounded(case):
     """Plain FP32 evaluation: accurate to ~1e-7 times the cancellation factor."""
@@ -363,6 +396,41 @@ def test_compute_model_fault_model_pins():
     series, rels, fr = inputs.series_from_golden(g)
     m = pipeline.Model(series, rels, g["unit_values"], g["sigmoid_slope"], fr)
     np.testing.assert_allclose(sol.scalar_field_at_surface_points, np.concatenate(m.isos), rtol=1e-9, atol=1e-12)
+
+
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_compute_model_keep_on_device_matches_host_outputs(dtype):
+    """The device-resident result (torch tensors) and the host result (numpy
+    views of the staged copies) hold the same arrays, level by level."""
+    import gempy_gb300 as gg
+    g = load_golden("fault_model.json")
+    ii, opts, dd, ext = engine_inputs_from_golden(g)
+    host = gg.compute_model(ii, opts, dd, config=gg.EngineConfig(dtype=dtype))
+    dev = gg.compute_model(ii, opts, dd, config=gg.EngineConfig(dtype=dtype, keep_on_device=True))
+    assert len(host.octrees_output) == len(dev.octrees_output) == g["octree"]["levels"]
+
+    def same(a, b):
+        if a is None or b is None:
+            assert a is None and b is None
+            return
+        assert isinstance(a, np.ndarray) and isinstance(b, torch.Tensor)
+        np.testing.assert_array_equal(a, b.cpu().numpy())
+
+    for lh, ld in zip(host.octrees_output, dev.octrees_output):
+        same(lh.grid_centers, ld.grid_centers)
+        same(lh.grid_corners, ld.grid_corners)
+        for oh, od in zip(lh.outputs, ld.outputs):
+            same(oh.exported_fields.scalar_field, od.exported_fields.scalar_field)
+            same(oh.values_block, od.values_block)
+            same(oh.mask, od.mask)
+        for ch, cd in [(lh.last_output_center, ld.last_output_center),
+                       (lh.last_output_corners, ld.last_output_corners)]:
+            if ch is None:
+                assert cd is None
+                continue
+            same(ch.block, cd.block)
+            same(ch.ids_block, cd.ids_block)
+            same(ch.mask_matrix, cd.mask_matrix)
 
 
 def test_compute_model_combination_model_matches_oracle():
