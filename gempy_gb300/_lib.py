@@ -85,6 +85,13 @@ class GkSeriesEval(ctypes.Structure):
                 ("max_iso", ctypes.c_double)]
 
 
+class GkOctreeLevelLayout(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64), ("n_points", ctypes.c_int64), ("n_series", ctypes.c_int32),
+                ("corners", ctypes.c_int32), ("refine", ctypes.c_int32), ("reserved", ctypes.c_int32)] + \
+               [(k, ctypes.c_uint64) for k in ("points", "fields", "values", "ids", "block", "lith_ids", "masks",
+                                               "children", "count", "work", "total")]
+
+
 class GkCtaJob(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int64), ("K", ctypes.c_void_p), ("ldk", ctypes.c_int64), ("b", ctypes.c_void_p),
                 ("x", ctypes.c_void_p), ("work", ctypes.c_void_p), ("work_bytes", ctypes.c_size_t),
@@ -160,6 +167,11 @@ SIGNATURES = [
     ("gk_octree_refine", ctypes.c_int, [ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
                                         ctypes.c_int32, c_double_p, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    ("gk_octree_level_plan", ctypes.c_int, [ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
+                                              ctypes.POINTER(GkOctreeLevelLayout)]),
+    ("gk_octree_level", ctypes.c_int, [ctypes.c_int32, ctypes.POINTER(GkSeriesEval), ctypes.c_void_p, c_double_p,
+                                       ctypes.c_int, ctypes.c_int32, c_int32_p, ctypes.POINTER(GkOctreeLevelLayout),
+                                       ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]),
     ("gk_batch_workspace_bytes", ctypes.c_size_t, [ctypes.POINTER(GkBatch)]),
     ("gk_batch_points", ctypes.c_int64, [ctypes.POINTER(GkBatch)]),
     ("gk_batch_plan", ctypes.c_int, [ctypes.POINTER(GkBatch), ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),

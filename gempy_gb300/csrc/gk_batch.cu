@@ -190,12 +190,39 @@ struct CtaSolveShared {
     double hcol[kBatchRestart + 2];
 };
 
+// Systems up to kSmemLuMaxN keep their equilibrated FP32 matrix in shared
+// memory (N x (N + 1) floats, then 3N floats of scratch); up to kRegInvMaxN it
+// is inverted there by register-resident Gauss-Jordan and every
+// preconditioner application is one FP32 matrix-vector product, above that it
+// is LU-factored in place and applied by triangular sweeps.
+constexpr int kSmemLuMaxN = 224;
+constexpr int kRegInvMaxN = 160;
+__host__ __device__ constexpr size_t cta_smem_lu_bytes(int n) {
+    return ((size_t)n * (n + 1) + 3 * (size_t)n) * sizeof(float);
+}
+
+// 2^-floor(e/2) for the binary exponent e of |v| (v >= 0, finite or not):
+// a power-of-two row scale near 1/sqrt(max|row|), from the bits alone -- the
+// FP64 pipe is ~1/64 of the FP32 one, and its sqrt and division sequences
+// dominated the equilibration.  Zero rows keep scale 1.
+__device__ __forceinline__ double pow2_rsqrt_scale(unsigned long long bits) {
+    const int e = (int)((bits >> 52) & 0x7ff);
+    if (e == 0) return 1.0;                       // zero or subnormal
+    const int ub = e - 1023;                      // |v| in [2^ub, 2^(ub+1))
+    const int h = ub >= 0 ? ub / 2 : -((-ub + 1) / 2);   // floor(ub / 2)
+    return __longlong_as_double((long long)(1023 - h) << 52);
+}
+
 // The whole mixed solve of one system by the calling CTA: symmetric
-// equilibration, FP32 LU without pivoting, FGMRES(30) in FP64 preconditioned
-// by the FP32 factors with Givens rotations and convergence tests on the
-// device.  Returns the status, iteration count and final relative residual.
+// equilibration by powers of two, an FP32 preconditioner without pivoting,
+// FGMRES(30) in FP64 with Givens rotations and convergence tests on the
+// device.  When ``sm`` is given the FP32 matrix lives in shared memory
+// (leading dimension ``sld``, then 3N floats of scratch) and is inverted
+// (N <= kRegInvMaxN) or LU-factored there; otherwise it is LU-factored in the
+// global workspace.  Returns the status, iteration count and final relative
+// residual.
 __device__ void cta_mixed_solve(const CtaSystem& d, double tol, int max_iter, CtaSolveShared& sh, int& status_out,
-                                int& its_out, double& rel_out) {
+                                int& its_out, double& rel_out, float* sm = nullptr, int sld = 0) {
     auto& Ds = sh.Ds;
     double* red = sh.red;
     float* xs = sh.xs;
@@ -208,28 +235,39 @@ __device__ void cta_mixed_solve(const CtaSystem& d, double tol, int max_iter, Ct
     double* hcol = sh.hcol;
     const int tid = threadIdx.x, nt = blockDim.x;
     const int N = d.N, ld = d.ld;
-    // equilibration and FP32 copy
+    // equilibration (row and column scales, powers of two) and FP32 copy
     {
         const int lane = tid & 31, wid = tid >> 5;
         for (int row = wid; row < N; row += nt >> 5) {
-            const double* k = d.K64 + (int64_t)row * ld;
-            double m = 0.0;
-            for (int j = lane; j < N; j += 32) m = fmax(m, fabs(k[j]));
-            for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
-            if (lane == 0) d.dsc[row] = m > 0.0 ? 1.0 / sqrt(m) : 1.0;
+            const unsigned long long* k = reinterpret_cast<const unsigned long long*>(d.K64 + (int64_t)row * ld);
+            unsigned long long m = 0;   // max |K_ij| compared as bit patterns (sign cleared)
+            for (int j = lane; j < N; j += 32) m = max(m, k[j] & 0x7fffffffffffffffULL);
+            for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_down_sync(0xffffffffu, m, o));
+            if (lane == 0) d.dsc[row] = pow2_rsqrt_scale(m);
         }
         __syncthreads();
         for (int row = wid; row < N; row += nt >> 5) {
-            const double di = d.dsc[row];
+            const float di = (float)d.dsc[row];
             const double* k = d.K64 + (int64_t)row * ld;
-            float* k32 = d.K32 + (int64_t)row * ld;
-            for (int j = lane; j < N; j += 32) k32[j] = (float)(di * k[j] * d.dsc[j]);
+            float* k32 = sm ? sm + (int64_t)row * sld : d.K32 + (int64_t)row * ld;
+            // scaling by powers of two is exact: one rounding, in the conversion
+            for (int j = lane; j < N; j += 32) k32[j] = (float)k[j] * (di * (float)d.dsc[j]);
         }
         __syncthreads();
     }
     int status = GK_OK, its = 0;
     double rel = 1.0;
-    if (!cta_lu_nopiv(d.K32, ld, N, Ds, &s_bad)) {
+    float* const K32 = sm ? sm : d.K32;
+    const int ld32 = sm ? sld : ld;
+    float* const t32 = sm ? sm + (int64_t)N * sld : d.t32;
+    const bool inverse = sm != nullptr && N <= kRegInvMaxN;
+    bool factored;
+    if (inverse)
+        factored = N <= 128 ? cta_gauss_jordan_regs<8, 4>(K32, ld32, N, t32 + N, t32 + 2 * N)
+                            : cta_gauss_jordan_regs<10, 5>(K32, ld32, N, t32 + N, t32 + 2 * N);
+    else
+        factored = cta_lu_nopiv(K32, ld32, N, Ds, &s_bad);
+    if (!factored) {
         status = GK_ERR_SINGULAR;
     } else {
         // FGMRES(restart) in FP64
@@ -244,8 +282,15 @@ __device__ void cta_mixed_solve(const CtaSystem& d, double tol, int max_iter, Ct
         double prev = INFINITY;
         status = GK_ERR_NOT_CONVERGED;
         if (!(bn > 0.0)) { status = GK_OK; rel = 0.0; }
+        bool x_zero = true;   // the first residual is b itself
         while (status == GK_ERR_NOT_CONVERGED && its < max_iter) {
-            cta_gemv64(d.K64, ld, N, d.x, d.b, d.r);
+            if (x_zero) {
+                for (int i = tid; i < N; i += nt) d.r[i] = d.b[i];
+                __syncthreads();
+                x_zero = false;
+            } else {
+                cta_gemv64(d.K64, ld, N, d.x, d.b, d.r);
+            }
             double s = 0.0;
             for (int i = tid; i < N; i += nt) s += d.r[i] * d.r[i];
             const double beta = sqrt(block_sum(s, red));
@@ -254,7 +299,8 @@ __device__ void cta_mixed_solve(const CtaSystem& d, double tol, int max_iter, Ct
             if (rel <= tol) { status = GK_OK; break; }
             if (rel > 0.98 * prev) break;
             prev = rel;
-            for (int i = tid; i < N; i += nt) d.V[i] = d.r[i] / beta;
+            const double ibeta = 1.0 / beta;
+            for (int i = tid; i < N; i += nt) d.V[i] = d.r[i] * ibeta;
             if (tid == 0) { for (int q = 0; q <= kBatchRestart; ++q) g[q] = 0.0; g[0] = beta; }
             __syncthreads();
             int j = 0;
@@ -262,10 +308,22 @@ __device__ void cta_mixed_solve(const CtaSystem& d, double tol, int max_iter, Ct
             for (; j < kBatchRestart && its < max_iter; ++j, ++its) {
                 const double* vj = d.V + (int64_t)j * N;
                 double* zj = d.Z + (int64_t)j * N;
-                for (int i = tid; i < N; i += nt) d.t32[i] = (float)(d.dsc[i] * vj[i]);
+                for (int i = tid; i < N; i += nt) t32[i] = (float)vj[i] * (float)d.dsc[i];
                 __syncthreads();
-                cta_lu_solve(d.K32, ld, N, d.t32, xs);
-                for (int i = tid; i < N; i += nt) zj[i] = d.dsc[i] * (double)d.t32[i];
+                if (inverse) {
+                    // z = D Kinv D v: warp per row of the inverse
+                    const int lane = tid & 31, wid = tid >> 5;
+                    for (int row = wid; row < N; row += nt >> 5) {
+                        const float* ar = K32 + (int64_t)row * ld32;
+                        float acc = 0.f;
+                        for (int c = lane; c < N; c += 32) acc = fmaf(ar[c], t32[c], acc);
+                        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+                        if (lane == 0) zj[row] = d.dsc[row] * (double)acc;
+                    }
+                } else {
+                    cta_lu_solve(K32, ld32, N, t32, xs);
+                    for (int i = tid; i < N; i += nt) zj[i] = d.dsc[i] * (double)t32[i];
+                }
                 __syncthreads();
                 cta_gemv64(d.K64, ld, N, zj, nullptr, d.w);
                 // CGS2: warp w computes the dot products c = w, w + 16, ...
@@ -294,8 +352,10 @@ __device__ void cta_mixed_solve(const CtaSystem& d, double tol, int max_iter, Ct
                 double sn2 = 0.0;
                 for (int i = tid; i < N; i += nt) sn2 += d.w[i] * d.w[i];
                 const double hn = sqrt(block_sum(sn2, red));
-                if (hn > 0.0)
-                    for (int i = tid; i < N; i += nt) d.V[(int64_t)(j + 1) * N + i] = d.w[i] / hn;
+                if (hn > 0.0) {
+                    const double ihn = 1.0 / hn;
+                    for (int i = tid; i < N; i += nt) d.V[(int64_t)(j + 1) * N + i] = d.w[i] * ihn;
+                }
                 if (tid == 0) {
                     hcol[j + 1] = hn;
                     for (int i = 0; i < j; ++i) {
@@ -303,9 +363,10 @@ __device__ void cta_mixed_solve(const CtaSystem& d, double tol, int max_iter, Ct
                         hcol[i + 1] = -sn[i] * hcol[i] + cs[i] * hcol[i + 1];
                         hcol[i] = t;
                     }
-                    double den = hypot(hcol[j], hcol[j + 1]);
-                    cs[j] = den > 0 ? hcol[j] / den : 1.0;
-                    sn[j] = den > 0 ? hcol[j + 1] / den : 0.0;
+                    const double den = hypot(hcol[j], hcol[j + 1]);
+                    const double iden = den > 0 ? 1.0 / den : 0.0;
+                    cs[j] = den > 0 ? hcol[j] * iden : 1.0;
+                    sn[j] = hcol[j + 1] * iden;
                     hcol[j] = den;
                     g[j + 1] = -sn[j] * g[j];
                     g[j] = cs[j] * g[j];
@@ -382,12 +443,15 @@ struct CtaJobs {
     gk_info* info[kCtaJobs];
 };
 
+// sld > 0: every system fits kSmemLuMaxN and the dynamic shared memory holds
+// its FP32 matrix and factors (leading dimension sld) and N floats.
 __global__ void __launch_bounds__(kSolveThreads) mixed_cta_kernel(const __grid_constant__ CtaJobs jobs, double tol,
-                                                                  int max_iter) {
+                                                                  int max_iter, int sld) {
     __shared__ CtaSolveShared sh;
+    extern __shared__ float cta_dyn[];
     int status, its;
     double rel;
-    cta_mixed_solve(jobs.sys[blockIdx.x], tol, max_iter, sh, status, its, rel);
+    cta_mixed_solve(jobs.sys[blockIdx.x], tol, max_iter, sh, status, its, rel, sld > 0 ? cta_dyn : nullptr, sld);
     gk_info* info = jobs.info[blockIdx.x];
     if (threadIdx.x == 0 && info != nullptr) {
         info->status = status;
@@ -985,7 +1049,21 @@ extern "C" gk_status gk_solve_mixed_cta_many(int32_t n_jobs, const gk_cta_job* j
         if (st != GK_OK) return st;
         J.info[i] = jobs[i].info;
     }
-    mixed_cta_kernel<<<n_jobs, kSolveThreads, 0, (cudaStream_t)stream>>>(J, tol, max_iter);
+    int n_max = 0;
+    for (int i = 0; i < n_jobs; ++i) n_max = std::max(n_max, J.sys[i].N);
+    int sld = 0;
+    size_t smem = 0;
+    if (n_max <= kSmemLuMaxN) {
+        sld = n_max + 1;
+        smem = cta_smem_lu_bytes(n_max);
+        int occ = 0;
+        if (cached_occupancy((const void*)mixed_cta_kernel, kSolveThreads, smem, occ) != GK_OK) {
+            (void)cudaGetLastError();
+            sld = 0;
+            smem = 0;
+        }
+    }
+    mixed_cta_kernel<<<n_jobs, kSolveThreads, smem, (cudaStream_t)stream>>>(J, tol, max_iter, sld);
     GK_LAUNCH_CHECK();
     return GK_OK;
 }

@@ -1,6 +1,8 @@
 // In-CTA dense kernels shared by the batched solver (gk_batch.cu) and the
 // two-level preconditioner (gk_lu.cu): blocked LU without pivoting of an
-// FP32 or FP64 matrix in global memory by one CTA, and the matching triangular solves.
+// FP32 or FP64 matrix by one CTA, and the matching triangular solves (the
+// matrix may sit in global or in shared memory: generic addressing); and a
+// register-resident Gauss-Jordan inversion of a small FP32 matrix.
 #pragma once
 
 #include "gk_common.cuh"
@@ -187,6 +189,77 @@ static __device__ void cta_lu_solve(const T* A, int ld, int N, T* t, T* xs) {
         }
         __syncthreads();
     }
+}
+
+// In-CTA Gauss-Jordan inversion without pivoting of the N x N FP32 matrix A
+// (shared memory, leading dimension lda), in place, for N <= 16 RA and
+// N <= 32 CB with 512 threads.  During the elimination the matrix lives in
+// registers: warp ty owns rows ty + 16 r, lane tx columns tx + 32 c.  Step k
+// publishes pivot row k and column k in shared memory (rowbuf, colbuf: N
+// floats each) and updates every owned element with one FMA; the owners of
+// row k (one warp) and of column k (one lane per warp) then overwrite theirs.
+// The pivots are those of LU without pivoting.  Returns false on a zero or
+// non-finite pivot (every thread sees the same pivot).
+template <int RA, int CB>
+static __device__ __noinline__ bool cta_gauss_jordan_regs(float* A, int lda, int N, float* rowbuf, float* colbuf) {
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    float a[RA][CB];
+#pragma unroll
+    for (int r = 0; r < RA; ++r)
+#pragma unroll
+        for (int c = 0; c < CB; ++c) {
+            const int i = ty + 16 * r, j = tx + 32 * c;
+            a[r][c] = (i < N && j < N) ? A[(int64_t)i * lda + j] : 0.f;
+        }
+    bool ok = true;
+    for (int k = 0; k < N; ++k) {
+#pragma unroll
+        for (int r = 0; r < RA; ++r)
+            if (ty + 16 * r == k)   // warp-uniform
+#pragma unroll
+                for (int c = 0; c < CB; ++c)
+                    if (tx + 32 * c < N) rowbuf[tx + 32 * c] = a[r][c];
+#pragma unroll
+        for (int c = 0; c < CB; ++c)
+            if (tx + 32 * c == k)
+#pragma unroll
+                for (int r = 0; r < RA; ++r)
+                    if (ty + 16 * r < N) colbuf[ty + 16 * r] = a[r][c];
+        __syncthreads();
+        const float p = colbuf[k];
+        if (!(fabsf(p) > 0.f) || !(fabsf(p) < INFINITY)) { ok = false; break; }
+        const float ip = 1.f / p;
+        float rv[CB], cv[RA];
+#pragma unroll
+        for (int c = 0; c < CB; ++c) rv[c] = tx + 32 * c < N ? rowbuf[tx + 32 * c] * ip : 0.f;
+#pragma unroll
+        for (int r = 0; r < RA; ++r) cv[r] = ty + 16 * r < N ? colbuf[ty + 16 * r] : 0.f;
+#pragma unroll
+        for (int r = 0; r < RA; ++r)
+#pragma unroll
+            for (int c = 0; c < CB; ++c) a[r][c] = fmaf(-cv[r], rv[c], a[r][c]);
+#pragma unroll
+        for (int r = 0; r < RA; ++r)
+            if (ty + 16 * r == k)
+#pragma unroll
+                for (int c = 0; c < CB; ++c) a[r][c] = rv[c];
+#pragma unroll
+        for (int c = 0; c < CB; ++c)
+            if (tx + 32 * c == k)
+#pragma unroll
+                for (int r = 0; r < RA; ++r) a[r][c] = ty + 16 * r == k ? ip : -cv[r] * ip;
+        __syncthreads();   // rowbuf / colbuf are rewritten by the next step
+    }
+    if (!ok) return false;
+#pragma unroll
+    for (int r = 0; r < RA; ++r)
+#pragma unroll
+        for (int c = 0; c < CB; ++c) {
+            const int i = ty + 16 * r, j = tx + 32 * c;
+            if (i < N && j < N) A[(int64_t)i * lda + j] = a[r][c];
+        }
+    __syncthreads();
+    return true;
 }
 
 }  // namespace gk

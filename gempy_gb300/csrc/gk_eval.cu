@@ -744,7 +744,7 @@ static void plan_tiles(EvalParams& P, int stage_bytes, int rec_bytes_ori, int re
 }
 
 constexpr int kMaxSplit = 16;          // cluster sizes above 8 are opted into per kernel
-constexpr int kMinSplitRecords = 48;   // records per rank below which a split does not pay
+constexpr int kMinSplitRecords = 8;    // records per rank below which a split does not pay
 
 // Launches `kernel` over the chunks of P or, when the chunks alone would fill
 // less than half of the GPU, `split_kernel` with the records split over a

@@ -7,6 +7,8 @@
 // parent order, which matches the point order of the reference's approved
 // anticline and fault-model scalar fields
 // (test/test_model_types/test_example_models_I.py:19-23, 41-68).
+#include <cstring>
+
 #include "gk_common.cuh"
 
 namespace gk {
@@ -31,13 +33,20 @@ __global__ void corners_kernel(int64_t n, const double* __restrict__ c, double h
 }
 
 constexpr int kScanBlock = 256;
+constexpr int kMaxIdSets = 1 + GK_MAX_SURFACES;
 
-// voxel v is marked when its 8 corners differ in any of the n_sets id arrays
-// (set s at ids + s * 8n)
-__device__ __forceinline__ int voxel_marked(const int32_t* __restrict__ ids, int n_sets, int64_t n, int64_t v) {
+// The id arrays a voxel's refinement looks at: set s holds the 8 corner ids
+// of voxel v at p[s][8 v .. 8 v + 7].
+struct IdSets {
+    const int32_t* p[kMaxIdSets];
+    int n;
+};
+
+// voxel v is marked when its 8 corners differ in any id set
+__device__ __forceinline__ int voxel_marked(const IdSets& ids, int64_t v) {
     int m = 0;
-    for (int s = 0; s < n_sets && !m; ++s) {
-        const int32_t* c = ids + (int64_t)s * 8 * n + 8 * v;
+    for (int s = 0; s < ids.n && !m; ++s) {
+        const int32_t* c = ids.p[s] + 8 * v;
         const int32_t a = c[0];
         for (int k = 1; k < 8; ++k) m |= (c[k] != a);
     }
@@ -45,11 +54,10 @@ __device__ __forceinline__ int voxel_marked(const int32_t* __restrict__ ids, int
 }
 
 // per-block count of marked voxels
-__global__ void mark_count_kernel(int64_t n, const int32_t* __restrict__ ids, int n_sets, int refine_all,
-                                  int64_t* __restrict__ block_counts) {
+__global__ void mark_count_kernel(int64_t n, const IdSets ids, int refine_all, int64_t* __restrict__ block_counts) {
     int64_t v = (int64_t)blockIdx.x * kScanBlock + threadIdx.x;
     int m = 0;
-    if (v < n) m = refine_all ? 1 : voxel_marked(ids, n_sets, n, v);
+    if (v < n) m = refine_all ? 1 : voxel_marked(ids, v);
     int w = __syncthreads_count(m);
     if (threadIdx.x == 0) block_counts[blockIdx.x] = w;
 }
@@ -79,13 +87,13 @@ __global__ void scan_blocks_kernel(int64_t nb, int64_t* __restrict__ counts, int
     if (threadIdx.x == 0) *total = carry * 8;
 }
 
-__global__ void scatter_children_kernel(int64_t n, const double* __restrict__ c, const int32_t* __restrict__ ids,
-                                        int n_sets, int refine_all, const int64_t* __restrict__ block_off, double qx,
-                                        double qy, double qz, double* __restrict__ out) {
+__global__ void scatter_children_kernel(int64_t n, const double* __restrict__ c, const IdSets ids, int refine_all,
+                                        const int64_t* __restrict__ block_off, double qx, double qy, double qz,
+                                        double* __restrict__ out) {
     __shared__ int pref[kScanBlock];
     int64_t v = (int64_t)blockIdx.x * kScanBlock + threadIdx.x;
     int m = 0;
-    if (v < n) m = refine_all ? 1 : voxel_marked(ids, n_sets, n, v);
+    if (v < n) m = refine_all ? 1 : voxel_marked(ids, v);
     pref[threadIdx.x] = m;
     __syncthreads();
     for (int off = 1; off < kScanBlock; off <<= 1) {
@@ -104,6 +112,24 @@ __global__ void scatter_children_kernel(int64_t n, const double* __restrict__ c,
         out[3 * o + 1] = c[3 * v + 1] + sy * qy;
         out[3 * o + 2] = c[3 * v + 2] + sz * qz;
     }
+}
+
+// Marks, counts and scatters the children of the n voxels at `centres`
+// (spacing h): children into `children` (8 per marked voxel), 8 x the marked
+// count into *count.
+static gk_status refine_voxels(int64_t n, const double* centres, const IdSets& ids, int refine_all, const double* h,
+                               double* children, int64_t* count, void* work, cudaStream_t st) {
+    const int64_t nb = (n + kScanBlock - 1) / kScanBlock;
+    if (nb > 0x7fffffff) return GK_ERR_SIZE;
+    int64_t* bc = (int64_t*)work;
+    mark_count_kernel<<<(unsigned)nb, kScanBlock, 0, st>>>(n, ids, refine_all, bc);
+    GK_LAUNCH_CHECK();
+    scan_blocks_kernel<<<1, 1024, 0, st>>>(nb, bc, count);
+    GK_LAUNCH_CHECK();
+    scatter_children_kernel<<<(unsigned)nb, kScanBlock, 0, st>>>(n, centres, ids, refine_all, bc, h[0] / 4,
+                                                                   h[1] / 4, h[2] / 4, children);
+    GK_LAUNCH_CHECK();
+    return GK_OK;
 }
 
 }  // namespace gk
@@ -139,18 +165,96 @@ extern "C" gk_status gk_octree_refine(int64_t n, const double* centres, const in
     }
     if (centres == nullptr || children == nullptr || (corner_ids == nullptr && !refine_all)) return GK_ERR_ARG;
     if (work == nullptr || work_bytes < gk_octree_workspace_bytes(n)) return GK_ERR_SIZE;
-    int64_t nb = (n + kScanBlock - 1) / kScanBlock;
-    if (nb > 0x7fffffff) return GK_ERR_SIZE;
-    int64_t* bc = (int64_t*)work;
-    mark_count_kernel<<<(unsigned)nb, kScanBlock, 0, st>>>(n, corner_ids, n_id_sets, refine_all, bc);
-    GK_LAUNCH_CHECK();
-    scan_blocks_kernel<<<1, 1024, 0, st>>>(nb, bc, count);
-    GK_LAUNCH_CHECK();
-    scatter_children_kernel<<<(unsigned)nb, kScanBlock, 0, st>>>(n, centres, corner_ids, n_id_sets, refine_all, bc,
-                                                                   spacing[0] / 4, spacing[1] / 4, spacing[2] / 4,
-                                                                   children);
-    GK_LAUNCH_CHECK();
+    IdSets ids;
+    memset(&ids, 0, sizeof(ids));
+    ids.n = refine_all ? 0 : n_id_sets;
+    for (int s = 0; s < ids.n; ++s) ids.p[s] = corner_ids + (int64_t)s * 8 * n;
+    return refine_voxels(n, centres, ids, refine_all, spacing, children, count, work, st);
+}
+
+static size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+extern "C" gk_status gk_octree_level_plan(int32_t n_series, int64_t n, int32_t corners, int32_t refine,
+                                            gk_octree_level_layout* L) {
+    if (L == nullptr || n_series < 1 || n_series > GK_MAX_SURFACES || n < 0) return GK_ERR_ARG;
+    if (refine < 0 || refine > 2 || (refine == 1 && !corners)) return GK_ERR_ARG;
+    memset(L, 0, sizeof(*L));
+    const int64_t np = corners ? 9 * n : n;
+    L->n = n;
+    L->n_points = np;
+    L->n_series = n_series;
+    L->corners = corners ? 1 : 0;
+    L->refine = refine;
+    size_t o = 0;
+    L->points = o;   o += al256((size_t)np * 3 * sizeof(double));
+    L->fields = o;   o += al256((size_t)n_series * np * sizeof(double));
+    L->values = o;   o += al256((size_t)n_series * np * sizeof(double));
+    L->ids = o;      o += al256((size_t)n_series * np * sizeof(int32_t));
+    L->block = o;    o += al256((size_t)np * sizeof(double));
+    L->lith_ids = o; o += al256((size_t)np * sizeof(int32_t));
+    L->masks = o;    o += al256((size_t)n_series * np);
+    L->children = o;
+    if (refine) {
+        o += al256((size_t)8 * n * 3 * sizeof(double));
+        L->count = o;  o += 256;
+        L->work = o;   o += al256(gk_octree_workspace_bytes(n));
+    } else {
+        L->count = L->work = o;
+    }
+    L->total = o;
     return GK_OK;
+}
+
+extern "C" gk_status gk_octree_level(int32_t n_series, const gk_series_eval* series, const double* centres,
+                                     const double spacing[3], gk_prec prec, int32_t n_fault_sets,
+                                     const int32_t* fault_series, const gk_octree_level_layout* L, void* buf,
+                                     size_t buf_bytes, gk_info* info, gk_stream stream) {
+    if (L == nullptr || series == nullptr || spacing == nullptr || n_series != L->n_series) return GK_ERR_ARG;
+    if (n_fault_sets < 0 || n_fault_sets > GK_MAX_SURFACES || (n_fault_sets > 0 && fault_series == nullptr))
+        return GK_ERR_ARG;
+    gk_octree_level_layout chk;
+    gk_status st = gk_octree_level_plan(n_series, L->n, L->corners, L->refine, &chk);
+    if (st != GK_OK) return st;
+    if (memcmp(&chk, L, sizeof(chk)) != 0) return GK_ERR_ARG;
+    if (buf == nullptr || buf_bytes < L->total) return GK_ERR_SIZE;
+    const int64_t n = L->n, np = L->n_points;
+    cudaStream_t cs = (cudaStream_t)stream;
+    char* b = (char*)buf;
+    if (n == 0) {
+        if (L->refine) GK_CUDA_TRY(cudaMemsetAsync(b + L->count, 0, sizeof(int64_t), cs));
+        return GK_OK;
+    }
+    if (centres == nullptr) return GK_ERR_ARG;
+    double* pts = (double*)(b + L->points);
+    GK_CUDA_TRY(cudaMemcpyAsync(pts, centres, (size_t)n * 3 * sizeof(double), cudaMemcpyDeviceToDevice, cs));
+    if (L->corners) {
+        st = gk_octree_corners(n, centres, spacing, pts + 3 * n, stream);
+        if (st != GK_OK) return st;
+    }
+    gk_points gp;
+    memset(&gp, 0, sizeof(gp));
+    gp.kind = 1;
+    gp.n = np;
+    gp.xyz = pts;
+    double* fields = (double*)(b + L->fields);
+    int32_t* ids = (int32_t*)(b + L->ids);
+    int32_t* lith = (int32_t*)(b + L->lith_ids);
+    st = gk_eval_series_set(n_series, series, &gp, prec, fields, (double*)(b + L->values), ids,
+                            (double*)(b + L->block), lith, (uint8_t*)(b + L->masks), info, stream);
+    if (st != GK_OK) return st;
+    if (!L->refine) return GK_OK;
+    IdSets sets;
+    memset(&sets, 0, sizeof(sets));
+    if (L->refine == 1) {
+        sets.p[sets.n++] = lith + n;   // the corners' lithology, then each fault series' block ids
+        for (int f = 0; f < n_fault_sets; ++f) {
+            const int s = fault_series[f];
+            if (s < 0 || s >= n_series) return GK_ERR_ARG;
+            sets.p[sets.n++] = ids + (int64_t)s * np + n;
+        }
+    }
+    return refine_voxels(n, pts, sets, L->refine == 2, spacing, (double*)(b + L->children), (int64_t*)(b + L->count),
+                         b + L->work, cs);
 }
 
 extern "C" const char* gk_version(void) { return "gempy_gb300 0.1.0 (sm_103a)"; }

@@ -171,13 +171,6 @@ class _Evaluation:
     masks: torch.Tensor           # (n_series, n) squeezed masks
     fault_rows: List[int]         # series that are FAULT stacks
 
-    def refinement_ids(self, a, b):
-        """Id sets of points a..b-1 whose change across a voxel's corners
-        refines it: the lithology, then each fault series' block."""
-        if not self.fault_rows:
-            return self.lith_ids[a:b].view(1, -1)
-        return torch.stack([self.lith_ids[a:b]] + [self.ids[i, a:b] for i in self.fault_rows])
-
     def slice(self, a, b):
         return _Evaluation(self.fields[:, a:b], self.values[:, a:b], self.ids[:, a:b],
                            [None if g is None else g[a:b] for g in self.grads], self.block[a:b],
@@ -214,15 +207,19 @@ class _Evaluator:
         """Every series at ``pts`` and their combination: one library call
         (gk_eval_series_set); gradients, when asked for, in FP64 per series."""
         F, V, I, cv, ci, masks = self._set().evaluate(pts, self.prec)
-        grads = []
-        for k, s in enumerate(self.series):
-            g = None
-            if gradient:   # gradients in FP64 (the float-float kernel computes the field only)
-                fv = V[s.faults] if s.faults else None
-                _, g, _, _ = K.evaluate(s.dev, s.model, pts, GK_F64 if self.prec == GK_FF else self.prec,
-                                        gradient=True, want_field=False, fault_values=fv)
-            grads.append(g)
+        grads = self.gradients(pts, V) if gradient else [None] * len(self.series)
         return _Evaluation(F, V, I, grads, cv, ci, masks, self._frows)
+
+    def gradients(self, pts: K.Points, V):
+        """Per-series field gradients at pts (FP64: the float-float kernel
+        computes the field only); V holds the series' soft values there."""
+        grads = []
+        for s in self.series:
+            fv = V[s.faults] if s.faults else None
+            _, g, _, _ = K.evaluate(s.dev, s.model, pts, GK_F64 if self.prec == GK_FF else self.prec,
+                                    gradient=True, want_field=False, fault_values=fv)
+            grads.append(g)
+        return grads
 
 
 def _outputs(ev: _Evaluation, series):
@@ -355,23 +352,20 @@ class _HostStager:
 
 @dataclass
 class _LevelRecord:
-    """What one octree level left on the device: its point buffer
-    ([centres; 8 corners each] or the centres alone), the series-set buffer
-    of its evaluation and the per-series gradients."""
-    pts: torch.Tensor
-    n: int
+    """One octree level left on the device by gk_octree_level (its results:
+    ``level.buffer[:level.result_bytes]``) and its per-series gradients."""
+    level: K.OctreeLevel
+    result: torch.Tensor
     spacing: np.ndarray
     surface: bool
-    buffer: torch.Tensor
-    layout: tuple
     grads: list
 
 
-def _level_output(rec: _LevelRecord, ev: "_Evaluator", series, pts, buffer, grads):
-    """The OctreeLevel of a record from its arrays (device tensors, or their
-    host copies: the same layout either way)."""
-    n = rec.n
-    F, V, I, B, L, M = ev._set().views(buffer, rec.layout)
+def _level_output(rec: _LevelRecord, ev: "_Evaluator", series, buffer, grads):
+    """The OctreeLevel of a record from its result bytes (the device buffer,
+    or its host copy: the same layout either way)."""
+    n = rec.level.n
+    pts, F, V, I, B, L, M = rec.level.views(buffer)
     e = _Evaluation(F, V, I, grads, B, L, M, ev._frows)
     ec = e.slice(0, n)
     outs = _outputs(e if rec.surface else ec, series)
@@ -525,11 +519,12 @@ def _compute_model(interpolation_input, options, data_descriptor, geophysics_inp
     eo = options.evaluation_options
     want_grad = bool(eo.compute_scalar_gradient)
 
-    # ---- 4a: octree levels.  Centres and (where needed) corners are one
-    # point set: [centres; 8 corners per centre], evaluated once per series.
-    # The loop only launches work and reads the size of the next level; each
-    # level's two buffers go to the host while the next level computes, and
-    # the output objects are built once, after the loop.
+    # ---- 4a: octree levels.  One library call per level (gk_octree_level):
+    # the level's points ([centres; 8 corners per centre] where corners are
+    # needed), every series there, their combination and the children of the
+    # refined voxels, in one device buffer.  The loop reads only the size of
+    # the next level; each level's results go to the host while the next
+    # level computes, and the output objects are built once, after the loop.
     t1 = time.perf_counter()
     stager = None if cfg.keep_on_device else _HostStager()
     records = []
@@ -542,27 +537,23 @@ def _compute_model(interpolation_input, options, data_descriptor, geophysics_inp
         d = np.array(og.dxdydz, dtype=np.float64)
         ss = ev._set()
         for level in range(n_levels):
-            n = centres.shape[0]
             last = level == n_levels - 1
             surface = level < levels_surface
             refine_all = level + 1 < min_level
-            need_corners = surface or (not last and not refine_all)
-            if need_corners:
-                pts_xyz = torch.empty((9 * n, 3), dtype=torch.float64, device=device)
-                pts_xyz[:n] = centres
-                K.octree_corners(centres, d, out=pts_xyz[n:])
-            else:
-                pts_xyz = centres.contiguous()
-            pts = K.Points(xyz=pts_xyz)
-            e = ev.run(pts, gradient=want_grad)
-            buf, offs, sizes, _ = ss.last_buffer
-            records.append(_LevelRecord(pts_xyz, n, d.copy(), surface, buf, (offs, sizes, pts.n), e.grads))
+            refine = 0 if last else (2 if refine_all else 1)
+            lvl = K.OctreeLevel(ss, centres, d, prec, corners=surface or refine == 1, refine=refine,
+                                fault_series=ev._frows)
+            grads = [None] * len(series)
+            if want_grad:
+                pts, _, V, _, _, _, _ = lvl.views(lvl.buffer)
+                grads = ev.gradients(K.Points(xyz=pts), V)
+            result = lvl.buffer[:lvl.result_bytes]
+            records.append(_LevelRecord(lvl, result, d.copy(), surface, grads))
             if stager is not None:
-                stager.push(pts_xyz, buf, *e.grads)   # copied while the next level computes
+                stager.push(result, *grads)   # copied while the next level computes
             if last:
                 break
-            corner_ids = None if refine_all else e.refinement_ids(n, 9 * n)
-            centres = K.octree_refine(centres, corner_ids, d, refine_all=refine_all)
+            centres = lvl.children()
             d = d / 2.0
             if cfg.timings:
                 torch.cuda.synchronize()
@@ -590,8 +581,7 @@ def _compute_model(interpolation_input, options, data_descriptor, geophysics_inp
         torch.cuda.synchronize()
         timings["grids_s"] = time.perf_counter() - t2
 
-    octrees = [] if stager is not None else [_level_output(r, ev, series, r.pts, r.buffer, r.grads)
-                                             for r in records]
+    octrees = [] if stager is not None else [_level_output(r, ev, series, r.result, r.grads) for r in records]
     root = RootOutput([InterpOutput(ExportedFields(scalar_field=None, scalar_field_at_surface_points=s.iso),
                                     None, weights=s.weights) for s in series])
     sfsp = [float(v) for s in series for v in s.iso]
@@ -606,8 +596,8 @@ def _compute_model(interpolation_input, options, data_descriptor, geophysics_inp
         stager.stage(sol.root_output)     # the octree levels are already on their way
         stager.stage(sol.raw_arrays)
         stager.finish()
-        sol.octrees_output = [_level_output(r, ev, series, stager.host(r.pts), stager.host(r.buffer),
-                                            [stager.host(g) for g in r.grads]) for r in records]
+        sol.octrees_output = [_level_output(r, ev, series, stager.host(r.result), [stager.host(g) for g in r.grads])
+                              for r in records]
     if cfg.timings:
         timings["transfer_s"] = time.perf_counter() - t3
         timings["total_s"] = time.perf_counter() - t0

@@ -543,31 +543,11 @@ class SeriesSet:
         check("gk_eval_series_set", lib.gk_eval_series_set(self.n, self.arr, ctypes.byref(pts.gk), prec, _ptr(F),
                                                            _ptr(V), _ptr(I), _ptr(B), _ptr(L), _ptr(M),
                                                            _ptr(info), _stream()))
-        self.last_buffer = (buf, offs, sizes, n)
         return F, V, I, B, L, M
 
-    def views(self, buffer, layout):
-        """fields, values, ids, block, lith ids, masks as views of ``buffer``
-        (a torch tensor or numpy array of bytes laid out like the buffer of an
-        earlier ``evaluate``; ``layout`` = (offsets, sizes, n) of that call)."""
-        offs, sizes, n = layout
-        ns = self.n
-        torch_buf = isinstance(buffer, torch.Tensor)
 
-        def piece(i, dt, shape):
-            b = buffer[offs[i]:offs[i] + sizes[i]]
-            if torch_buf:
-                return b.view(dt).view(shape)
-            return b.view(_NP_OF[dt]).reshape(shape)
-        out = [piece(0, torch.float64, (ns, n)), piece(1, torch.float64, (ns, n)), piece(2, torch.int32, (ns, n))]
-        if len(sizes) > 3:
-            out += [piece(3, torch.float64, (n,)), piece(4, torch.int32, (n,)), piece(5, torch.uint8, (ns, n))]
-        else:
-            out += [None, None, None]
-        return tuple(out)
-
-
-_NP_OF = {torch.float64: np.float64, torch.int32: np.int32, torch.uint8: np.uint8}
+_NP_OF = {torch.float64: np.float64, torch.int32: np.int32, torch.uint8: np.uint8, torch.int64: np.int64}
+_ITEMSIZE = {torch.float64: 8, torch.int32: 4, torch.uint8: 1, torch.int64: 8}
 
 
 def combine(fields, values, ids, relations, min_iso, max_iso, want_masks=True):
@@ -623,6 +603,54 @@ def octree_refine(centres, corner_ids, spacing, refine_all=False):
                                                    _ptr(work), wb, _stream()))
     m = int(count.item())
     return children[:m]
+
+
+class OctreeLevel:
+    """One octree level computed by ``gk_octree_level``: every series at the
+    level's points ([centres; corners] or the centres), their combination and
+    -- unless it is the last level -- the children of the refined voxels, all
+    in one device buffer.  ``result_bytes`` covers the level's results (points
+    to masks); the children follow."""
+
+    def __init__(self, series_set: "SeriesSet", centres, spacing, prec, corners, refine, fault_series=(),
+                 info=None):
+        lib = _lib.load()
+        n = int(centres.shape[0])
+        L = _lib.GkOctreeLevelLayout()
+        check("gk_octree_level_plan", lib.gk_octree_level_plan(series_set.n, n, int(bool(corners)),
+                                                                   int(refine), ctypes.byref(L)))
+        self.layout, self.n, self.n_points, self.ns = L, n, int(L.n_points), series_set.n
+        self.buffer = torch.empty(int(L.total), dtype=torch.uint8, device=centres.device)
+        fs = (ctypes.c_int32 * max(1, len(fault_series)))(*[int(f) for f in fault_series])
+        sp = (ctypes.c_double * 3)(*[float(v) for v in spacing])
+        check("gk_octree_level", lib.gk_octree_level(series_set.n, series_set.arr, _ptr(centres.contiguous()), sp,
+                                                     prec, len(fault_series), fs, ctypes.byref(L),
+                                                     self.buffer.data_ptr(), int(L.total), _ptr(info), _stream()))
+        self.result_bytes = int(L.children)
+
+    def views(self, buffer):
+        """points, fields, values, ids, block, lith ids, masks as views of
+        ``buffer``: this level's device buffer, or a host copy (numpy bytes)
+        of its first ``result_bytes``."""
+        L, np_, ns = self.layout, self.n_points, self.ns
+        torch_buf = isinstance(buffer, torch.Tensor)
+
+        def piece(off, dt, shape):
+            nbytes = int(np.prod(shape)) * _ITEMSIZE[dt]
+            b = buffer[int(off):int(off) + nbytes]
+            return b.view(dt).view(shape) if torch_buf else b.view(_NP_OF[dt]).reshape(shape)
+        return (piece(L.points, torch.float64, (np_, 3)), piece(L.fields, torch.float64, (ns, np_)),
+                piece(L.values, torch.float64, (ns, np_)), piece(L.ids, torch.int32, (ns, np_)),
+                piece(L.block, torch.float64, (np_,)), piece(L.lith_ids, torch.int32, (np_,)),
+                piece(L.masks, torch.uint8, (ns, np_)))
+
+    def children(self):
+        """The next level's centres (reads the count: one synchronisation)."""
+        L = self.layout
+        if not L.refine or self.n == 0:
+            return self.buffer[:0].view(torch.float64).view(0, 3)
+        m = int(self.buffer[int(L.count):int(L.count) + 8].view(torch.int64).item())
+        return self.buffer[int(L.children):int(L.children) + 24 * m].view(torch.float64).view(m, 3)
 
 
 def set_wait_limit(spins):

@@ -359,6 +359,43 @@ gk_status gk_octree_refine(int64_t n, const double* centres,
                            double* children, int64_t* count, void* work,
                            size_t work_bytes, gk_stream stream);
 
+/* One level of the octree loop of compute_model (gempy/API/compute_API.py:
+ * 68-73 over the octree grid of gempy/core/data/grid.py:128-151) in one call:
+ * the level's points -- its voxel centres, followed by 8 corners per voxel
+ * when ``corners`` -- every series at those points and their combination
+ * (gk_eval_series_set), and, when ``refine`` (1: voxels whose corners differ
+ * in lithology or in the block of a fault series ``fault_series[0..
+ * n_fault_sets-1]``; 2: every voxel), the children of the refined voxels and
+ * 8 x their count.  Every output lands in one device buffer of ``total``
+ * bytes laid out by gk_octree_level_plan (byte offsets, 256-aligned):
+ *   points   n_points x 3 FP64      fields, values  n_series x n_points FP64
+ *   ids      n_series x n_points i32   block  n_points FP64
+ *   lith_ids n_points i32           masks  n_series x n_points u8
+ *   children 8n x 3 FP64            count  int64 (refine only), then scratch.
+ * Everything before ``children`` is the level's result; ``children[0..count)``
+ * are the next level's centres.  ``centres`` may lie in the previous level's
+ * buffer. */
+typedef struct gk_octree_level_layout {
+    int64_t n;          /* voxels of the level                        */
+    int64_t n_points;   /* n, or 9n with corners                      */
+    int32_t n_series;
+    int32_t corners;    /* 1: points are [centres; corners]           */
+    int32_t refine;     /* 0: last level, 1: marked voxels, 2: all    */
+    int32_t reserved;
+    uint64_t points, fields, values, ids, block, lith_ids, masks;
+    uint64_t children, count, work, total;
+} gk_octree_level_layout;
+gk_status gk_octree_level_plan(int32_t n_series, int64_t n, int32_t corners,
+                                 int32_t refine, gk_octree_level_layout* out);
+gk_status gk_octree_level(int32_t n_series, const gk_series_eval* series,
+                          const double* centres,
+                          const double spacing[3] /* HOST */, gk_prec prec,
+                          int32_t n_fault_sets,
+                          const int32_t* fault_series /* HOST */,
+                          const gk_octree_level_layout* layout /* HOST */,
+                          void* buf, size_t buf_bytes, gk_info* info,
+                          gk_stream stream);
+
 /* ---------------- batched realisations (many compute_model calls) ------- */
 
 /* One realisation of a batch: a single-series model, its 3-D regular grid

@@ -82,6 +82,8 @@ int main(void) {
          offsetof(gk_system, fault_sp), offsetof(gk_points, fault_values), offsetof(gk_points, fault_ld));
   printf("%zu %zu %zu %zu\\n", sizeof(gk_series_eval), offsetof(gk_series_eval, min_iso), sizeof(gk_cta_job),
          offsetof(gk_cta_job, info));
+  printf("%zu %zu %zu\\n", sizeof(gk_octree_level_layout), offsetof(gk_octree_level_layout, points),
+         offsetof(gk_octree_level_layout, total));
   return 0;
 }
 """)
@@ -93,8 +95,45 @@ int main(void) {
             _lib.GkMlp.params.offset, _lib.GkSystem.range.offset, _lib.GkSystem.fault_sp.offset,
             _lib.GkPoints.fault_values.offset, _lib.GkPoints.fault_ld.offset,
             ctypes.sizeof(_lib.GkSeriesEval), _lib.GkSeriesEval.min_iso.offset, ctypes.sizeof(_lib.GkCtaJob),
-            _lib.GkCtaJob.info.offset]
+            _lib.GkCtaJob.info.offset, ctypes.sizeof(_lib.GkOctreeLevelLayout),
+            _lib.GkOctreeLevelLayout.points.offset, _lib.GkOctreeLevelLayout.total.offset]
     assert got == want
+
+
+def test_octree_level_plan_on_the_host(lib):
+    """gk_octree_level_plan is host arithmetic: every piece 256-aligned, in
+    order, sized for its rows; the children and count only when refining."""
+    L = _lib.GkOctreeLevelLayout()
+    ns, n = 3, 1000
+    assert lib.gk_octree_level_plan(ns, n, 1, 1, ctypes.byref(L)) == _lib.GK_OK
+    np_ = 9 * n
+    assert (L.n, L.n_points, L.n_series, L.corners, L.refine) == (n, np_, ns, 1, 1)
+    order = ["points", "fields", "values", "ids", "block", "lith_ids", "masks", "children", "count", "work", "total"]
+    offs = [getattr(L, k) for k in order]
+    assert offs == sorted(offs) and all(o % 256 == 0 for o in offs) and L.points == 0
+    need = {"points": 24 * np_, "fields": 8 * ns * np_, "values": 8 * ns * np_, "ids": 4 * ns * np_,
+            "block": 8 * np_, "lith_ids": 4 * np_, "masks": ns * np_, "children": 8 * n * 24, "count": 8,
+            "work": lib.gk_octree_workspace_bytes(n)}
+    for a, b in zip(order[:-1], order[1:]):
+        assert getattr(L, b) - getattr(L, a) >= need[a], a
+    # the last level: no children; without corners the points are the centres
+    assert lib.gk_octree_level_plan(ns, n, 0, 0, ctypes.byref(L)) == _lib.GK_OK
+    assert L.n_points == n and L.children == L.count == L.work == L.total
+    # marking needs the corners; bad sizes and modes are rejected
+    assert lib.gk_octree_level_plan(ns, n, 0, 1, ctypes.byref(L)) == _lib.GK_ERR_ARG
+    assert lib.gk_octree_level_plan(0, n, 1, 1, ctypes.byref(L)) == _lib.GK_ERR_ARG
+    assert lib.gk_octree_level_plan(ns, -1, 1, 1, ctypes.byref(L)) == _lib.GK_ERR_ARG
+    assert lib.gk_octree_level_plan(ns, n, 1, 3, ctypes.byref(L)) == _lib.GK_ERR_ARG
+    # a layout that the plan did not make, or a short buffer, is refused before any launch
+    assert lib.gk_octree_level_plan(ns, n, 1, 1, ctypes.byref(L)) == _lib.GK_OK
+    items = (_lib.GkSeriesEval * ns)()
+    sp3 = (ctypes.c_double * 3)(1.0, 1.0, 1.0)
+    buf = ctypes.c_void_p(256)
+    assert lib.gk_octree_level(ns, items, buf, sp3, 0, 0, None, ctypes.byref(L), buf, L.total - 1, None,
+                               None) == _lib.GK_ERR_SIZE
+    L.masks += 256
+    assert lib.gk_octree_level(ns, items, buf, sp3, 0, 0, None, ctypes.byref(L), buf, L.total, None,
+                               None) == _lib.GK_ERR_ARG
 
 
 def test_invalid_arguments_rejected_before_any_launch(lib):

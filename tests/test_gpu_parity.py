@@ -136,6 +136,36 @@ def test_mixed_solve_reaches_fp64_residual(case):
     assert np.abs(w - w_ref).max() <= 1e-6 * np.abs(w_ref).max()
 
 
+@pytest.mark.parametrize("per,n_o", [(4, 2), (30, 12), (52, 22), (52, 23), (150, 60)])
+def test_cta_mixed_solve_matches_lapack(per, n_o):
+    """The one-block mixed solve on both preconditioner forms: systems up to
+    224 unknowns invert their equilibrated FP32 matrix in shared memory,
+    larger ones factor it in global memory.  Here N = 3 (per + n_o): 18, 126,
+    222 (shared), 225, 630 (global).  Single and many-system entries agree
+    with LAPACK to the FGMRES tolerance."""
+    from gempy_gb300 import kernels as K
+    s = _random_series(per + n_o, n_surf=3, per=per, n_o=n_o)
+    Kr, br = kriging.build_system(s)
+    N = len(br)
+    w_ref = kriging.solve(Kr, br)
+    ds = _dev_series(s)
+    x, info = K.solve_mixed_cta(ds, tol=1e-12)
+    inf = K.read_info(info)
+    assert inf["status"] == 0 and inf["residual"] <= 1e-12, (N, inf)
+    x = x.cpu().numpy()
+    assert np.linalg.norm(br - Kr @ x) <= 1e-11 * np.linalg.norm(br)
+    assert np.abs(x - w_ref).max() <= 1e-6 * np.abs(w_ref).max()
+    # one launch over systems of different sizes: the largest decides the form
+    small = _random_series(7, n_surf=2, per=5, n_o=3)
+    Ks, bs = K.build(_dev_series(small), K.GK_F64)
+    Kb, bb = K.build(ds, K.GK_F64)
+    (xs, i_s), (xb, i_b) = K.solve_mixed_cta_many([(Ks, bs), (Kb, bb)], tol=1e-12)
+    assert K.read_info(i_s)["status"] == 0 and K.read_info(i_b)["status"] == 0
+    np.testing.assert_allclose(xb.cpu().numpy(), x, rtol=0, atol=1e-9 * np.abs(x).max())
+    Kr2, br2 = kriging.build_system(small)
+    assert np.linalg.norm(br2 - Kr2 @ xs.cpu().numpy()) <= 1e-11 * np.linalg.norm(br2)
+
+
 def _eval_gpu(s, w, x, prec, gradient=False, seg=None):
     from gempy_gb300 import kernels as K
     ds = _dev_series(s)
