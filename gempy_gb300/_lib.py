@@ -172,6 +172,12 @@ SIGNATURES = [
     ("gk_octree_level", ctypes.c_int, [ctypes.c_int32, ctypes.POINTER(GkSeriesEval), ctypes.c_void_p, c_double_p,
                                        ctypes.c_int, ctypes.c_int32, c_int32_p, ctypes.POINTER(GkOctreeLevelLayout),
                                        ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]),
+    ("gk_adjoint_rhs", ctypes.c_int, [ctypes.POINTER(GkSystem), ctypes.POINTER(GkPoints), ctypes.c_void_p,
+                                      ctypes.c_void_p, ctypes.c_void_p]),
+    ("gk_build_adjoint", ctypes.c_int, [ctypes.POINTER(GkSystem), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    ("gk_eval_adjoint", ctypes.c_int, [ctypes.POINTER(GkSystem), ctypes.c_void_p, ctypes.POINTER(GkPoints),
+                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     ("gk_batch_workspace_bytes", ctypes.c_size_t, [ctypes.POINTER(GkBatch)]),
     ("gk_batch_points", ctypes.c_int64, [ctypes.POINTER(GkBatch)]),
     ("gk_batch_plan", ctypes.c_int, [ctypes.POINTER(GkBatch), ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),

@@ -82,13 +82,7 @@ extern "C" gk_status gk_build(const gk_system* s, gk_prec prec, void* K, int64_t
     const int64_t N = gk_system_size(s);
     if (K == nullptr || ldk < N) return GK_ERR_ARG;
     if (N > (int64_t)1 << 20) return GK_ERR_SIZE;
-    BuildParams P;
-    P.n_ori = s->n_ori; P.n_iface = s->n_iface; P.degree = s->uni_degree;
-    P.n_drift = drift_count(s->uni_degree); P.kernel = s->kernel; P.N = N;
-    P.range = s->range; P.c_o = s->c_o; P.i_res = s->i_res; P.gi_res = s->gi_res;
-    P.dip_positions = s->dip_positions; P.dip_gradients = s->dip_gradients; P.nugget_grad = s->nugget_grad;
-    P.sp_coords = s->sp_coords; P.nugget_sp = s->nugget_sp; P.ref_index = s->ref_index; P.rest_index = s->rest_index;
-    P.n_fault = s->n_fault; P.fault_sp = s->fault_sp; P.n_sp = s->n_sp;
+    const BuildParams P = build_params(s);
     dim3 block(32, 8), grid((unsigned)((N + 31) / 32), (unsigned)((N + 31) / 32));
     cudaStream_t st_ = (cudaStream_t)stream;
     if (prec == GK_F64)

@@ -672,6 +672,14 @@ using namespace gk;
 
 gk_status gk_check_system(const gk_system* s);
 
+// The FP64 records of a packed model (for the adjoint): orientations
+// (x, c_o gi_res w, 0, 0) x n_ori, surface points (x, c_o gi_res alpha) x n_sp.
+void gk_eval_model_records(const gk_system* s, const void* model, const double** ori64, const double** sp64) {
+    const ModelLayout L = model_layout(s->n_ori, s->n_sp);
+    *ori64 = (const double*)((const char*)model + L.ori64);
+    *sp64 = (const double*)((const char*)model + L.sp64);
+}
+
 extern "C" size_t gk_eval_model_bytes(const gk_system* s) {
     if (s == nullptr) return 0;
     return model_layout(s->n_ori, s->n_sp).total;

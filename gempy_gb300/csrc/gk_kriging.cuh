@@ -43,6 +43,19 @@ struct BuildParams {
     int n_sp;
 };
 
+// Build parameters of one series' system (N = 3 n_ori + n_iface + n_drift + n_fault).
+inline BuildParams build_params(const gk_system* s) {
+    BuildParams P;
+    P.n_ori = s->n_ori; P.n_iface = s->n_iface; P.degree = s->uni_degree;
+    P.n_drift = drift_count(s->uni_degree); P.kernel = s->kernel;
+    P.N = 3 * (int64_t)s->n_ori + s->n_iface + P.n_drift + s->n_fault;
+    P.range = s->range; P.c_o = s->c_o; P.i_res = s->i_res; P.gi_res = s->gi_res;
+    P.dip_positions = s->dip_positions; P.dip_gradients = s->dip_gradients; P.nugget_grad = s->nugget_grad;
+    P.sp_coords = s->sp_coords; P.nugget_sp = s->nugget_sp; P.ref_index = s->ref_index; P.rest_index = s->rest_index;
+    P.n_fault = s->n_fault; P.fault_sp = s->fault_sp; P.n_sp = s->n_sp;
+    return P;
+}
+
 __device__ inline void decode(const BuildParams& P, int64_t i, Item& it) {
     const int ng = 3 * P.n_ori;
     it.nug = 0.0;
@@ -111,13 +124,12 @@ __device__ inline T dist(const T* a, const T* b, T* h) {
     return gsqrt<T>(h[0] * h[0] + h[1] * h[1] + h[2] * h[2] + (T)kDistEps2);
 }
 
+// K(A, B) with the items' positions given in T (the adjoint evaluates it on
+// dual numbers seeded on A's positions).
 template <typename T>
-__device__ T entry(const BuildParams& P, const Cov<T>& cv, const Item& A, const Item& B, bool diag) {
+__device__ T entry_at(const BuildParams& P, const Cov<T>& cv, const Item& A, const Item& B, bool diag,
+                      const T* ap, const T* aq, const T* bp, const T* bq) {
     const T c_o = (T)P.c_o;
-    T ap[3] = {(T)A.p[0], (T)A.p[1], (T)A.p[2]};
-    T aq[3] = {(T)A.q[0], (T)A.q[1], (T)A.q[2]};
-    T bp[3] = {(T)B.p[0], (T)B.p[1], (T)B.p[2]};
-    T bq[3] = {(T)B.q[0], (T)B.q[1], (T)B.q[2]};
     T h[3], g[3];
     if (A.type == 0 && B.type == 0) {
         T r = dist(ap, bp, h);
@@ -157,6 +169,15 @@ __device__ T entry(const BuildParams& P, const Cov<T>& cv, const Item& A, const 
         return (T)(P.gi_res * (F[B.rest] - F[B.ref]));
     }
     return (T)0;
+}
+
+template <typename T>
+__device__ T entry(const BuildParams& P, const Cov<T>& cv, const Item& A, const Item& B, bool diag) {
+    T ap[3] = {(T)A.p[0], (T)A.p[1], (T)A.p[2]};
+    T aq[3] = {(T)A.q[0], (T)A.q[1], (T)A.q[2]};
+    T bp[3] = {(T)B.p[0], (T)B.p[1], (T)B.p[2]};
+    T bq[3] = {(T)B.q[0], (T)B.q[1], (T)B.q[2]};
+    return entry_at<T>(P, cv, A, B, diag, ap, aq, bp, bq);
 }
 
 }  // namespace gk

@@ -395,3 +395,4 @@ class Solutions:
     gravity: Optional[np.ndarray] = None
     timings: dict = field(default_factory=dict)
     solver_info: list = field(default_factory=list)
+    taped_interpolation_input: Optional[object] = None   # leaf tensors of a compute_grads run

@@ -21,6 +21,7 @@ Flow per call, all arithmetic on the GPU through ``libgempy_gb300.so``:
      levels refine voxels whose corners differ in lithology or fault id.
 There is no CPU path: without the CUDA library this raises.
 """
+import dataclasses
 import os
 import time
 from dataclasses import dataclass
@@ -49,7 +50,13 @@ class EngineConfig:
     solved by FGMRES to ``learned_tol`` with the two-level preconditioner the
     trained network picks (``learned.py``; FP64 LU fallback) when a trained
     model is available (``learned_model``, default: the packaged one);
-    ``learned_min_n`` = 0 disables this."""
+    ``learned_min_n`` = 0 disables this.
+
+    ``compute_grads`` (FP64 form only) returns the octree levels' scalar
+    fields as torch tensors that back-propagate, through the adjoint kernels
+    (``adjoint.py``), into ``Solutions.taped_interpolation_input``: the
+    interpolation input with its surface points, nuggets and orientations as
+    leaf tensors (transformed frame), as the reference's PyTorch tape does."""
     dtype: str = "float64"
     use_gpu: bool = True
     keep_on_device: bool = False
@@ -60,6 +67,7 @@ class EngineConfig:
     learned_min_n: int = 16384
     learned_tol: float = 1e-8
     learned_model: Optional[str] = None
+    compute_grads: bool = False
 
 
 class _Series:
@@ -495,8 +503,60 @@ def compute_model(interpolation_input, options, data_descriptor, geophysics_inpu
         return _compute_model(interpolation_input, options, data_descriptor, geophysics_input, config)
 
 
+def _attach_grads(sol, records, series, interpolation_input, options, data_descriptor, device):
+    """Makes every octree level's scalar fields differentiable: one
+    ``adjoint.series_field`` per series over all levels' points, split back
+    into the levels, on leaf tensors of the inputs."""
+    import copy
+
+    from . import adjoint
+    ii = interpolation_input
+    leaf = lambda a: torch.as_tensor(np.asarray(a, dtype=np.float64)).to(device).requires_grad_(True)
+    sp = leaf(np.asarray(ii.surface_points.sp_coords).reshape(-1, 3))
+    nsp = leaf(ii.surface_points.nugget_effect_scalar)
+    dpos = leaf(np.asarray(ii.orientations.dip_positions).reshape(-1, 3))
+    dgr = leaf(np.asarray(ii.orientations.dip_gradients).reshape(-1, 3))
+    ngr = leaf(ii.orientations.nugget_effect_grad)
+    taped = copy.copy(ii)
+    taped.surface_points = copy.copy(ii.surface_points)
+    taped.orientations = copy.copy(ii.orientations)
+    taped.surface_points.sp_coords, taped.surface_points.nugget_effect_scalar = sp, nsp
+    taped.orientations.dip_positions, taped.orientations.dip_gradients = dpos, dgr
+    taped.orientations.nugget_effect_grad = ngr
+    sol.taped_interpolation_input = taped
+    if not records:
+        return
+    ko = options.kernel_options
+    ss = data_descriptor.stack_structure
+    views = [r.level.views(r.result) for r in records]
+    xyz = torch.cat([v[0] for v in views])
+    sizes = [int(v[0].shape[0]) for v in views]
+    p_off = o_off = 0
+    for si, s in enumerate(series):
+        n_p = int(ss.number_of_points_per_stack[si])
+        n_o = int(ss.number_of_orientations_per_stack[si])
+        fv = torch.cat([v[2][s.faults] for v in views], dim=1).detach() if s.faults else None
+        spec = adjoint.SeriesSpec(s.dev.points_per_surface, ko.range, ko.c_o, ko.uni_degree, ko.kernel_function,
+                                  ko.i_res, ko.gi_res, s.dev.fault_sp, fv)
+        z = adjoint.series_field(sp[p_off:p_off + n_p], nsp[p_off:p_off + n_p], dpos[o_off:o_off + n_o],
+                                 dgr[o_off:o_off + n_o], ngr[o_off:o_off + n_o], xyz, spec)
+        for lv, r, zl in zip(sol.octrees_output, records, torch.split(z, sizes)):
+            n = r.level.n
+            lv.outputs[si].exported_fields.scalar_field = zl if r.surface else zl[:n]
+            if si == len(series) - 1:
+                lv.last_output_center.exported_fields.scalar_field = zl[:n]
+                if lv.last_output_corners is not None:
+                    lv.last_output_corners.exported_fields.scalar_field = zl[n:]
+        p_off += n_p
+        o_off += n_o
+
+
 def _compute_model(interpolation_input, options, data_descriptor, geophysics_input, config) -> Solutions:
     cfg = config or EngineConfig()
+    if cfg.compute_grads:
+        if str(cfg.dtype) != "float64":
+            raise ValueError("compute_grads needs the FP64 form (dtype='float64'): the adjoint reuses its LU factors")
+        cfg = dataclasses.replace(cfg, keep_on_device=True)
     device = torch.device("cuda")
     mixed = str(cfg.dtype) in ("float32", "mixed")
     ko = options.kernel_options
@@ -598,6 +658,8 @@ def _compute_model(interpolation_input, options, data_descriptor, geophysics_inp
         stager.finish()
         sol.octrees_output = [_level_output(r, ev, series, stager.host(r.result), [stager.host(g) for g in r.grads])
                               for r in records]
+    if cfg.compute_grads:
+        _attach_grads(sol, records, series, interpolation_input, options, data_descriptor, device)
     if cfg.timings:
         timings["transfer_s"] = time.perf_counter() - t3
         timings["total_s"] = time.perf_counter() - t0

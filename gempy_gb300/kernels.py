@@ -605,6 +605,54 @@ def octree_refine(centres, corner_ids, spacing, refine_all=False):
     return children[:m]
 
 
+def _adjoint_points(series: DeviceSeries, pts: Points, fault_values=None):
+    gp = GkPoints()
+    ctypes.pointer(gp)[0] = pts.gk
+    keep = None
+    if series.n_faults:
+        if fault_values is None:
+            raise ValueError("a series with fault drift needs its faults' blocks at the points")
+        keep = fault_values.to(dtype=torch.float64).contiguous()
+        gp.fault_values = keep.data_ptr()
+        gp.fault_ld = int(keep.shape[1])
+    return gp, keep
+
+
+def adjoint_rhs(series: DeviceSeries, pts: Points, g, fault_values=None):
+    """r = sum_x g(x) dZ(x)/dw (N)."""
+    lib = _lib.load()
+    gp, keep = _adjoint_points(series, pts, fault_values)
+    g = g.to(dtype=torch.float64).contiguous()
+    r = torch.empty(series.N, dtype=torch.float64, device=series.device)
+    check("gk_adjoint_rhs", lib.gk_adjoint_rhs(ctypes.byref(series.sys), ctypes.byref(gp), _ptr(g), _ptr(r),
+                                               _stream()))
+    return r
+
+
+def build_adjoint(series: DeviceSeries, lam, w):
+    """-lambda^T (dK/dtheta) w: (d surface points (n_sp, 3), d orientation
+    positions (n_ori, 3), d surface-point nuggets (n_sp), d orientation
+    nuggets (n_ori))."""
+    lib = _lib.load()
+    dev, s = series.device, series.sys
+    d_sp = torch.empty((s.n_sp, 3), dtype=torch.float64, device=dev)
+    d_dip = torch.empty((s.n_ori, 3), dtype=torch.float64, device=dev)
+    d_nsp = torch.empty(s.n_sp, dtype=torch.float64, device=dev)
+    d_ngr = torch.empty(s.n_ori, dtype=torch.float64, device=dev)
+    check("gk_build_adjoint", lib.gk_build_adjoint(ctypes.byref(s), _ptr(lam.contiguous()), _ptr(w.contiguous()),
+                                                   _ptr(d_sp), _ptr(d_dip), _ptr(d_nsp), _ptr(d_ngr), _stream()))
+    return d_sp, d_dip, d_nsp, d_ngr
+
+
+def eval_adjoint(series: DeviceSeries, model, pts: Points, g, d_sp, d_dip, fault_values=None):
+    """Adds sum_x g(x) dZ(x)/d(record positions) at fixed weights into d_sp, d_dip."""
+    lib = _lib.load()
+    gp, keep = _adjoint_points(series, pts, fault_values)
+    g = g.to(dtype=torch.float64).contiguous()
+    check("gk_eval_adjoint", lib.gk_eval_adjoint(ctypes.byref(series.sys), _ptr(model), ctypes.byref(gp), _ptr(g),
+                                                 _ptr(d_sp), _ptr(d_dip), _stream()))
+
+
 class OctreeLevel:
     """One octree level computed by ``gk_octree_level``: every series at the
     level's points ([centres; corners] or the centres), their combination and

@@ -396,6 +396,37 @@ gk_status gk_octree_level(int32_t n_series, const gk_series_eval* series,
                           void* buf, size_t buf_bytes, gk_info* info,
                           gk_stream stream);
 
+/* ---------------- adjoint derivatives (engine autodiff) ------------------ */
+
+/* Reverse-mode derivatives of J = sum_x g(x) Z(x) for one series, the
+ * gradients the reference takes through compute_model with a PyTorch tape
+ * (``compute_grads``, checked against central differences at
+ * test/test_modules/test_ad/test_ad_I.py:158-258; used by the nugget
+ * optimiser, gempy/modules/optimize_nuggets/_optimizer.py:9-62).  With
+ * Z(x) = sum_i w_i e_i(x) and K w = b:
+ *   gk_adjoint_rhs    r = sum_x g(x) e(x)                         (N)
+ *   solve K lambda = r (K is symmetric: the forward LU factors serve)
+ *   gk_build_adjoint  -lambda^T (dK/dtheta) w for theta = surface-point
+ *                     coordinates (n_sp x 3), orientation positions
+ *                     (n_ori x 3) and, when not NULL, the nuggets of the
+ *                     surface points (n_sp) and orientations (n_ori); the
+ *                     outputs are overwritten
+ *   gk_eval_adjoint   adds sum_x g(x) dZ(x)/dtheta at fixed weights (the
+ *                     surface points' and orientations' positions) into the
+ *                     same position outputs; ``model`` from gk_eval_prepare
+ *   dJ/d(dip gradient of orientation o, component u) = lambda[u n_ori + o].
+ * The fault-drift functions (other series' blocks) are held constant; ``g``
+ * has pts->n entries. */
+gk_status gk_adjoint_rhs(const gk_system* sys, const gk_points* pts,
+                         const double* g, double* r, gk_stream stream);
+gk_status gk_build_adjoint(const gk_system* sys, const double* lambda,
+                           const double* w, double* d_sp, double* d_dip,
+                           double* d_nugget_sp, double* d_nugget_grad,
+                           gk_stream stream);
+gk_status gk_eval_adjoint(const gk_system* sys, const void* model,
+                          const gk_points* pts, const double* g, double* d_sp,
+                          double* d_dip, gk_stream stream);
+
 /* ---------------- batched realisations (many compute_model calls) ------- */
 
 /* One realisation of a batch: a single-series model, its 3-D regular grid
