@@ -35,6 +35,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "grid points/s + kriging solves/s: mixed/learned vs FP64 GPU at 1e-6 field error"
+# thread instructions per point-record pair of the float-float field kernel,
+# from ncu's executed-instruction count (profiles/eval_ff_precision_64.md)
+FF_OPS_PER_PAIR = 116
 WORKLOAD = ("precision: 1 series, 4000 surface points on 8 folded surfaces, 1500 orientations "
             "(N=8495), cubic, linear drift, 256^3 regular grid")
 
@@ -452,11 +455,12 @@ def main():
                                     f"(max SM clock from MEASURED_PEAKS.json, {pk['_source']})",
                      "work": f"{fl_pt} algorithmic flops/point x {n_pts} points per launch",
                      "eval_ms": ev_mixed,
-                     # float-float executes ~168 FP32-pipe instructions per point-record pair (ncu count)
+                     # float-float executes ~116 thread instructions per point-record pair (ncu count of the
+                     # shipped kernel at 64^3, profiles/eval_ff_precision_64.md)
                      # where the algorithmic count has 20: the pipe view
-                     "fp32_pipe_ops_per_pair": 168, "algorithmic_flops_per_pair": 20,
-                     "fp32_pipe_achieved": achieved_tf * 168 / 20,
-                     "fp32_pipe_frac": achieved_tf * 168 / 20 / fp32_peak},
+                     "fp32_pipe_ops_per_pair": FF_OPS_PER_PAIR, "algorithmic_flops_per_pair": 20,
+                     "fp32_pipe_achieved": achieved_tf * FF_OPS_PER_PAIR / 20,
+                     "fp32_pipe_frac": achieved_tf * FF_OPS_PER_PAIR / 20 / fp32_peak},
     }
     if not args.no_extra and rank == 0:
         line["plain"] = plain_section()
@@ -598,7 +602,8 @@ def plain_section():
 
 def octree_section():
     """Config 2: three folded series, quadratic drift, 7 octree levels, through
-    compute_model (host inputs), plain FP64 and mixed."""
+    compute_model (host inputs), plain FP64 and mixed: 3 warm-up calls, then
+    the median of 10 calls each timed alone."""
     import torch
     import gempy_gb300 as gg
     from gempy_gb300 import synthetic
@@ -607,16 +612,19 @@ def octree_section():
                        "7 octree levels (128^3 effective)"}
     for name, dt in (("plain_fp64", "float64"), ("mixed", "float32")):
         cfg = gg.EngineConfig(dtype=dt)
-        gg.compute_model(m.interpolation_input, m.options, m.data_descriptor, config=cfg)
+        for _ in range(3):
+            gg.compute_model(m.interpolation_input, m.options, m.data_descriptor, config=cfg)
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        reps = 3
-        for _ in range(reps):
+        times = []
+        for _ in range(10):   # each call timed alone (host inputs, results on the host)
+            t0 = time.perf_counter()
             sol = gg.compute_model(m.interpolation_input, m.options, m.data_descriptor, config=cfg)
-        torch.cuda.synchronize()
-        dt_s = (time.perf_counter() - t0) / reps
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
+        dt_s = float(np.median(times))
         npts = sum(len(l.grid_centers) for l in sol.octrees_output)
-        out[name] = {"ms": 1e3 * dt_s, "octree_points": npts, "points_per_s": npts / dt_s,
+        out[name] = {"ms": 1e3 * dt_s, "mean_ms": 1e3 * float(np.mean(times)), "calls": len(times),
+                     "octree_points": npts, "points_per_s": npts / dt_s,
                      "levels": [len(l.grid_centers) for l in sol.octrees_output]}
         out.setdefault("_ids", {})[name] = sol.octrees_output[-1].last_output_center.ids_block
     a, b = out.pop("_ids").values()
