@@ -116,6 +116,12 @@ class GkAdam(ctypes.Structure):
 
 # (name, restype, argtypes) of every exported symbol; tests check the header
 # declares exactly these.
+class GkMcVolume(ctypes.Structure):
+    _fields_ = [("field", ctypes.c_void_p), ("mask", ctypes.c_void_p), ("dims", ctypes.c_int32 * 3),
+                ("reserved", ctypes.c_int32), ("level", ctypes.c_double), ("spacing", ctypes.c_double * 3),
+                ("origin", ctypes.c_double * 3)]
+
+
 SIGNATURES = [
     ("gk_system_size", ctypes.c_int64, [ctypes.POINTER(GkSystem)]),
     ("gk_build", ctypes.c_int, [ctypes.POINTER(GkSystem), ctypes.c_int, ctypes.c_void_p, ctypes.c_int64,
@@ -178,6 +184,11 @@ SIGNATURES = [
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     ("gk_eval_adjoint", ctypes.c_int, [ctypes.POINTER(GkSystem), ctypes.c_void_p, ctypes.POINTER(GkPoints),
                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    ("gk_mc_workspace_bytes", ctypes.c_size_t, [c_int32_p]),
+    ("gk_mc_count", ctypes.c_int, [ctypes.POINTER(GkMcVolume), ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
+                                   ctypes.c_void_p]),
+    ("gk_mc_emit", ctypes.c_int, [ctypes.POINTER(GkMcVolume), ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
+                                  ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),
     ("gk_batch_workspace_bytes", ctypes.c_size_t, [ctypes.POINTER(GkBatch)]),
     ("gk_batch_points", ctypes.c_int64, [ctypes.POINTER(GkBatch)]),
     ("gk_batch_plan", ctypes.c_int, [ctypes.POINTER(GkBatch), ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),

@@ -706,3 +706,34 @@ def set_wait_limit(spins):
     makes them give up at once, None or a negative value restores the
     defaults.  For tests of the failure paths."""
     check("gk_set_wait_limit", _lib.load().gk_set_wait_limit(-1 if spins is None else int(spins)))
+
+
+def marching_cubes(field, dims, level, spacing, origin, mask=None):
+    """Vertices (n_v x 3, FP64) and triangles (n_t x 3, int32) of the level
+    surface of a dense-grid field on the device (``gk_mc_count`` then
+    ``gk_mc_emit``; one host read of the two counts in between)."""
+    lib = _lib.load()
+    field = field.to(dtype=torch.float64).contiguous()
+    dev = field.device
+    m = None if mask is None else mask.to(device=dev, dtype=torch.uint8).contiguous()
+    d3 = (ctypes.c_int32 * 3)(*[int(v) for v in dims])
+    n = int(dims[0]) * int(dims[1]) * int(dims[2])
+    if field.numel() != n or (m is not None and m.numel() != n):
+        raise ValueError(f"field/mask of {field.numel()} points for dims {tuple(dims)}")
+    vol = _lib.GkMcVolume()
+    vol.field = field.data_ptr()
+    vol.mask = 0 if m is None else m.data_ptr()
+    vol.dims = d3
+    vol.level = float(level)
+    vol.spacing = (ctypes.c_double * 3)(*[float(v) for v in spacing])
+    vol.origin = (ctypes.c_double * 3)(*[float(v) for v in origin])
+    wb = lib.gk_mc_workspace_bytes(d3)
+    work = torch.empty(max(wb, 8), dtype=torch.uint8, device=dev)
+    counts = torch.empty(2, dtype=torch.int64, device=dev)
+    st = _stream()
+    check("gk_mc_count", lib.gk_mc_count(ctypes.byref(vol), _ptr(work), wb, _ptr(counts), st))
+    nv, nt = (int(v) for v in counts.tolist())
+    verts = torch.empty((nv, 3), dtype=torch.float64, device=dev)
+    faces = torch.empty((nt, 3), dtype=torch.int32, device=dev)
+    check("gk_mc_emit", lib.gk_mc_emit(ctypes.byref(vol), _ptr(work), wb, _ptr(verts), nv, _ptr(faces), nt, st))
+    return verts, faces

@@ -271,7 +271,9 @@ gk_status gk_solve_twolevel(int64_t n, const double* K, int64_t ldk,
  * returns GK_ERR_SIZE before any work is queued.  The caller still passes K,
  * b and x.  The first call made on a device looks up the array's device
  * address (cudaGetSymbolAddress); make that first call before any stream
- * capture.  All calls share the one array: calls that overlap on the GPU
+ * capture.  The address is kept for the life of the process: after a
+ * cudaDeviceReset the library must be reloaded before this entry point is
+ * called again.  All calls share the one array: calls that overlap on the GPU
  * race, so serialize them (one stream, or explicit ordering).  Nothing here
  * calls cudaMalloc, cudaFree or an allocating library routine.  Arguments,
  * results and ``info`` are as for gk_solve_mixed (``info`` may be NULL). */
@@ -426,6 +428,44 @@ gk_status gk_build_adjoint(const gk_system* sys, const double* lambda,
 gk_status gk_eval_adjoint(const gk_system* sys, const void* model,
                           const gk_points* pts, const double* g, double* d_sp,
                           double* d_dip, gk_stream stream);
+
+/* ---------------- mesh extraction (marching cubes) ----------------------- */
+
+/* One level surface of a dense-grid field, the mesh the reference makes per
+ * structural element with skimage.measure.marching_cubes(volume, level,
+ * spacing, mask, method="lewiner") and the extent minimum added
+ * (gempy/modules/mesh_extranction/marching_cubes.py:12-56, 86-98).  A cube
+ * is processed when ``mask`` is set at its far corner (lower corner + 1 on
+ * every axis); a grid edge that the level crosses and that a processed cube
+ * holds carries one vertex (ids in edge order 3 * point + axis, position
+ * (i + t) * spacing + origin); the vertex counts of the reference's
+ * combination model test follow this rule (test/test_modules/
+ * test_marching_cubes.py:44-47).  Triangles come cube by cube: each cube's
+ * F <= level boundary cycles on its faces (four-crossing faces split by the
+ * bilinear saddle value), fanned from their first edge, oriented with
+ * F <= level on the left of each cube-face segment seen from outside. */
+typedef struct gk_mc_volume {
+    const double* field;   /* dims[0] x dims[1] x dims[2], ij order (z fastest) */
+    const uint8_t* mask;   /* same layout, nonzero = inside; NULL = all points  */
+    int32_t dims[3];
+    int32_t reserved;
+    double level;
+    double spacing[3];
+    double origin[3];      /* position of grid point (0,0,0)                  */
+} gk_mc_volume;
+/* Workspace of gk_mc_count / gk_mc_emit (0 for invalid dims).  3 * points
+ * must stay below 2^31 (vertex ids are int32). */
+size_t gk_mc_workspace_bytes(const int32_t dims[3]);
+/* Counts the vertices and triangles: counts[0], counts[1] (device int64),
+ * and keeps per-block offsets in ``work`` for gk_mc_emit. */
+gk_status gk_mc_count(const gk_mc_volume* vol, void* work, size_t work_bytes,
+                      int64_t* counts, gk_stream stream);
+/* Writes vertices (n_v x 3 FP64) and triangles (n_t x 3 int32) after a
+ * gk_mc_count of the same volume on the same workspace; writes beyond
+ * max_vertices / max_faces are dropped. */
+gk_status gk_mc_emit(const gk_mc_volume* vol, void* work, size_t work_bytes,
+                     double* vertices, int64_t max_vertices, int32_t* faces,
+                     int64_t max_faces, gk_stream stream);
 
 /* ---------------- batched realisations (many compute_model calls) ------- */
 

@@ -235,3 +235,53 @@ def test_combination_model_export_layout_and_field():
     on_node = [np.abs(zn - v).min() <= t for v, t in zip(approved, tol)]
     assert all(on_centre[:6])
     assert all(on_node[6:])
+
+
+def test_marching_cubes_vertex_counts_of_combination_model():
+    """G4: the reference's marching-cubes vertex counts of the combination
+    model on a 40 x 20 x 20 dense grid (test/test_modules/
+    test_marching_cubes.py:13-47): 600 (fault), 860 (eroding series), 1256
+    and 1680 (basement series), from the oracle's field, masks and isovalues
+    with the mesh rule of oracle/mesh.py (cube processed when the mask is set
+    at its far corner, one vertex per crossed edge of a processed cube)."""
+    from oracle import inputs, mesh
+    g = load_golden("combination_model.json")
+    series, rels, fr = inputs.series_from_golden(g)
+    ext = inputs.golden_extent(g)
+    res = np.array([40, 20, 20])
+    d = (ext[1::2] - ext[0::2]) / res
+    axes = [ext[2 * a] + (np.arange(res[a]) + 0.5) * d[a] for a in range(3)]
+    X = np.stack(np.meshgrid(*axes, indexing="ij"), -1).reshape(-1, 3)
+    r = pipeline.Model(series, rels, g["unit_values"], g["sigmoid_slope"], fr).evaluate(X)
+    counts = []
+    for s in range(len(series)):
+        mask = None if rels[s] == segmentation.FAULT else r.masks[s]
+        for level in r.isovalues[s]:
+            v, t = mesh.marching_cubes(r.fields[s], res, level, d, ext[0::2], mask)
+            counts.append(len(v))
+            assert t.min() >= 0 and t.max() < len(v)
+    assert counts == [600, 860, 1256, 1680]
+
+
+def test_marching_cubes_cycles_close_for_every_cube_configuration():
+    """Every one of the 256 corner-sign configurations (random magnitudes, so
+    both pairings of four-crossing faces occur) links its crossing edges into
+    closed cycles, and a closed level surface is a consistently oriented
+    sphere (Euler characteristic 2)."""
+    from oracle import mesh
+    rng = np.random.default_rng(0)
+    for cfg in range(256):
+        for _ in range(8):
+            g = np.array([(1 if (cfg >> q) & 1 else -1) * rng.uniform(0.1, 1) for q in range(8)])
+            n_cross = sum((g[q0] > 0) != (g[q1] > 0) for _, q0, q1 in mesh.EDGES)
+            assert sum(len(c) for c in mesh.cube_cycles(g)) == n_cross
+    n = 20
+    ax = np.arange(n, dtype=np.float64)
+    X, Y, Z = np.meshgrid(ax, ax, ax, indexing="ij")
+    F = np.sqrt((X - 9.3) ** 2 + (Y - 9.9) ** 2 + (Z - 9.6) ** 2) + 0.8 * np.sin(0.9 * X) * np.cos(0.7 * Y)
+    v, t = mesh.marching_cubes(F, (n, n, n), 6.0)
+    e = np.concatenate([t[:, [0, 1]], t[:, [1, 2]], t[:, [2, 0]]]).astype(np.int64)
+    key, rkey = e[:, 0] * len(v) + e[:, 1], e[:, 1] * len(v) + e[:, 0]
+    u, c = np.unique(key, return_counts=True)
+    assert (c == 1).all() and np.isin(rkey, u).all()
+    assert len(v) - len(u) // 2 + len(t) == 2

@@ -95,6 +95,25 @@ def test_noalloc_solve_matches_allocating_solve_on_two_calls_in_a_row():
             assert np.abs(x - x_ref).max() <= 1e-12 * np.abs(x_ref).max()
 
 
+def test_noalloc_solve_at_its_largest_accepted_size():
+    """n = GK_NOALLOC_MAX_N (1024 unknowns: 99 orientations, 4 surfaces of 182
+    points, linear drift): the scratch it needs fits the library's array on
+    this device, and the result matches the allocating solve."""
+    from gempy_gb300 import _lib
+    lib = _lib.load()
+    K, b = _random_system(5, n_surf=4, per=182, n_o=99)
+    n = K.shape[0]
+    assert n == _lib.GK_NOALLOC_MAX_N
+    assert lib.gk_solve_mixed_workspace_bytes(n) <= 8 << 20
+    x_ref, info_ref = _solve_allocating(K, b)
+    assert info_ref["residual"] <= 1e-11
+    for _ in range(2):
+        x, info = _solve_noalloc(K, b)
+        assert info["status"] == 0, info
+        assert info["residual"] <= 1e-11
+        assert np.abs(x - x_ref).max() <= 1e-12 * np.abs(x_ref).max()
+
+
 def test_noalloc_solve_rejects_systems_above_its_limit():
     from gempy_gb300 import _lib
     lib = _lib.load()
