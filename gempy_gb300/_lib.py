@@ -20,6 +20,7 @@ GK_MAX_SURFACES = 32
 GK_MAX_FAULTS = 16
 GK_TIE_TOL = 1e-9
 GK_NOALLOC_MAX_N = 1024
+GK_LU_UPDATE_SIMT, GK_LU_UPDATE_TC = 0, 1
 GK_CTA_MAX_N = 4096
 GK_TUNE_EVAL_FF, GK_TUNE_EVAL_F32, GK_TUNE_BATCH_EVAL = 0, 1, 2
 TUNABLES = {"eval_ff": GK_TUNE_EVAL_FF, "eval_f32": GK_TUNE_EVAL_F32, "batch_eval": GK_TUNE_BATCH_EVAL}
@@ -133,6 +134,8 @@ SIGNATURES = [
     ("gk_lu_solve", ctypes.c_int, [ctypes.c_int, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
                                    ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
                                    ctypes.c_void_p, ctypes.c_void_p]),
+    ("gk_lu_update_select", ctypes.c_int, [ctypes.c_int32]),
+    ("gk_lu_update_engine", ctypes.c_int32, []),
     ("gk_gemv", ctypes.c_int, [ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
                                ctypes.c_void_p]),
     ("gk_solve_mixed_workspace_bytes", ctypes.c_size_t, [ctypes.c_int64]),

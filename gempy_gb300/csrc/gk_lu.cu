@@ -823,6 +823,27 @@ __global__ void __launch_bounds__(256, 2) sgemm_update_kernel(float* __restrict_
     }
 }
 
+// The tensor-core form of the FP32 trailing update (gk_lu_tc.cu) and the
+// switch between it and sgemm_update_kernel (gk_lu_update_select).
+gk_status lu_tc_update(float* A, int64_t lda, int64_t k, int kb, int64_t r_lo, int64_t r_hi, int64_t c_lo,
+                       int64_t c_hi, int diag_bs, unsigned nz, gk_info* info, cudaStream_t st);
+bool lu_update_on_tensor_cores();
+cudaError_t wait_cap_set_lu_tc(long long v);
+
+// C -= L U over rows [r_lo, r_hi) x columns [c_lo, c_hi) (or nz diagonal
+// blocks of diag_bs), on the engine gk_lu_update_select chose.
+static gk_status sgemm_update(float* A, int64_t lda, int64_t k, int kb, int64_t r_lo, int64_t r_hi, int64_t c_lo,
+                              int64_t c_hi, int diag_bs, unsigned nz, gk_info* info, cudaStream_t st) {
+    if (lu_update_on_tensor_cores()) return lu_tc_update(A, lda, k, kb, r_lo, r_hi, c_lo, c_hi, diag_bs, nz, info, st);
+    const int64_t rows = diag_bs > 0 ? diag_bs : r_hi - r_lo;
+    const int64_t cols = diag_bs > 0 ? diag_bs : c_hi - c_lo;
+    if (rows <= 0 || cols <= 0) return GK_OK;
+    dim3 grid((unsigned)((cols + 127) / 128), (unsigned)((rows + 127) / 128), nz < 1 ? 1u : nz);
+    sgemm_update_kernel<<<grid, 256, 0, st>>>(A, lda, k, kb, r_lo, r_hi, c_lo, c_hi, diag_bs);
+    GK_LAUNCH_CHECK();
+    return GK_OK;
+}
+
 // ----------------------------------------------------------------------------
 // Solves
 // ----------------------------------------------------------------------------
@@ -1191,11 +1212,12 @@ static gk_status lu_factor(int64_t n, T* A, int64_t lda, int32_t* ipiv, void* wo
             dim3 grid((unsigned)((rest + BN - 1) / BN), (unsigned)((rest + BM - 1) / BM));
             if (sizeof(T) == 4 && ((k + kb) % 4) == 0 && (lda % 4) == 0 &&
                 ((uintptr_t)A % 16) == 0) {
-                sgemm_update_kernel<<<grid, 256, 0, st>>>((float*)A, lda, k, kb, k + kb, n, k + kb, n, 0);
+                gk_status s = sgemm_update((float*)A, lda, k, kb, k + kb, n, k + kb, n, 0, 1, info, st);
+                if (s != GK_OK) return s;
             } else {
                 gemm_update_kernel<T, BM, BN, 16><<<grid, 256, 0, st>>>(A, lda, n, k, kb);
+                GK_LAUNCH_CHECK();
             }
-            GK_LAUNCH_CHECK();
         }
     }
     // row permutation for the solves, kept in the workspace
@@ -1235,12 +1257,14 @@ static gk_status lu_factor_nopiv(int64_t n, T* A, int64_t lda, int32_t* ipiv, vo
             constexpr int BM = sizeof(T) == 8 ? 64 : 128;
             constexpr int BN = BM;
             dim3 grid((unsigned)((rest + BN - 1) / BN), (unsigned)((rest + BM - 1) / BM));
-            if (sizeof(T) == 4 && ((k + kb) % 4) == 0 && (lda % 4) == 0 && ((uintptr_t)A % 16) == 0) {
-                sgemm_update_kernel<<<grid, 256, 0, st>>>((float*)A, lda, k, kb, k + kb, n, k + kb, n, 0);
+            if (sizeof(T) == 4 && ((k + kb) % 4) == 0 && (lda % 4) == 0 &&
+                ((uintptr_t)A % 16) == 0) {
+                gk_status s = sgemm_update((float*)A, lda, k, kb, k + kb, n, k + kb, n, 0, 1, info, st);
+                if (s != GK_OK) return s;
             } else {
                 gemm_update_kernel<T, BM, BN, 16><<<grid, 256, 0, st>>>(A, lda, n, k, kb);
+                GK_LAUNCH_CHECK();
             }
-            GK_LAUNCH_CHECK();
         }
     }
     int32_t* perm = (int32_t*)((char*)work + panel_ws_bytes<T, NB>(sms));
@@ -1660,18 +1684,15 @@ static gk_status twolevel_setup(int64_t n, const double* K, int64_t ldk, const i
         float* Af = (float*)A;
         if (o < r) {
             // landmark rows, all columns to the right
-            dim3 ga((unsigned)((n - o + 127) / 128), (unsigned)((r - o + 127) / 128));
-            sgemm_update_kernel<<<ga, 256, 0, st>>>(Af, lda, k, kb, o, r, o, n, 0);
-            GK_LAUNCH_CHECK();
+            gk_status s = sgemm_update(Af, lda, k, kb, o, r, o, n, 0, 1, info, st);
+            if (s != GK_OK) return s;
             // remaining rows, landmark columns
-            dim3 gb((unsigned)((r - o + 127) / 128), (unsigned)((n - r + 127) / 128));
-            sgemm_update_kernel<<<gb, 256, 0, st>>>(Af, lda, k, kb, r, n, o, r, 0);
-            GK_LAUNCH_CHECK();
+            s = sgemm_update(Af, lda, k, kb, r, n, o, r, 0, 1, info, st);
+            if (s != GK_OK) return s;
         }
         // diagonal blocks of the Schur complement
-        dim3 gc((unsigned)((bs + 127) / 128), (unsigned)((bs + 127) / 128), (unsigned)nblk);
-        sgemm_update_kernel<<<gc, 256, 0, st>>>(Af, lda, k, kb, r, n, r, n, bs);
-        GK_LAUNCH_CHECK();
+        gk_status s = sgemm_update(Af, lda, k, kb, r, n, r, n, bs, (unsigned)nblk, info, st);
+        if (s != GK_OK) return s;
     }
     block_lu_kernel<T><<<(unsigned)nblk, block_lu_threads<T>(), 0, st>>>(A, lda, r, n, bs, info);
     GK_LAUNCH_CHECK();
@@ -1759,6 +1780,7 @@ size_t gk_internal_lu_ws_f64(int64_t n) { return lu_ws_bytes<double>(n); }
 extern "C" gk_status gk_set_wait_limit(int64_t spins) {
     const long long v = spins < 0 ? -1 : (long long)spins;
     if (set_wait_cap_here(v) != cudaSuccess) return GK_ERR_CUDA;
+    if (wait_cap_set_lu_tc(v) != cudaSuccess) return GK_ERR_CUDA;
     if (wait_cap_set_eval(v) != cudaSuccess) return GK_ERR_CUDA;
     if (wait_cap_set_batch(v) != cudaSuccess) return GK_ERR_CUDA;
     return GK_OK;

@@ -737,3 +737,16 @@ def marching_cubes(field, dims, level, spacing, origin, mask=None):
     faces = torch.empty((nt, 3), dtype=torch.int32, device=dev)
     check("gk_mc_emit", lib.gk_mc_emit(ctypes.byref(vol), _ptr(work), wb, _ptr(verts), nv, _ptr(faces), nt, st))
     return verts, faces
+
+
+@contextlib.contextmanager
+def lu_update_engine(engine):
+    """Within the block the FP32 trailing updates run on ``engine``
+    (``_lib.GK_LU_UPDATE_TC`` or ``_lib.GK_LU_UPDATE_SIMT``)."""
+    lib = _lib.load()
+    prev = lib.gk_lu_update_engine()
+    check("gk_lu_update_select", lib.gk_lu_update_select(int(engine)))
+    try:
+        yield
+    finally:
+        lib.gk_lu_update_select(prev)

@@ -162,6 +162,19 @@ gk_status gk_lu_factor(gk_prec prec, int64_t n, void* A, int64_t lda,
                        int32_t* ipiv, void* work, size_t work_bytes,
                        gk_info* info, gk_stream stream);
 
+/* Engine of the FP32 trailing updates (Schur-complement products) of every
+ * FP32 factorization -- gk_lu_factor(GK_F32), the FP32 preconditioner of
+ * gk_solve_mixed and the FP32 two-level setup of gk_solve_twolevel: the
+ * tensor cores (GK_LU_UPDATE_TC, the default: tcgen05.mma kind::tf32 with
+ * split operands, three TF32 products per update, ~FP32 accuracy) or the
+ * FP32 SIMT pipe (GK_LU_UPDATE_SIMT).  Process-wide; the FP64 updates always
+ * run on the FP64 pipe.  No reference counterpart: the engine's solve is a
+ * library call. */
+#define GK_LU_UPDATE_SIMT 0
+#define GK_LU_UPDATE_TC 1
+gk_status gk_lu_update_select(int32_t engine);
+int32_t gk_lu_update_engine(void);
+
 /* Solves A x = b with the factors of gk_lu_factor; b is overwritten by x.
  * ``work`` must be the workspace the factorization used: it holds the row
  * permutation gk_lu_factor derived from ipiv. */
