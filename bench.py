@@ -368,7 +368,19 @@ def main():
     K32_[:, :N] = K64_[:, :N].float()
     t_lu32 = _ev(lambda: K.lu_factor(K32_, K.GK_F32))
     t_lu64 = _ev(lambda: K.lu_factor(K64_, K.GK_F64), reps=1)
-    del K64_, K32_
+    # the FP32 trailing updates on either engine: the partially pivoted FP32
+    # LU and the mixed solve (whose preconditioner is the unpivoted FP32 LU)
+    from gempy_gb300 import _lib as L
+    b64_ = K.build(ds, K.GK_F64)[1]
+    eng = {}
+    for name, e in (("tensor_cores_3xtf32", L.GK_LU_UPDATE_TC), ("fp32_simt", L.GK_LU_UPDATE_SIMT)):
+        with K.lu_update_engine(e):
+            its = []
+            t_m = _ev(lambda: its.append(K.solve_mixed(ds, tol=1e-11, K=K64_, b=b64_)[1]))
+            eng[name] = {"lu_f32_partial_pivoting_ms": _ev(lambda: K.lu_factor(K32_, K.GK_F32)),
+                         "mixed_solve_ms": t_m, "fgmres_iterations": int(K.read_info(its[-1])["iterations"])}
+    del K64_, K32_, b64_
+    mesh = mesh_section(fld_m, iso_m, grid) if rank == 0 else None
     pk0 = peaks()
     kern = {
         "build_f64": {"ms": t_build, "bytes": N * N * 8, "achieved_GBps": N * N * 8 / (t_build * 1e-3) / 1e9,
@@ -380,8 +392,12 @@ def main():
         "eval_ff": {"ms": ev_mixed, "points": n_pts},
         "segmentation": {"fused": True, "bytes_per_point": 8 + 8,
                          "note": "written in the evaluation epilogue; no separate pass over the field"},
-        "tensor_pipe": {"used": False, "note": "float-float on the FP32 pipe: TF32/BF16 products cannot "
-                                               "meet the 1e-6 field-error target on this workload"},
+        "lu_f32_update_engines": eng,
+        "tensor_pipe": {"used": True,
+                        "where": "FP32 LU trailing updates (tcgen05.mma kind::tf32, 3 split-operand products, "
+                                 "TMEM accumulators) of the mixed solve's preconditioner and of gk_lu_factor(F32)",
+                        "not_used_for": "the field evaluation: float-float on the FP32 pipe, because TF32/BF16 "
+                                        "products cannot meet the 1e-6 field-error target on this workload"},
     }
 
     # ---- end to end through compute_model with host inputs (H2D + D2H inside)
@@ -462,6 +478,8 @@ def main():
                      "fp32_pipe_achieved": achieved_tf * FF_OPS_PER_PAIR / 20,
                      "fp32_pipe_frac": achieved_tf * FF_OPS_PER_PAIR / 20 / fp32_peak},
     }
+    if mesh is not None:
+        line["mesh"] = mesh
     if not args.no_extra and rank == 0:
         line["plain"] = plain_section()
         line["batch"] = batch_section(n_real=args.batch_realisations)
@@ -473,6 +491,50 @@ def main():
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def mesh_section(field, isovalues, grid):
+    """Marching cubes of every surface of the precision workload on its 256^3
+    dense-grid field (gk_mc_count + gk_mc_emit per surface, one host read of
+    the counts in between), timed with CUDA events.  Algorithmic bytes: the
+    field read once per surface plus the vertices and triangles written."""
+    import torch
+    from gempy_gb300 import kernels as K
+    res = [int(v) for v in grid.regular_grid_shape]
+    ext = np.asarray(grid.orthogonal_extent, dtype=np.float64)
+    sp = (ext[1::2] - ext[0::2]) / np.asarray(res, dtype=np.float64)
+    f = field.reshape(-1).contiguous()
+    out = []
+
+    def run():
+        out.clear()
+        for lev in isovalues:
+            out.append(K.marching_cubes(f, res, float(lev), sp, ext[0::2]))
+    run()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(3):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        run()
+        b.record()
+        torch.cuda.synchronize()
+        ts.append(a.elapsed_time(b))
+    ms = float(np.median(ts))
+    nv = sum(int(v.shape[0]) for v, _ in out)
+    nt = sum(int(t.shape[0]) for _, t in out)
+    n = int(np.prod(res))
+    alg = len(isovalues) * n * 8 + nv * 24 + nt * 12
+    pk = peaks()
+    return {"workload": f"{len(isovalues)} level surfaces of the {res[0]}^3 precision-workload field",
+            "ms": ms, "ms_per_surface": ms / len(isovalues), "vertices": nv, "triangles": nt,
+            "launches_per_surface": 4,
+            "algorithmic_bytes": alg, "achieved_GBps": alg / (ms * 1e-3) / 1e9,
+            "hbm_peak_GBps": pk.get("hbm_gbs"),
+            "frac_of_hbm": alg / (ms * 1e-3) / 1e9 / pk["hbm_gbs"] if pk.get("hbm_gbs") else None,
+            "note": "per surface: a count pass and a vertex pass over the field, a triangle pass over the "
+                    "cubes, a scan of block counts; the host reads the two counts to size the outputs"}
 
 
 def batch_section(n_real=512, res=64, plain=True):
