@@ -192,6 +192,10 @@ SIGNATURES = [
                                    ctypes.c_void_p]),
     ("gk_mc_emit", ctypes.c_int, [ctypes.POINTER(GkMcVolume), ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
                                   ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),
+    ("gk_gravity_tz", ctypes.c_int, [ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                     ctypes.c_void_p, ctypes.c_void_p]),
+    ("gk_gravity", ctypes.c_int, [ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
+                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     ("gk_batch_workspace_bytes", ctypes.c_size_t, [ctypes.POINTER(GkBatch)]),
     ("gk_batch_points", ctypes.c_int64, [ctypes.POINTER(GkBatch)]),
     ("gk_batch_plan", ctypes.c_int, [ctypes.POINTER(GkBatch), ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),

@@ -190,6 +190,74 @@ class GenericGrid:
 
 
 @dataclass
+class CenteredGrid:
+    """Kernel of voxels around each device, the grid behind forward gravity
+    (``gp.set_centered_grid(grid, centers, resolution, radius)``,
+    ``gempy/API/grid_API.py:99-108``; the engine's adapter hands it over with
+    centres and radius in the transformed frame, ``gempy/modules/
+    data_manipulation/_engine_factory.py:82-87``).
+
+    Kernel per axis: x and y symmetric about the device at
+    ``radius * [-g[::-1], 0, g]``, ``g = geomspace(0.01, 1, resolution // 2)``;
+    z below it only, at ``-radius * (0.05 + [0, geomspace(0.01, 1,
+    resolution)])``.  Each voxel reaches half-way to its neighbours and the
+    outermost ones as far out as they reach in, so the voxels tile a box.
+    ``kernel_grid_centers`` are relative to the device, ``left_voxel_edges`` /
+    ``right_voxel_edges`` the half-widths below / above each centre (positive),
+    all in ``ij`` order (x slowest); ``values`` lists every device's kernel
+    points, device-major."""
+    centers: np.ndarray
+    resolution: np.ndarray
+    radius: np.ndarray
+    kernel_grid_centers: np.ndarray = field(init=False)
+    left_voxel_edges: np.ndarray = field(init=False)
+    right_voxel_edges: np.ndarray = field(init=False)
+
+    def __post_init__(self):
+        self.centers = np.asarray(self.centers, dtype=np.float64).reshape(-1, 3)
+        self.resolution = np.asarray(self.resolution).astype(np.int64).reshape(3)
+        self.radius = np.broadcast_to(np.asarray(self.radius, dtype=np.float64), (3,)).copy()
+        nodes = [self._axis(int(self.resolution[a]), float(self.radius[a]), a == 2) for a in range(3)]
+
+        def grid(k):
+            m = np.meshgrid(nodes[0][k], nodes[1][k], nodes[2][k], indexing="ij")
+            return np.stack([a.ravel() for a in m], axis=1)
+        self.kernel_grid_centers, self.left_voxel_edges, self.right_voxel_edges = grid(0), grid(1), grid(2)
+
+    @staticmethod
+    def _axis(resolution, radius, vertical):
+        if vertical:
+            g = np.geomspace(0.01, 1.0, resolution)
+            c = (-radius * (0.05 + np.concatenate(([0.0], g))))[::-1]
+        else:
+            g = np.geomspace(0.01, 1.0, resolution // 2)
+            c = radius * np.concatenate((-g[::-1], [0.0], g))
+        d = np.diff(c) / 2.0
+        return c, np.concatenate(([d[0]], d)), np.concatenate((d, [d[-1]]))
+
+    @property
+    def n_devices(self):
+        return len(self.centers)
+
+    @property
+    def n_voxels(self):
+        return len(self.kernel_grid_centers)
+
+    @property
+    def values(self):
+        return (self.centers[:, None, :] + self.kernel_grid_centers[None]).reshape(-1, 3)
+
+
+@dataclass
+class GeophysicsInput:
+    """``tz`` per kernel voxel (``calculate_gravity_gradient``) and the
+    density of every lithology id (1-based), as the reference's
+    ``GeophysicsInput(tz, densities)`` (``test_gravity.py:74-78``)."""
+    tz: np.ndarray
+    densities: np.ndarray
+
+
+@dataclass
 class EngineGrid:
     octree_grid: Optional[RegularGrid] = None
     dense_grid: Optional[RegularGrid] = None

@@ -637,6 +637,13 @@ def _compute_model(interpolation_input, options, data_descriptor, geophysics_inp
         pts = torch.as_tensor(grid.custom_grid.values).to(device)
         e = ev.run(K.Points(xyz=pts))
         raw.custom = e.block
+    grav = None
+    cg = getattr(grid, "geophysics_grid", None)
+    if cg is not None and geophysics_input is not None and getattr(geophysics_input, "tz", None) is not None:
+        # forward gravity: segment the centred grid's points, then density x tz per device
+        from . import gravity as G
+        e = ev.run(K.Points(xyz=torch.as_tensor(cg.values).to(device)))
+        grav = G.device_gravity(e.lith_ids, cg, geophysics_input, device)
     if cfg.timings:
         torch.cuda.synchronize()
         timings["grids_s"] = time.perf_counter() - t2
@@ -648,7 +655,8 @@ def _compute_model(interpolation_input, options, data_descriptor, geophysics_inp
     sol = Solutions(octrees_output=octrees, root_output=root, raw_arrays=raw,
                     scalar_field_at_surface_points=sfsp, _ordered_elements=[s.order for s in series],
                     block_solution_type=options.block_solutions_type, timings=timings,
-                    solver_info=[s.info_host for s in series])
+                    solver_info=[s.info_host for s in series],
+                    gravity=None if grav is None else grav.cpu().numpy())
     if cfg.timings:
         torch.cuda.synchronize()
         t3 = time.perf_counter()

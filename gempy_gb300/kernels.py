@@ -750,3 +750,29 @@ def lu_update_engine(engine):
         yield
     finally:
         lib.gk_lu_update_select(prev)
+
+
+def gravity_tz(centres, lower, upper):
+    """tz of every voxel of a centred-grid kernel (gk_gravity_tz); (n, 3)
+    CUDA FP64 tensors in, (n,) out."""
+    lib = _lib.load()
+    n = int(centres.shape[0])
+    c, lo, hi = (t.to(dtype=torch.float64).contiguous() for t in (centres, lower, upper))
+    out = torch.empty(n, dtype=torch.float64, device=c.device)
+    check("gk_gravity_tz", lib.gk_gravity_tz(n, _ptr(c), _ptr(lo), _ptr(hi), _ptr(out), _stream()))
+    return out
+
+
+def gravity(ids, n_devices, densities, tz):
+    """Density-weighted tz sum per device over lithology ids (gk_gravity)."""
+    lib = _lib.load()
+    n_vox = int(tz.shape[0])
+    ids = ids.to(dtype=torch.int32).contiguous()
+    rho = densities.to(device=ids.device, dtype=torch.float64).contiguous()
+    tz = tz.to(device=ids.device, dtype=torch.float64).contiguous()
+    if ids.numel() != n_devices * n_vox:
+        raise ValueError(f"{ids.numel()} ids for {n_devices} devices x {n_vox} voxels")
+    out = torch.empty(n_devices, dtype=torch.float64, device=ids.device)
+    check("gk_gravity", lib.gk_gravity(int(n_devices), n_vox, _ptr(ids), int(rho.numel()), _ptr(rho), _ptr(tz),
+                                       _ptr(out), _stream()))
+    return out

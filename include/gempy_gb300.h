@@ -480,6 +480,27 @@ gk_status gk_mc_emit(const gk_mc_volume* vol, void* work, size_t work_bytes,
                      double* vertices, int64_t max_vertices, int32_t* faces,
                      int64_t max_faces, gk_stream stream);
 
+/* ---------------- forward gravity (engine geophysics) -------------------- */
+
+/* Vertical attraction per unit density of each voxel of a centred-grid
+ * kernel at its device, the reference's gp.calculate_gravity_gradient
+ * (imported at gempy/API/__init__.py:65, used at test/test_modules/
+ * test_geophysics/test_gravity.py:67-80): the closed-form prism attraction
+ * (Nagy 1966; Plouff 1976), z up (mass below gives tz < 0), G = 6.674e-3
+ * (lengths in m, densities in g/cm^3, tz in mGal).  ``centres``, ``lower``
+ * and ``upper`` are n_voxels x 3: voxel centres relative to the device and
+ * the half-widths below and above them per axis. */
+gk_status gk_gravity_tz(int64_t n_voxels, const double* centres,
+                        const double* lower, const double* upper, double* tz,
+                        gk_stream stream);
+/* Solutions.gravity: gravity[d] = sum_v densities[ids[d n_voxels + v] - 1]
+ * tz[v] for every device d (ids are lithology ids 1..n_units of the
+ * segmented kernel points, device-major; ids outside that range add 0),
+ * reduced in a fixed order.  ``densities`` has n_units entries (device). */
+gk_status gk_gravity(int64_t n_devices, int64_t n_voxels, const int32_t* ids,
+                     int32_t n_units, const double* densities, const double* tz,
+                     double* gravity, gk_stream stream);
+
 /* ---------------- batched realisations (many compute_model calls) ------- */
 
 /* One realisation of a batch: a single-series model, its 3-D regular grid

@@ -285,3 +285,40 @@ def test_marching_cubes_cycles_close_for_every_cube_configuration():
     u, c = np.unique(key, return_counts=True)
     assert (c == 1).all() and np.isin(rkey, u).all()
     assert len(v) - len(u) // 2 + len(t) == 2
+
+
+def test_prism_attraction_matches_quadrature_and_kernel_tiles_its_box():
+    """The closed-form prism attraction (Nagy 1966; Plouff 1976) against
+    Gauss-Legendre quadrature of G z / r^3, and the centred-grid kernel of the
+    reference's gravity test (resolution [10, 10, 100], radius 16000,
+    test/test_modules/test_geophysics/test_gravity.py:67-72) tiling its box:
+    the voxels' tz add up to the whole box's."""
+    from oracle import gravity
+    x, w = np.polynomial.legendre.leggauss(40)
+    for box in [(-1, 2, -0.5, 1.5, -3, -1), (0.5, 1.5, 0.2, 0.9, -2, -0.7), (-2, -1, 1, 3, 0.5, 2.5)]:
+        x0, x1, y0, y1, z0, z1 = box
+        X, Y, Z = [(b - a) / 2 * x + (b + a) / 2 for a, b in ((x0, x1), (y0, y1), (z0, z1))]
+        W = np.einsum("i,j,k->ijk", w, w, w) * (x1 - x0) * (y1 - y0) * (z1 - z0) / 8
+        XX, YY, ZZ = np.meshgrid(X, Y, Z, indexing="ij")
+        q = gravity.G_MGAL * (W * ZZ / np.sqrt(XX ** 2 + YY ** 2 + ZZ ** 2) ** 3).sum()
+        assert abs(gravity.prism_tz(*box) - q) <= 1e-12 * abs(q)
+    c, lo, hi = gravity.kernel([10, 10, 100], 16000.0)
+    assert len(c) == 11 * 11 * 101
+    a, b = c - lo, c + hi
+    box = gravity.prism_tz(a[:, 0].min(), b[:, 0].max(), a[:, 1].min(), b[:, 1].max(), a[:, 2].min(), b[:, 2].max())
+    t = gravity.tz([10, 10, 100], 16000.0)
+    assert abs(t.sum() - box) <= 1e-9 * abs(box)
+    assert (t < 0).all()        # every voxel lies below the device
+
+
+def test_centered_grid_matches_oracle_kernel():
+    """The package's CenteredGrid (host set-up of the gravity grid) builds the
+    oracle's kernel: same voxel centres and half-widths, device-major points."""
+    from gempy_gb300.data import CenteredGrid
+    from oracle import gravity
+    cg = CenteredGrid(np.array([[6.0, 0.0, 4.0], [1.0, 2.0, 3.0]]), [10, 10, 100], [16000.0, 8000.0, 16000.0])
+    c, lo, hi = gravity.kernel([10, 10, 100], [16000.0, 8000.0, 16000.0])
+    np.testing.assert_array_equal(cg.kernel_grid_centers, c)
+    np.testing.assert_array_equal(cg.left_voxel_edges, lo)
+    np.testing.assert_array_equal(cg.right_voxel_edges, hi)
+    np.testing.assert_array_equal(cg.values, gravity.points(cg.centers, [10, 10, 100], [16000.0, 8000.0, 16000.0]))
