@@ -649,7 +649,7 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchDesc* __rest
         const BatchDesc& d = D[s];
         const int64_t c = item - chunk_prefix[s];
         const double q = d.meta[0], inv_a = d.meta[2];
-        const float eps2 = (float)(kDistEps2 * inv_a * inv_a);
+        const float eps2 = fmaxf((float)(kDistEps2 * inv_a * inv_a), 1.17549435e-38f);  // a positive normal float
         const int nt = tiles_of(s);
         const int to = (d.n_ori + rec_ori - 1) / rec_ori;
         const int nyz = d.dims[1] * d.dims[2];

@@ -195,6 +195,7 @@ struct EvalParams {
     double* values;
     int32_t* ids;
     gk_info* info;     // device status word (timeouts), may be NULL
+    int col;           // float-float path: each thread takes two consecutive points of one grid column
 };
 
 template <typename T> __device__ __forceinline__ T fast_r(T r2);
@@ -512,7 +513,7 @@ __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const 
     __syncthreads();
     if (SPLIT) cg::this_cluster().sync();  // abort words initialised before any peer can set one
     const double q = meta[0], inv_a = meta[2];
-    const float eps2 = (float)(kDistEps2 * inv_a * inv_a);
+    const float eps2 = fmaxf((float)(kDistEps2 * inv_a * inv_a), 1.17549435e-38f);  // a positive normal float
     const int64_t chunk_pts = (int64_t)blockDim.x * PPT;
     const int64_t n_chunks = (P.n + chunk_pts - 1) / chunk_pts;
     const int n_tiles = P.tiles_ori + P.tiles_sp;
@@ -545,21 +546,26 @@ __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const 
     };
     if (n_items > 0) issue(0);
     if (n_items > 1) issue(1);
+    // point of slot p within a chunk: strided by the block, or (col) two
+    // consecutive points of one grid column, which share x and y
+    const bool col = PPT == 2 && P.col != 0;
+    auto slot = [&](int p) -> int64_t { return col ? (int64_t)PPT * tid + p : tid + (int64_t)p * blockDim.x; };
 
     int64_t item = 0;
     for (int64_t lc = 0; lc < my_chunks; ++lc) {
         const int64_t chunk = group + lc * n_groups;
         PointFF X[PPT];
-        bool all_exact = true, act[PPT], any_act = false;
+        bool all_exact = true, act[PPT], any_act = false, all_act = true;
 #pragma unroll
         for (int p = 0; p < PPT; ++p) {
-            const int64_t pidp = chunk * chunk_pts + tid + (int64_t)p * blockDim.x;
+            const int64_t pidp = chunk * chunk_pts + slot(p);
             act[p] = pidp < P.n;
             double xd[3];
             point_coords(P, act[p] ? pidp : P.n - 1, xd);
             ff_point(xd, inv_a, q, X[p]);
             all_exact = all_exact && (X[p].exact || !act[p]);
             any_act = any_act || act[p];
+            all_act = all_act && act[p];
         }
         double Z[PPT];
 #pragma unroll
@@ -586,7 +592,16 @@ __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const 
                 const bool ori = t < P.tiles_ori;
                 const int nr = ori ? min(P.rec_ori, P.n_ori - t * P.rec_ori)
                                    : min(P.rec_sp, P.n_sp - (t - P.tiles_ori) * P.rec_sp);
-                if (!any_act) {
+                bool done = !any_act;
+                if constexpr (PPT == 2) {
+                    if (!done && col && all_exact && all_act) {
+                        ff_tile_col2(rec, ori, nr, X, eps2, acc);
+                        done = true;
+                    }
+                }
+                if (done) {
+                } else if (all_exact && all_act) {
+                    ff_tile<PPT, true, true>(rec, ori, nr, X, act, eps2, acc);
                 } else if (all_exact) {
                     ff_tile<PPT, true>(rec, ori, nr, X, act, eps2, acc);
                 } else {
@@ -601,13 +616,13 @@ __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const 
         if (SPLIT) {
             double* red = reinterpret_cast<double*>(smem + 2 * (size_t)P.stage_bytes);
 #pragma unroll
-            for (int p = 0; p < PPT; ++p) red[tid + p * blockDim.x] = Z[p];
+            for (int p = 0; p < PPT; ++p) red[slot(p)] = Z[p];
             if (split_finish<float, 1>(P, chunk, chunk_pts, rank, red, &s_abort, s_fail != 0)) goto drain;
         } else {
 #pragma unroll
             for (int p = 0; p < PPT; ++p) {
                 if (!act[p]) continue;
-                const int64_t pidp = chunk * chunk_pts + tid + (int64_t)p * blockDim.x;
+                const int64_t pidp = chunk * chunk_pts + slot(p);
                 double xd[3];
                 point_coords(P, pidp, xd);
                 finish_point<float>(P, pidp, xd, Z[p], nullptr);
@@ -817,6 +832,9 @@ static gk_status launch_eval(EvalParams& P, cudaStream_t st, int stage_kb = 32) 
 
 template <int PPT>
 static gk_status launch_eval_ff(EvalParams& P, const double* meta, cudaStream_t st, int stage_kb) {
+    // a regular grid with an even number of points per column: each thread's
+    // two points share their column (x, y)
+    P.col = (PPT == 2 && P.kind == 0 && P.dims[2] % 2 == 0) ? 1 : 0;
     return launch_chunks(eval_ff_kernel<PPT, false>, eval_ff_kernel<PPT, true>, P, PPT, stage_kb,
                          (int)(16 * sizeof(float)), (int)(8 * sizeof(float)), 1, st, meta);
 }

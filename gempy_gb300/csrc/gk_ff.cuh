@@ -79,6 +79,15 @@ __device__ __forceinline__ ff ff_sqrt(ff a) {
     return {s, e * 0.5f * y};
 }
 
+// ff_sqrt for an argument known to be positive: r^2 + eps2 of the tile
+// loops, whose distance regulariser eps2 is a positive normal float.
+__device__ __forceinline__ ff ff_sqrt_pos(ff a) {
+    float y = rsqrtf(a.h);
+    float s = a.h * y;
+    float e = __fmaf_rn(-s, s, a.h) + a.l;
+    return {s, e * 0.5f * y};
+}
+
 __device__ __forceinline__ double ff_to_double(ff a) { return (double)a.h + (double)a.l; }
 
 // ---------------------------------------------------------------------------
@@ -228,8 +237,10 @@ __device__ __forceinline__ ff ff_dist2(const PointFF& X, const float* ph, const 
 // records (16 floats: x, y, z hi/lo, then w_x, w_y, w_z hi/lo) add
 // C'/r(|x - x_o|) (w . (x_o - x)), surface-point records (8 floats: x, y, z
 // hi/lo, alpha hi/lo) add alpha C(|x - p|); coordinates are scaled by 1/range.
-// EXACT: every point's split is exact (the common case).
-template <int PPT, bool EXACT>
+// EXACT: every point's split is exact (the common case).  ALL_ACT: every
+// point slot holds a point (all but a grid's last chunk), so the per-pair
+// slot test is compiled out.  eps2 must be a positive normal float.
+template <int PPT, bool EXACT, bool ALL_ACT = false>
 __device__ __forceinline__ void ff_tile(const float* __restrict__ rec, bool orientation, int nr,
                                         const PointFF (&X)[PPT], const bool (&act)[PPT], float eps2,
                                         ffacc (&acc)[PPT]) {
@@ -241,11 +252,11 @@ __device__ __forceinline__ void ff_tile(const float* __restrict__ rec, bool orie
             const ff wx = {a1.z, a1.w}, wy = {a2.x, a2.y}, wz = {a2.z, a2.w};
 #pragma unroll
             for (int p = 0; p < PPT; ++p) {
-                if (!act[p]) continue;  // a slot past the end of the point list
+                if (!ALL_ACT && !act[p]) continue;  // a slot past the end of the point list
                 float dh[3], dl[3];
                 const ff r2 = ff_dist2<EXACT>(X[p], ph, pl, dh, dl, eps2);
                 if (r2.h >= 1.f) continue;  // beyond the range: C'/r = 0
-                const ff k = ff_cubic_d1(r2, ff_sqrt(r2));
+                const ff k = ff_cubic_d1(r2, ff_sqrt_pos(r2));
                 // h = x_o - x = -(dh + dl)
                 const ff wh = ff_dot3(wx, wy, wz, ff{-dh[0], -dl[0]}, ff{-dh[1], -dl[1]}, ff{-dh[2], -dl[2]});
                 ff_acc_fma(acc[p], k, wh);
@@ -263,16 +274,65 @@ __device__ __forceinline__ void ff_tile(const float* __restrict__ rec, bool orie
             const ff W = {a1.z, a1.w};
 #pragma unroll
             for (int p = 0; p < PPT; ++p) {
-                if (!act[p]) continue;
+                if (!ALL_ACT && !act[p]) continue;
                 float dh[3], dl[3];
                 const ff r2 = ff_dist2<EXACT>(X[p], ph, pl, dh, dl, eps2);
                 if (r2.h >= 1.f) continue;  // beyond the range: C = 0
-                ff_acc_fma(acc[p], ff_cubic_C(r2, ff_sqrt(r2)), W);
+                ff_acc_fma(acc[p], ff_cubic_C(r2, ff_sqrt_pos(r2)), W);
             }
             if ((qr & 7) == 7) {
 #pragma unroll
                 for (int p = 0; p < PPT; ++p) ff_acc_norm(acc[p]);
             }
+        }
+    }
+}
+
+// ff_tile for two points of one grid column (equal x and y, exact splits,
+// both slots filled): the x and y terms of r^2 -- their exact squares, the
+// two-sum of their high words and the low-order terms -- are formed once per
+// record and shared; only the z terms are per point.
+__device__ __forceinline__ void ff_tile_col2(const float* __restrict__ rec, bool orientation, int nr,
+                                             const PointFF (&X)[2], float eps2, ffacc (&acc)[2]) {
+    for (int qr = 0; qr < nr; ++qr) {
+        const float* R = rec + (orientation ? 16 : 8) * qr;
+        const float4 a0 = reinterpret_cast<const float4*>(R)[0];
+        const float4 a1 = reinterpret_cast<const float4*>(R)[1];
+        const float dh0 = X[0].h[0] - a0.x, dl0 = X[0].l[0] - a0.y;
+        const float dh1 = X[0].h[1] - a0.z, dl1 = X[0].l[1] - a0.w;
+        const ff b0 = two_prod(dh0, dh0), b1 = two_prod(dh1, dh1);
+        const ff sxy = two_sum(b0.h, b1.h);
+        float lxy = sxy.l + b0.l + b1.l + eps2;
+        lxy = __fmaf_rn(dl0, 2.f * dh0 + dl0, lxy);
+        lxy = __fmaf_rn(dl1, 2.f * dh1 + dl1, lxy);
+        ff wx = {0.f, 0.f}, wy = {0.f, 0.f}, wz = {0.f, 0.f}, W = {a1.z, a1.w};
+        if (orientation) {
+            const float4 a2 = reinterpret_cast<const float4*>(R)[2];
+            wx = ff{a1.z, a1.w};
+            wy = ff{a2.x, a2.y};
+            wz = ff{a2.z, a2.w};
+        }
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+            const float dh2 = X[p].h[2] - a1.x, dl2 = X[p].l[2] - a1.y;
+            const ff b2 = two_prod(dh2, dh2);
+            const ff s2 = two_sum(sxy.h, b2.h);
+            float low = lxy + s2.l + b2.l;
+            low = __fmaf_rn(dl2, 2.f * dh2 + dl2, low);
+            const ff r2 = fast_two_sum(s2.h, low);
+            if (r2.h >= 1.f) continue;  // beyond the range: C = C'/r = 0
+            if (orientation) {
+                const ff k = ff_cubic_d1(r2, ff_sqrt_pos(r2));
+                // h = x_o - x = -(dh + dl)
+                const ff wh = ff_dot3(wx, wy, wz, ff{-dh0, -dl0}, ff{-dh1, -dl1}, ff{-dh2, -dl2});
+                ff_acc_fma(acc[p], k, wh);
+            } else {
+                ff_acc_fma(acc[p], ff_cubic_C(r2, ff_sqrt_pos(r2)), W);
+            }
+        }
+        if ((qr & 7) == 7) {  // fold the low words back every 8 records
+            ff_acc_norm(acc[0]);
+            ff_acc_norm(acc[1]);
         }
     }
 }

@@ -13,19 +13,19 @@
 // which is what the preconditioner of the mixed solve needs (its FGMRES
 // absorbs rounding of that size, as it does the SIMT kernel's).
 //
-// One CTA of 8 warps per 128 x 128 tile of C.  The CTA stages the tile's
-// 128 x kb slice of the panel (A operand, K-major as stored) and the kb x 128
-// slice of the row block (B operand, transposed to K-major while staging),
-// both split into hi/lo, in shared memory in the canonical no-swizzle K-major
-// layout: core matrices of 8 rows x 16 bytes (4 TF32), K-adjacent core
-// matrices 128 bytes apart (LBO), 8-row groups 2048 bytes apart (SBO, 16 core
-// matrices along K = 64); every thread issues all of its staging loads before
-// its first store.  One thread issues 3 x kb/8 tcgen05.mma (cta_group::1,
-// kind::tf32, M = N = 128, K = 8) into a 128-column FP32 accumulator in
-// tensor memory and commits them to an mbarrier; meanwhile every thread loads
-// its 64 entries of C (one row, half the columns).  After the bounded wait
-// each warp reads its row's accumulators with tcgen05.ld (warps w and w + 4
-// share TMEM lanes 32 (w % 4) ..) and writes C back.
+// Tiles of 128 x 128 of C, walked by one persistent 8-warp CTA per SM.  Per
+// tile the CTA stages the 128 x kb slice of the panel (A operand, K-major as
+// stored) and the kb x 128 slice of the row block (B operand, transposed to
+// K-major while staging), both split into hi/lo, in shared memory in the
+// canonical no-swizzle K-major layout: core matrices of 8 rows x 16 bytes (4
+// TF32), K-adjacent core matrices 128 bytes apart (LBO), 8-row groups 2048
+// bytes apart (SBO, 16 core matrices along K = 64).  One thread issues
+// 3 x kb/8 tcgen05.mma (cta_group::1, kind::tf32, M = N = 128, K = 8) into
+// one of two 128-column FP32 accumulators in tensor memory and commits them
+// to an mbarrier.  While they run, the CTA writes back the previous tile
+// (tcgen05.ld of its accumulator, warps w and w + 4 sharing TMEM lanes
+// 32 (w % 4) ..) and loads this tile's C and the next tile's operands into
+// registers, so loads, MMAs and write-backs of neighbouring tiles overlap.
 #include <atomic>
 
 #include "gk_common.cuh"
@@ -41,7 +41,7 @@ constexpr int kAIters = kBM * kKP / 4 / kThreads;     // float4 loads of A per t
 constexpr int kBIters = (kBN / 4) * (kKP / 4) / kThreads;  // 4 x 4 blocks of B per thread
 constexpr uint32_t kOpBytes = kBM * kKP * 4;   // one operand buffer: 32 KB
 constexpr uint32_t kSmemBytes = 4 * kOpBytes;  // A hi, A lo, B hi, B lo
-constexpr uint32_t kTmemCols = 128;
+constexpr uint32_t kTmemCols = 2 * kBN;       // two accumulators: MMA of one tile, write-back of the previous
 constexpr uint32_t kSbo = (kKP / 4) * 128;
 
 __device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -94,19 +94,43 @@ __device__ __forceinline__ void store_split(unsigned char* hi, unsigned char* lo
     *reinterpret_cast<float4*>(lo + off) = l;
 }
 
-__global__ void __launch_bounds__(kThreads, 1) update_kernel(float* __restrict__ A, int64_t lda, int64_t k, int kb,
-                                                             int64_t r_lo, int64_t r_hi, int64_t c_lo, int64_t c_hi,
-                                                             int diag_bs, gk_info* info) {
-    extern __shared__ __align__(1024) unsigned char smem[];
-    __shared__ __align__(8) uint64_t mbar;
-    __shared__ uint32_t tmem_slot;
+// One tile of C: rows [i0, i0 + 128) x columns [j0, j0 + 128), clipped to
+// r_hi / c_hi.  Tiles are numbered column tile fastest, then row tile, then
+// diagonal block (diag_bs > 0: block z covers [r_lo + z diag_bs, ...) in
+// both ranges).
+struct Tile {
+    int64_t i0, j0, r_hi, c_hi;
+};
+
+__device__ __forceinline__ Tile tile_of(int64_t t, int tx, int ty, int64_t r_lo, int64_t r_hi, int64_t c_lo,
+                                        int64_t c_hi, int diag_bs) {
+    const int64_t per = (int64_t)tx * ty;
+    const int64_t z = t / per, rem = t - z * per;
+    const int64_t by = rem / tx, bx = rem - by * tx;
     if (diag_bs > 0) {
-        const int64_t b0 = r_lo + (int64_t)blockIdx.z * diag_bs;
+        const int64_t b0 = r_lo + z * diag_bs;
         r_lo = c_lo = b0;
         r_hi = c_hi = min(r_hi, b0 + diag_bs);
     }
-    const int64_t i0 = r_lo + (int64_t)blockIdx.y * kBM, j0 = c_lo + (int64_t)blockIdx.x * kBN;
-    if (i0 >= r_hi || j0 >= c_hi) return;
+    return {r_lo + by * kBM, c_lo + bx * kBN, r_hi, c_hi};
+}
+
+// Persistent: one CTA per SM walks the tiles t = blockIdx.x + i gridDim.x.
+// Iteration i: wait for the MMAs of tile i-1 (its operands in shared memory
+// are then free and its accumulator readable), store tile i's operands
+// (loaded into registers during iteration i-1), issue its MMAs into tensor
+// memory buffer i & 1, write back tile i-1 (accumulator from buffer
+// (i-1) & 1, C prefetched during iteration i-1), then load tile i's C and
+// tile i+1's operands into registers.  The loads of one tile overlap the
+// MMAs of the next and the write-back of the previous.
+__global__ void __launch_bounds__(kThreads, 1) update_kernel(float* __restrict__ A, int64_t lda, int64_t k, int kb,
+                                                             int64_t r_lo, int64_t r_hi, int64_t c_lo, int64_t c_hi,
+                                                             int diag_bs, int tx, int ty, int64_t n_tiles,
+                                                             gk_info* info) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_slot;
+    if ((int64_t)blockIdx.x >= n_tiles) return;
     unsigned char* Ah = smem;
     unsigned char* Al = smem + kOpBytes;
     unsigned char* Bh = smem + 2 * kOpBytes;
@@ -124,138 +148,95 @@ __global__ void __launch_bounds__(kThreads, 1) update_kernel(float* __restrict__
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-    // Every global load of the staging is issued before the first store (8
-    // float4 of A and 8 of B per thread in flight), then split and stored.
-    // A operand: rows i0.., k columns; a quarter-warp takes 8 rows of one
-    // 4-column group (conflict-free 16-byte stores), a warp 8 rows x 64 bytes.
-    const int nq = kp8 / 4;                 // 4-column groups staged
-    float4 va[kAIters];
-#pragma unroll
-    for (int it = 0; it < kAIters; ++it) {
-        const int e = tid + it * kThreads;
-        const int l = e & 31, g = e >> 5;
-        const int row = (l & 7) + 8 * (g % (kBM / 8));
-        const int kq = 4 * ((l >> 3) + 4 * (g / (kBM / 8)));
-        const int64_t gi = i0 + row;
-        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (gi < r_hi && kq < kb) {
-            const float* src = A + gi * lda + k + kq;
-            if (kq + 3 < kb) {
-                v = *reinterpret_cast<const float4*>(src);
-            } else {
-                v.x = src[0];
-                if (kq + 1 < kb) v.y = src[1];
-                if (kq + 2 < kb) v.z = src[2];
-            }
-        }
-        va[it] = v;
-    }
-    // B operand: element (n, p) = A[k + p][j0 + n], staged K-major: each
-    // thread loads 4 x 4 blocks (4 rows p, 4 consecutive n) and stores their
-    // transposes as 16-byte rows
-    float4 vb[kBIters][4];
-#pragma unroll
-    for (int it = 0; it < kBIters; ++it) {
-        const int e = tid + it * kThreads;
-        const int n4 = 4 * (e % (kBN / 4)), p4 = 4 * (e / (kBN / 4));
-        const int64_t gj = j0 + n4;
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            const int p = p4 + r;
-            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (p < kb) {
-                const float* src = A + (k + p) * lda + gj;
-                if (gj + 3 < c_hi) {
-                    v = *reinterpret_cast<const float4*>(src);
-                } else {
-                    if (gj < c_hi) v.x = src[0];
-                    if (gj + 1 < c_hi) v.y = src[1];
-                    if (gj + 2 < c_hi) v.z = src[2];
-                }
-            }
-            vb[it][r] = v;
-        }
-    }
-#pragma unroll
-    for (int it = 0; it < kAIters; ++it) {
-        const int e = tid + it * kThreads;
-        const int l = e & 31, g = e >> 5;
-        const int row = (l & 7) + 8 * (g % (kBM / 8));
-        const int kq = 4 * ((l >> 3) + 4 * (g / (kBM / 8)));
-        if (kq < kp8) store_split(Ah, Al, core_off(row, kq), va[it]);
-    }
-#pragma unroll
-    for (int it = 0; it < kBIters; ++it) {
-        const int e = tid + it * kThreads;
-        const int n4 = 4 * (e % (kBN / 4)), p4 = 4 * (e / (kBN / 4));
-        if (p4 >= kp8) continue;
-        store_split(Bh, Bl, core_off(n4 + 0, p4), make_float4(vb[it][0].x, vb[it][1].x, vb[it][2].x, vb[it][3].x));
-        store_split(Bh, Bl, core_off(n4 + 1, p4), make_float4(vb[it][0].y, vb[it][1].y, vb[it][2].y, vb[it][3].y));
-        store_split(Bh, Bl, core_off(n4 + 2, p4), make_float4(vb[it][0].z, vb[it][1].z, vb[it][2].z, vb[it][3].z));
-        store_split(Bh, Bl, core_off(n4 + 3, p4), make_float4(vb[it][0].w, vb[it][1].w, vb[it][2].w, vb[it][3].w));
-    }
-    (void)nq;
-    // generic-proxy stores -> visible to the tensor core; the TMEM address
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_slot;
-    if (tid == 0) {
-        const uint32_t idesc = idesc_tf32(kBM, kBN);
-        const uint32_t ops[3][2] = {{saddr(Ah), saddr(Bh)}, {saddr(Ah), saddr(Bl)}, {saddr(Al), saddr(Bh)}};
-        uint32_t accumulate = 0;
-        for (int pr = 0; pr < 3; ++pr)
-            for (int kk = 0; kk < kp8 / 8; ++kk) {
-                const uint64_t ad = smem_desc(ops[pr][0] + (uint32_t)kk * 256u, 128u, kSbo);
-                const uint64_t bd = smem_desc(ops[pr][1] + (uint32_t)kk * 256u, 128u, kSbo);
-                asm volatile(
-                    "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
-                    " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-                    "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate)
-                    : "memory");
-                accumulate = 1;
+
+    float4 va[kAIters];
+    float4 vb[kBIters][4];
+    float4 cv[kBN / 8];
+    // A operand: a quarter-warp takes 8 rows of one 4-column group
+    // (conflict-free 16-byte stores), a warp 8 rows x 64 bytes
+    auto a_slot = [&](int it, int& row, int& kq) {
+        const int e = tid + it * kThreads;
+        const int l = e & 31, g = e >> 5;
+        row = (l & 7) + 8 * (g % (kBM / 8));
+        kq = 4 * ((l >> 3) + 4 * (g / (kBM / 8)));
+    };
+    // B operand: element (n, p) = A[k + p][j0 + n]; each thread loads 4 x 4
+    // blocks (4 rows p, 4 consecutive n) and stores their transposes
+    auto b_slot = [&](int it, int& n4, int& p4) {
+        const int e = tid + it * kThreads;
+        n4 = 4 * (e % (kBN / 4));
+        p4 = 4 * (e / (kBN / 4));
+    };
+    auto load4 = [&](const float* src, int64_t avail) {
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (avail >= 4) {
+            v = *reinterpret_cast<const float4*>(src);
+        } else {
+            if (avail > 0) v.x = src[0];
+            if (avail > 1) v.y = src[1];
+            if (avail > 2) v.z = src[2];
+        }
+        return v;
+    };
+    auto load_ab = [&](const Tile& T) {
+#pragma unroll
+        for (int it = 0; it < kAIters; ++it) {
+            int row, kq;
+            a_slot(it, row, kq);
+            const int64_t gi = T.i0 + row;
+            va[it] = (gi < T.r_hi && kq < kb) ? load4(A + gi * lda + k + kq, kb - kq) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int it = 0; it < kBIters; ++it) {
+            int n4, p4;
+            b_slot(it, n4, p4);
+            const int64_t gj = T.j0 + n4;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const int p = p4 + r;
+                vb[it][r] = (p < kb && gj < T.c_hi) ? load4(A + (k + p) * lda + gj, T.c_hi - gj)
+                                                    : make_float4(0.f, 0.f, 0.f, 0.f);
             }
-        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                         saddr(&mbar))
-                     : "memory");
-    }
-    // While the MMAs run, each thread loads its part of C: warp w holds TMEM
-    // lanes 32 (w % 4) .. + 31 (its rows), warps 0-3 columns 0-63, warps 4-7
-    // columns 64-127.
+        }
+    };
+    auto store_ab = [&]() {
+#pragma unroll
+        for (int it = 0; it < kAIters; ++it) {
+            int row, kq;
+            a_slot(it, row, kq);
+            if (kq < kp8) store_split(Ah, Al, core_off(row, kq), va[it]);
+        }
+#pragma unroll
+        for (int it = 0; it < kBIters; ++it) {
+            int n4, p4;
+            b_slot(it, n4, p4);
+            if (p4 >= kp8) continue;
+            store_split(Bh, Bl, core_off(n4 + 0, p4), make_float4(vb[it][0].x, vb[it][1].x, vb[it][2].x, vb[it][3].x));
+            store_split(Bh, Bl, core_off(n4 + 1, p4), make_float4(vb[it][0].y, vb[it][1].y, vb[it][2].y, vb[it][3].y));
+            store_split(Bh, Bl, core_off(n4 + 2, p4), make_float4(vb[it][0].z, vb[it][1].z, vb[it][2].z, vb[it][3].z));
+            store_split(Bh, Bl, core_off(n4 + 3, p4), make_float4(vb[it][0].w, vb[it][1].w, vb[it][2].w, vb[it][3].w));
+        }
+    };
+    // each thread owns one row of the tile (TMEM lane 32 (w % 4) + lane) and
+    // half of its columns (warps 0-3 the first 64, warps 4-7 the last 64)
     const int row = (warp & 3) * 32 + lane;
     const int half = warp >> 2;
-    const int64_t gi = i0 + row;
-    const int64_t jc = j0 + half * (kBN / 2);
-    float4 cv[kBN / 8];
+    auto load_c = [&](const Tile& T) {
+        const int64_t gi = T.i0 + row;
+        const int64_t jc = T.j0 + half * (kBN / 2);
 #pragma unroll
-    for (int q = 0; q < kBN / 8; ++q) {
-        const int64_t gj = jc + 4 * q;
-        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (gi < r_hi) {
-            const float* c = A + gi * lda + gj;
-            if (gj + 3 < c_hi) {
-                v = *reinterpret_cast<const float4*>(c);
-            } else {
-                if (gj < c_hi) v.x = c[0];
-                if (gj + 1 < c_hi) v.y = c[1];
-                if (gj + 2 < c_hi) v.z = c[2];
-            }
+        for (int q = 0; q < kBN / 8; ++q) {
+            const int64_t gj = jc + 4 * q;
+            cv[q] = (gi < T.r_hi && gj < T.c_hi) ? load4(A + gi * lda + gj, T.c_hi - gj)
+                                                 : make_float4(0.f, 0.f, 0.f, 0.f);
         }
-        cv[q] = v;
-    }
-    const long long cap = wait_cap(kCopySpin);
-    bool done = false;
-    for (long long i = 0; i < cap && !done; ++i) done = mbar_try_wait(&mbar, 0);
-    if (__syncthreads_or(done ? 0 : 1)) {
-        // the MMAs did not signal in time: report, wait once more (default
-        // cap) for anything still in flight, release the tensor memory
-        if (tid == 0 && info) atomicExch(&info->status, (int)GK_ERR_TIMEOUT);
-        for (long long i = 0; i < kCopySpin && !mbar_try_wait(&mbar, 0); ++i) {
-        }
-    } else {
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t lanes = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(half * (kBN / 2));
+    };
+    auto write_back = [&](const Tile& T, uint32_t buf) {
+        const uint32_t lanes = tmem + ((uint32_t)((warp & 3) * 32) << 16) + buf * kBN + (uint32_t)(half * (kBN / 2));
 #pragma unroll
         for (int c0 = 0; c0 < kBN / 2; c0 += 16) {
             uint32_t r[16];
@@ -269,19 +250,89 @@ __global__ void __launch_bounds__(kThreads, 1) update_kernel(float* __restrict__
                 v.w -= __uint_as_float(r[4 * q4 + 3]);
             }
         }
-        if (gi < r_hi) {
+        const int64_t gi = T.i0 + row;
+        if (gi >= T.r_hi) return;
+        const int64_t jc = T.j0 + half * (kBN / 2);
 #pragma unroll
-            for (int q = 0; q < kBN / 8; ++q) {
-                const int64_t gj = jc + 4 * q;
-                float* c = A + gi * lda + gj;
-                if (gj + 3 < c_hi) {
-                    *reinterpret_cast<float4*>(c) = cv[q];
-                } else {
-                    if (gj < c_hi) c[0] = cv[q].x;
-                    if (gj + 1 < c_hi) c[1] = cv[q].y;
-                    if (gj + 2 < c_hi) c[2] = cv[q].z;
-                }
+        for (int q = 0; q < kBN / 8; ++q) {
+            const int64_t gj = jc + 4 * q;
+            float* c = A + gi * lda + gj;
+            if (gj + 3 < T.c_hi) {
+                *reinterpret_cast<float4*>(c) = cv[q];
+            } else {
+                if (gj < T.c_hi) c[0] = cv[q].x;
+                if (gj + 1 < T.c_hi) c[1] = cv[q].y;
+                if (gj + 2 < T.c_hi) c[2] = cv[q].z;
             }
+        }
+    };
+    // true when the MMAs committed as the it-th arrival have completed
+    auto wait_mma = [&](uint32_t it) {
+        const long long cap = wait_cap(kCopySpin);
+        bool done = false;
+        for (long long i = 0; i < cap && !done; ++i) done = mbar_try_wait(&mbar, it & 1u);
+        return __syncthreads_or(done ? 0 : 1) == 0;
+    };
+
+    Tile cur = tile_of(blockIdx.x, tx, ty, r_lo, r_hi, c_lo, c_hi, diag_bs), prev = cur;
+    load_ab(cur);
+    uint32_t it = 0;
+    bool ok = true;
+    for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x, ++it) {
+        if (it > 0) {
+            if (!wait_mma(it - 1)) {
+                ok = false;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        }
+        store_ab();
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (tid == 0) {
+            const uint32_t idesc = idesc_tf32(kBM, kBN);
+            const uint32_t dst = tmem + (it & 1u) * kBN;
+            const uint32_t ops[3][2] = {{saddr(Ah), saddr(Bh)}, {saddr(Ah), saddr(Bl)}, {saddr(Al), saddr(Bh)}};
+            uint32_t accumulate = 0;
+            for (int pr = 0; pr < 3; ++pr)
+                for (int kk = 0; kk < kp8 / 8; ++kk) {
+                    const uint64_t ad = smem_desc(ops[pr][0] + (uint32_t)kk * 256u, 128u, kSbo);
+                    const uint64_t bd = smem_desc(ops[pr][1] + (uint32_t)kk * 256u, 128u, kSbo);
+                    asm volatile(
+                        "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+                        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(dst),
+                        "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate)
+                        : "memory");
+                    accumulate = 1;
+                }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             saddr(&mbar))
+                         : "memory");
+        }
+        if (it > 0) write_back(prev, (it - 1) & 1u);
+        load_c(cur);
+        prev = cur;
+        const int64_t nt = t + gridDim.x;
+        if (nt < n_tiles) {
+            cur = tile_of(nt, tx, ty, r_lo, r_hi, c_lo, c_hi, diag_bs);
+            load_ab(cur);
+        }
+    }
+    if (ok) {
+        if (wait_mma(it - 1)) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            write_back(prev, (it - 1) & 1u);
+        } else {
+            ok = false;
+        }
+    }
+    if (!ok) {
+        // the MMAs did not signal in time: report, wait once more (default
+        // cap) for the commit still outstanding, then release tensor memory
+        if (tid == 0 && info) atomicExch(&info->status, (int)GK_ERR_TIMEOUT);
+        for (long long i = 0; i < kCopySpin && !mbar_try_wait(&mbar, (it - 1) & 1u); ++i) {
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -312,10 +363,11 @@ gk_status lu_tc_update(float* A, int64_t lda, int64_t k, int kb, int64_t r_lo, i
     int occ = 0;
     gk_status s = cached_occupancy((const void*)lu_tc::update_kernel, lu_tc::kThreads, lu_tc::kSmemBytes, occ);
     if (s != GK_OK) return s;
-    dim3 grid((unsigned)((cols + lu_tc::kBN - 1) / lu_tc::kBN), (unsigned)((rows + lu_tc::kBM - 1) / lu_tc::kBM),
-              nz < 1 ? 1u : nz);
-    lu_tc::update_kernel<<<grid, lu_tc::kThreads, lu_tc::kSmemBytes, st>>>(A, lda, k, kb, r_lo, r_hi, c_lo, c_hi,
-                                                                          diag_bs, info);
+    const int tx = (int)((cols + lu_tc::kBN - 1) / lu_tc::kBN), ty = (int)((rows + lu_tc::kBM - 1) / lu_tc::kBM);
+    const int64_t n_tiles = (int64_t)tx * ty * (nz < 1 ? 1 : nz);
+    const int64_t ctas = min(n_tiles, (int64_t)device_sm_count() * occ);
+    lu_tc::update_kernel<<<(unsigned)ctas, lu_tc::kThreads, lu_tc::kSmemBytes, st>>>(
+        A, lda, k, kb, r_lo, r_hi, c_lo, c_hi, diag_bs, tx, ty, n_tiles, info);
     GK_LAUNCH_CHECK();
     return GK_OK;
 }
