@@ -195,7 +195,7 @@ struct EvalParams {
     double* values;
     int32_t* ids;
     gk_info* info;     // device status word (timeouts), may be NULL
-    int col;           // float-float path: each thread takes two consecutive points of one grid column
+    int col;           // float-float path: each thread takes PPT consecutive points of one grid column
 };
 
 template <typename T> __device__ __forceinline__ T fast_r(T r2);
@@ -546,9 +546,9 @@ __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const 
     };
     if (n_items > 0) issue(0);
     if (n_items > 1) issue(1);
-    // point of slot p within a chunk: strided by the block, or (col) two
+    // point of slot p within a chunk: strided by the block, or (col) PPT
     // consecutive points of one grid column, which share x and y
-    const bool col = PPT == 2 && P.col != 0;
+    const bool col = P.col != 0;
     auto slot = [&](int p) -> int64_t { return col ? (int64_t)PPT * tid + p : tid + (int64_t)p * blockDim.x; };
 
     int64_t item = 0;
@@ -593,11 +593,9 @@ __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const 
                 const int nr = ori ? min(P.rec_ori, P.n_ori - t * P.rec_ori)
                                    : min(P.rec_sp, P.n_sp - (t - P.tiles_ori) * P.rec_sp);
                 bool done = !any_act;
-                if constexpr (PPT == 2) {
-                    if (!done && col && all_exact && all_act) {
-                        ff_tile_col2(rec, ori, nr, X, eps2, acc);
-                        done = true;
-                    }
+                if (!done && col && all_exact && all_act) {
+                    ff_tile_col<PPT>(rec, ori, nr, X, eps2, acc);
+                    done = true;
                 }
                 if (done) {
                 } else if (all_exact && all_act) {
@@ -832,9 +830,9 @@ static gk_status launch_eval(EvalParams& P, cudaStream_t st, int stage_kb = 32) 
 
 template <int PPT>
 static gk_status launch_eval_ff(EvalParams& P, const double* meta, cudaStream_t st, int stage_kb) {
-    // a regular grid with an even number of points per column: each thread's
-    // two points share their column (x, y)
-    P.col = (PPT == 2 && P.kind == 0 && P.dims[2] % 2 == 0) ? 1 : 0;
+    // a regular grid whose columns hold a multiple of PPT points: each
+    // thread's PPT points share their column (x, y)
+    P.col = (P.kind == 0 && P.dims[2] % PPT == 0) ? 1 : 0;
     return launch_chunks(eval_ff_kernel<PPT, false>, eval_ff_kernel<PPT, true>, P, PPT, stage_kb,
                          (int)(16 * sizeof(float)), (int)(8 * sizeof(float)), 1, st, meta);
 }

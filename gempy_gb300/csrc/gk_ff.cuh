@@ -288,12 +288,14 @@ __device__ __forceinline__ void ff_tile(const float* __restrict__ rec, bool orie
     }
 }
 
-// ff_tile for two points of one grid column (equal x and y, exact splits,
-// both slots filled): the x and y terms of r^2 -- their exact squares, the
-// two-sum of their high words and the low-order terms -- are formed once per
-// record and shared; only the z terms are per point.
-__device__ __forceinline__ void ff_tile_col2(const float* __restrict__ rec, bool orientation, int nr,
-                                             const PointFF (&X)[2], float eps2, ffacc (&acc)[2]) {
+// ff_tile for NP points of one grid column (equal x and y, exact splits,
+// every slot filled): the x and y terms of r^2 -- their exact squares, the
+// two-sum of their high words and the low-order terms -- and, for an
+// orientation record, the x and y terms of w . h are formed once per record
+// and shared; only the z terms are per point.
+template <int NP>
+__device__ __forceinline__ void ff_tile_col(const float* __restrict__ rec, bool orientation, int nr,
+                                            const PointFF (&X)[NP], float eps2, ffacc (&acc)[NP]) {
     for (int qr = 0; qr < nr; ++qr) {
         const float* R = rec + (orientation ? 16 : 8) * qr;
         const float4 a0 = reinterpret_cast<const float4*>(R)[0];
@@ -305,34 +307,47 @@ __device__ __forceinline__ void ff_tile_col2(const float* __restrict__ rec, bool
         float lxy = sxy.l + b0.l + b1.l + eps2;
         lxy = __fmaf_rn(dl0, 2.f * dh0 + dl0, lxy);
         lxy = __fmaf_rn(dl1, 2.f * dh1 + dl1, lxy);
-        ff wx = {0.f, 0.f}, wy = {0.f, 0.f}, wz = {0.f, 0.f}, W = {a1.z, a1.w};
         if (orientation) {
             const float4 a2 = reinterpret_cast<const float4*>(R)[2];
-            wx = ff{a1.z, a1.w};
-            wy = ff{a2.x, a2.y};
-            wz = ff{a2.z, a2.w};
-        }
+            const ff wx = {a1.z, a1.w}, wy = {a2.x, a2.y}, wz = {a2.z, a2.w};
+            // w . h with h = x_o - x = -(dh + dl): the x and y products once
+            const ff q0 = two_prod(wx.h, -dh0), q1 = two_prod(wy.h, -dh1);
+            float exy = __fmaf_rn(wx.h, -dl0, __fmaf_rn(wx.l, -dh0, q0.l));
+            exy += __fmaf_rn(wy.h, -dl1, __fmaf_rn(wy.l, -dh1, q1.l));
+            const ff sw = two_sum(q0.h, q1.h);
+            exy += sw.l;
 #pragma unroll
-        for (int p = 0; p < 2; ++p) {
-            const float dh2 = X[p].h[2] - a1.x, dl2 = X[p].l[2] - a1.y;
-            const ff b2 = two_prod(dh2, dh2);
-            const ff s2 = two_sum(sxy.h, b2.h);
-            float low = lxy + s2.l + b2.l;
-            low = __fmaf_rn(dl2, 2.f * dh2 + dl2, low);
-            const ff r2 = fast_two_sum(s2.h, low);
-            if (r2.h >= 1.f) continue;  // beyond the range: C = C'/r = 0
-            if (orientation) {
+            for (int p = 0; p < NP; ++p) {
+                const float dh2 = X[p].h[2] - a1.x, dl2 = X[p].l[2] - a1.y;
+                const ff b2 = two_prod(dh2, dh2);
+                const ff s2 = two_sum(sxy.h, b2.h);
+                float low = lxy + s2.l + b2.l;
+                low = __fmaf_rn(dl2, 2.f * dh2 + dl2, low);
+                const ff r2 = fast_two_sum(s2.h, low);
+                if (r2.h >= 1.f) continue;  // beyond the range: C'/r = 0
                 const ff k = ff_cubic_d1(r2, ff_sqrt_pos(r2));
-                // h = x_o - x = -(dh + dl)
-                const ff wh = ff_dot3(wx, wy, wz, ff{-dh0, -dl0}, ff{-dh1, -dl1}, ff{-dh2, -dl2});
-                ff_acc_fma(acc[p], k, wh);
-            } else {
+                const ff q2 = two_prod(wz.h, -dh2);
+                const float e2 = __fmaf_rn(wz.h, -dl2, __fmaf_rn(wz.l, -dh2, q2.l));
+                const ff sz = two_sum(sw.h, q2.h);
+                ff_acc_fma(acc[p], k, ff{sz.h, exy + sz.l + e2});   // unnormalised, read through exact products
+            }
+        } else {
+            const ff W = {a1.z, a1.w};
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                const float dh2 = X[p].h[2] - a1.x, dl2 = X[p].l[2] - a1.y;
+                const ff b2 = two_prod(dh2, dh2);
+                const ff s2 = two_sum(sxy.h, b2.h);
+                float low = lxy + s2.l + b2.l;
+                low = __fmaf_rn(dl2, 2.f * dh2 + dl2, low);
+                const ff r2 = fast_two_sum(s2.h, low);
+                if (r2.h >= 1.f) continue;  // beyond the range: C = 0
                 ff_acc_fma(acc[p], ff_cubic_C(r2, ff_sqrt_pos(r2)), W);
             }
         }
         if ((qr & 7) == 7) {  // fold the low words back every 8 records
-            ff_acc_norm(acc[0]);
-            ff_acc_norm(acc[1]);
+#pragma unroll
+            for (int p = 0; p < NP; ++p) ff_acc_norm(acc[p]);
         }
     }
 }
