@@ -653,13 +653,16 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchDesc* __rest
         const int nt = tiles_of(s);
         const int to = (d.n_ori + rec_ori - 1) / rec_ori;
         const int nyz = d.dims[1] * d.dims[2];
+        // columns holding a multiple of kPPT points: each thread's points are
+        // consecutive in one column and share x and y (ff_tile_col)
+        const bool col = d.dims[2] % kPPT == 0;
         for (int pass = 0; pass < kPasses; ++pass) {
         PointFF X[kPPT];
         int64_t pid[kPPT];
         double Z[kPPT];
 #pragma unroll
         for (int p = 0; p < kPPT; ++p) {
-            pid[p] = c * kChunkPoints + pass * (256 * kPPT) + tid + p * 256;
+            pid[p] = c * kChunkPoints + pass * (256 * kPPT) + (col ? kPPT * tid + p : tid + p * 256);
             const int64_t qd = pid[p] < d.n_points ? pid[p] : d.n_points - 1;
             const int64_t ix = qd / nyz, rem = qd - ix * nyz;
             const int64_t iy = rem / d.dims[2], iz = rem - iy * d.dims[2];
@@ -668,12 +671,13 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchDesc* __rest
             ff_point(xd, inv_a, q, X[p]);
             Z[p] = 0.0;
         }
-        bool all_exact = true, act[kPPT], any_act = false;
+        bool all_exact = true, act[kPPT], any_act = false, all_act = true;
 #pragma unroll
         for (int p = 0; p < kPPT; ++p) {
             act[p] = pid[p] < d.n_points;
             all_exact = all_exact && (X[p].exact || !act[p]);
             any_act = any_act || act[p];
+            all_act = all_act && act[p];
         }
         for (int t = 0; t < nt; ++t) {
             const int sg = (int)(consumed & 1);
@@ -721,6 +725,10 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchDesc* __rest
             const bool ori = t < to;
             const int nr = ori ? min(rec_ori, d.n_ori - t * rec_ori) : min(rec_sp, d.n_sp - (t - to) * rec_sp);
             if (!any_act) {
+            } else if (col && all_exact && all_act) {
+                ff_tile_col<kPPT>(rec, ori, nr, X, eps2, acc);
+            } else if (all_exact && all_act) {
+                ff_tile<kPPT, true, true>(rec, ori, nr, X, act, eps2, acc);
             } else if (all_exact) {
                 ff_tile<kPPT, true>(rec, ori, nr, X, act, eps2, acc);
             } else {
