@@ -826,15 +826,17 @@ __global__ void __launch_bounds__(256, 2) sgemm_update_kernel(float* __restrict_
 // The tensor-core form of the FP32 trailing update (gk_lu_tc.cu) and the
 // switch between it and sgemm_update_kernel (gk_lu_update_select).
 gk_status lu_tc_update(float* A, int64_t lda, int64_t k, int kb, int64_t r_lo, int64_t r_hi, int64_t c_lo,
-                       int64_t c_hi, int diag_bs, unsigned nz, gk_info* info, cudaStream_t st);
+                       int64_t c_hi, int diag_bs, unsigned nz, gk_info* info, cudaStream_t st, int max_ctas);
 bool lu_update_on_tensor_cores();
 cudaError_t wait_cap_set_lu_tc(long long v);
 
 // C -= L U over rows [r_lo, r_hi) x columns [c_lo, c_hi) (or nz diagonal
 // blocks of diag_bs), on the engine gk_lu_update_select chose.
 static gk_status sgemm_update(float* A, int64_t lda, int64_t k, int kb, int64_t r_lo, int64_t r_hi, int64_t c_lo,
-                              int64_t c_hi, int diag_bs, unsigned nz, gk_info* info, cudaStream_t st) {
-    if (lu_update_on_tensor_cores()) return lu_tc_update(A, lda, k, kb, r_lo, r_hi, c_lo, c_hi, diag_bs, nz, info, st);
+                              int64_t c_hi, int diag_bs, unsigned nz, gk_info* info, cudaStream_t st,
+                              int max_ctas = 0) {
+    if (lu_update_on_tensor_cores())
+        return lu_tc_update(A, lda, k, kb, r_lo, r_hi, c_lo, c_hi, diag_bs, nz, info, st, max_ctas);
     const int64_t rows = diag_bs > 0 ? diag_bs : r_hi - r_lo;
     const int64_t cols = diag_bs > 0 ? diag_bs : c_hi - c_lo;
     if (rows <= 0 || cols <= 0) return GK_OK;
@@ -1235,6 +1237,35 @@ static gk_status lu_factor(int64_t n, T* A, int64_t lda, int32_t* ipiv, void* wo
     return GK_OK;
 }
 
+// The second stream of the unpivoted FP32 LU's look-ahead: per device, the
+// highest priority, created on first use and kept for the process.
+static gk_status lookahead_stream(cudaStream_t& out) {
+    static std::mutex mu;
+    static cudaStream_t tab[64] = {};
+    int dev = 0;
+    GK_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return GK_ERR_CUDA;
+    std::lock_guard<std::mutex> g(mu);
+    if (tab[dev] == nullptr) {
+        int lo = 0, hi = 0;
+        GK_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        GK_CUDA_TRY(cudaStreamCreateWithPriority(&tab[dev], cudaStreamNonBlocking, hi));
+    }
+    out = tab[dev];
+    return GK_OK;
+}
+
+// Systems above this size factor with look-ahead (below it the panels are
+// too short to hide anything).
+constexpr int64_t kLookaheadMinN = 2048;
+
+// Unpivoted blocked LU.  Per panel k: the diagonal block (one CTA),
+// L21 = A21 U11^-1, U12 = L11^-1 A12, then the trailing update.  For FP32
+// systems above kLookaheadMinN the update is split: first the next panel's
+// columns, then the rest; the next diagonal block is factored on a second,
+// higher-priority stream while the rest of the update runs (which then
+// leaves one SM free on the tensor-core engine), so the one-CTA factorization
+// leaves the critical path.
 template <typename T>
 static gk_status lu_factor_nopiv(int64_t n, T* A, int64_t lda, int32_t* ipiv, void* work, size_t wbytes,
                                  gk_info* info, cudaStream_t st) {
@@ -1243,30 +1274,74 @@ static gk_status lu_factor_nopiv(int64_t n, T* A, int64_t lda, int32_t* ipiv, vo
     if (work == nullptr || wbytes < lu_ws_bytes<T>(n)) return GK_ERR_SIZE;
     int sms = device_sm_count();
     if (info) GK_CUDA_TRY(cudaMemsetAsync(info, 0, sizeof(gk_info), st));
-    for (int64_t k = 0; k < n; k += NB) {
-        int kb = (int)min((int64_t)NB, n - k);
-        diag_lu_kernel<T, NB><<<1, 256, 0, st>>>(A, lda, k, kb, ipiv, info);
-        GK_LAUNCH_CHECK();
-        int64_t rest = n - k - kb;
-        if (rest > 0) {
-            trsm_right_kernel<T, NB><<<(unsigned)((rest + kTrsmRows - 1) / kTrsmRows), kTrsmRows * kTrsmLanes, 0, st>>>(
-                A, lda, n, k, kb);
-            GK_LAUNCH_CHECK();
-            trsm_kernel<T, NB><<<(unsigned)((rest + 127) / 128), 128, 0, st>>>(A, lda, n, k, kb);
-            GK_LAUNCH_CHECK();
-            constexpr int BM = sizeof(T) == 8 ? 64 : 128;
-            constexpr int BN = BM;
-            dim3 grid((unsigned)((rest + BN - 1) / BN), (unsigned)((rest + BM - 1) / BM));
-            if (sizeof(T) == 4 && ((k + kb) % 4) == 0 && (lda % 4) == 0 &&
-                ((uintptr_t)A % 16) == 0) {
-                gk_status s = sgemm_update((float*)A, lda, k, kb, k + kb, n, k + kb, n, 0, 1, info, st);
-                if (s != GK_OK) return s;
-            } else {
-                gemm_update_kernel<T, BM, BN, 16><<<grid, 256, 0, st>>>(A, lda, n, k, kb);
-                GK_LAUNCH_CHECK();
-            }
+    const bool fast = sizeof(T) == 4 && (lda % 4) == 0 && ((uintptr_t)A % 16) == 0;
+    const bool lookahead = fast && n > kLookaheadMinN;
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_ready = nullptr, ev_diag = nullptr;
+    if (lookahead) {
+        gk_status s = lookahead_stream(side);
+        if (s != GK_OK) return s;
+        GK_CUDA_TRY(cudaEventCreateWithFlags(&ev_ready, cudaEventDisableTiming));
+        if (cudaEventCreateWithFlags(&ev_diag, cudaEventDisableTiming) != cudaSuccess) {
+            cudaEventDestroy(ev_ready);
+            return GK_ERR_CUDA;
         }
     }
+    gk_status status = GK_OK;
+    bool diag_ready = false;   // the diagonal block of panel k was factored ahead
+    for (int64_t k = 0; k < n && status == GK_OK; k += NB) {
+        int kb = (int)min((int64_t)NB, n - k);
+        if (!diag_ready) {
+            diag_lu_kernel<T, NB><<<1, 256, 0, st>>>(A, lda, k, kb, ipiv, info);
+            gk_launch_counter().fetch_add(1, std::memory_order_relaxed);
+            if (cudaPeekAtLastError() != cudaSuccess) { (void)cudaGetLastError(); status = GK_ERR_CUDA; break; }
+        }
+        diag_ready = false;
+        int64_t rest = n - k - kb;
+        if (rest <= 0) break;
+        trsm_right_kernel<T, NB><<<(unsigned)((rest + kTrsmRows - 1) / kTrsmRows), kTrsmRows * kTrsmLanes, 0, st>>>(
+            A, lda, n, k, kb);
+        trsm_kernel<T, NB><<<(unsigned)((rest + 127) / 128), 128, 0, st>>>(A, lda, n, k, kb);
+        gk_launch_counter().fetch_add(2, std::memory_order_relaxed);
+        if (cudaPeekAtLastError() != cudaSuccess) { (void)cudaGetLastError(); status = GK_ERR_CUDA; break; }
+        constexpr int BM = sizeof(T) == 8 ? 64 : 128;
+        constexpr int BN = BM;
+        if (fast && ((k + kb) % 4) == 0) {
+            const int64_t c0 = k + kb;
+            const int nkb = (int)min((int64_t)NB, rest);
+            if (lookahead && c0 + nkb < n) {
+                // the next panel's columns, then its diagonal block on the side stream
+                status = sgemm_update((float*)A, lda, k, kb, c0, n, c0, c0 + nkb, 0, 1, info, st, 0);
+                if (status != GK_OK) break;
+                if (cudaEventRecord(ev_ready, st) != cudaSuccess || cudaStreamWaitEvent(side, ev_ready, 0) != cudaSuccess) {
+                    status = GK_ERR_CUDA;
+                    break;
+                }
+                diag_lu_kernel<T, NB><<<1, 256, 0, side>>>(A, lda, c0, nkb, ipiv, info);
+                gk_launch_counter().fetch_add(1, std::memory_order_relaxed);
+                if (cudaPeekAtLastError() != cudaSuccess || cudaEventRecord(ev_diag, side) != cudaSuccess) {
+                    (void)cudaGetLastError();
+                    status = GK_ERR_CUDA;
+                    break;
+                }
+                // the rest of the update, one SM left to the side stream
+                status = sgemm_update((float*)A, lda, k, kb, c0, n, c0 + nkb, n, 0, 1, info, st, sms - 1);
+                if (cudaStreamWaitEvent(st, ev_diag, 0) != cudaSuccess && status == GK_OK) status = GK_ERR_CUDA;
+                if (status != GK_OK) break;
+                diag_ready = true;
+            } else {
+                status = sgemm_update((float*)A, lda, k, kb, c0, n, c0, n, 0, 1, info, st, 0);
+            }
+        } else {
+            dim3 grid((unsigned)((rest + BN - 1) / BN), (unsigned)((rest + BM - 1) / BM));
+            gemm_update_kernel<T, BM, BN, 16><<<grid, 256, 0, st>>>(A, lda, n, k, kb);
+            gk_launch_counter().fetch_add(1, std::memory_order_relaxed);
+            if (cudaPeekAtLastError() != cudaSuccess) { (void)cudaGetLastError(); status = GK_ERR_CUDA; }
+        }
+    }
+    if (ev_ready) cudaEventDestroy(ev_ready);
+    if (ev_diag) cudaEventDestroy(ev_diag);
+    if (status != GK_OK) return status;
     int32_t* perm = (int32_t*)((char*)work + panel_ws_bytes<T, NB>(sms));
     size_t psmem = n <= kPermSmem ? (size_t)n * sizeof(int32_t) : 0;
     GK_CUDA_TRY(cudaFuncSetAttribute(perm_from_ipiv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPermSmem * 4));

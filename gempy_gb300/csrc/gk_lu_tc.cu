@@ -351,11 +351,12 @@ cudaError_t wait_cap_set_lu_tc(long long v) { return set_wait_cap_here(v); }
 // Whether the FP32 trailing updates go to the tensor cores.
 bool lu_update_on_tensor_cores() { return lu_tc::g_engine.load(std::memory_order_relaxed) == GK_LU_UPDATE_TC; }
 
-// The FP32 trailing update on the tensor cores (grid: column tiles, row
-// tiles, nz diagonal blocks).  A, lda and k + kb are multiples of 4 floats
-// (16-byte rows), like the SIMT kernel's fast path.
+// The FP32 trailing update on the tensor cores: one persistent CTA per SM
+// (at most max_ctas when > 0) over the column tiles, row tiles and nz
+// diagonal blocks.  A, lda and k + kb are multiples of 4 floats (16-byte
+// rows), like the SIMT kernel's fast path.
 gk_status lu_tc_update(float* A, int64_t lda, int64_t k, int kb, int64_t r_lo, int64_t r_hi, int64_t c_lo,
-                       int64_t c_hi, int diag_bs, unsigned nz, gk_info* info, cudaStream_t st) {
+                       int64_t c_hi, int diag_bs, unsigned nz, gk_info* info, cudaStream_t st, int max_ctas) {
     if (kb < 1 || kb > lu_tc::kKP) return GK_ERR_ARG;
     const int64_t rows = diag_bs > 0 ? diag_bs : r_hi - r_lo;
     const int64_t cols = diag_bs > 0 ? diag_bs : c_hi - c_lo;
@@ -365,7 +366,8 @@ gk_status lu_tc_update(float* A, int64_t lda, int64_t k, int kb, int64_t r_lo, i
     if (s != GK_OK) return s;
     const int tx = (int)((cols + lu_tc::kBN - 1) / lu_tc::kBN), ty = (int)((rows + lu_tc::kBM - 1) / lu_tc::kBM);
     const int64_t n_tiles = (int64_t)tx * ty * (nz < 1 ? 1 : nz);
-    const int64_t ctas = min(n_tiles, (int64_t)device_sm_count() * occ);
+    int64_t ctas = min(n_tiles, (int64_t)device_sm_count() * occ);
+    if (max_ctas > 0) ctas = min(ctas, (int64_t)max_ctas);
     lu_tc::update_kernel<<<(unsigned)ctas, lu_tc::kThreads, lu_tc::kSmemBytes, st>>>(
         A, lda, k, kb, r_lo, r_hi, c_lo, c_hi, diag_bs, tx, ty, n_tiles, info);
     GK_LAUNCH_CHECK();

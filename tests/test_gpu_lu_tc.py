@@ -92,3 +92,26 @@ def test_mixed_solve_on_tensor_core_preconditioner(case):
         assert np.linalg.norm(br - Kr @ w) <= 1e-11 * np.linalg.norm(br)
         out[e] = inf["iterations"]
     assert out[_engines()[0]] <= out[_engines()[1]] + 2
+
+
+def test_mixed_solve_with_lookahead_matches_lapack():
+    """A system above the look-ahead threshold (N = 3495: the next panel's
+    diagonal block is factored on a second stream while the rest of the
+    update runs): the mixed solve reaches the FP64 residual on both engines
+    and its weights match LAPACK's solution."""
+    from gempy_gb300 import kernels as K
+    from gempy_gb300 import synthetic
+    from tests._models import oracle_series_list
+    m = synthetic.precision(n_points=2000, n_orient=500, resolution=(8, 8, 8))
+    (s,) = oracle_series_list(m)
+    Kr, br = kriging.build_system(s)
+    assert Kr.shape[0] > 2048
+    w_ref = kriging.solve(Kr, br)
+    for e in _engines():
+        with K.lu_update_engine(e):
+            w, info = K.solve_mixed(_dev_series(s), tol=1e-12)
+        inf = K.read_info(info)
+        w = w.cpu().numpy()
+        assert inf["status"] == 0 and inf["residual"] <= 1e-11, inf
+        assert np.linalg.norm(br - Kr @ w) <= 1e-11 * np.linalg.norm(br)
+        assert np.abs(w - w_ref).max() <= 1e-6 * np.abs(w_ref).max()
