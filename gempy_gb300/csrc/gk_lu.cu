@@ -336,7 +336,8 @@ __global__ void __launch_bounds__(256) panel_cluster_kernel(T* __restrict__ A, i
 // ----------------------------------------------------------------------------
 template <typename T, int NB>
 __global__ void __launch_bounds__(256) diag_lu_kernel(T* __restrict__ A, int64_t lda, int64_t k, int kb,
-                                                      int32_t* __restrict__ ipiv, gk_info* info) {
+                                                      int32_t* __restrict__ ipiv, gk_info* info,
+                                                      T* __restrict__ uinv = nullptr) {
     __shared__ T S[NB][NB + 1];
     const int tid = threadIdx.x;
     for (int idx = tid; idx < NB * NB; idx += blockDim.x) {
@@ -374,6 +375,57 @@ __global__ void __launch_bounds__(256) diag_lu_kernel(T* __restrict__ A, int64_t
         int r = idx / NB, c = idx % NB;
         if (r < kb && c < kb) A[(k + r) * lda + k + c] = S[r][c];
     }
+    // U11^-1 (row-major NB x NB, zero below the diagonal) for the
+    // right-looking triangular solve L21 = A21 U11^-1: thread c back-
+    // substitutes column c with the column held in registers (rows below c
+    // come out zero); only for full panels that factored without a bad pivot
+    if (uinv == nullptr || kb != NB || steps != kb) return;
+    if (tid < NB) {
+        const int c = tid;
+        T x[NB];
+#pragma unroll
+        for (int i = NB - 1; i >= 0; --i) {
+            T s = (i == c) ? (T)1 : (T)0;
+#pragma unroll
+            for (int j = i + 1; j < NB; ++j) s -= S[i][j] * x[j];
+            x[i] = s / S[i][i];
+        }
+#pragma unroll
+        for (int i = 0; i < NB; ++i) uinv[i * NB + c] = x[i];
+    }
+}
+
+// L21 = A21 U11^-1 with the explicit inverse from diag_lu_kernel: 64 rows per
+// CTA, four threads per row, 16 output columns each (upper-triangular
+// inverse: column c sums over rows j <= c).  A full panel (kb = NB) only.
+template <typename T, int NB>
+__global__ void __launch_bounds__(256) trsm_right_inv_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k,
+                                                             const T* __restrict__ uinv) {
+    __shared__ T U[NB][NB + 1];
+    __shared__ T X[64][NB + 1];
+    const int tid = threadIdx.x;
+    for (int idx = tid; idx < NB * NB; idx += 256) U[idx / NB][idx % NB] = uinv[idx];
+    const int64_t row0 = k + NB + (int64_t)blockIdx.x * 64;
+    for (int idx = tid; idx < 64 * NB; idx += 256) {
+        const int r = idx / NB, c = idx % NB;
+        const int64_t gr = row0 + r;
+        X[r][c] = gr < n ? A[gr * lda + k + c] : (T)0;
+    }
+    __syncthreads();
+    const int r = tid >> 2, c0 = (tid & 3) * (NB / 4);
+    const int64_t gr = row0 + r;
+    if (gr >= n) return;
+    T out[NB / 4];
+#pragma unroll
+    for (int q = 0; q < NB / 4; ++q) out[q] = (T)0;
+    for (int j = 0; j < c0 + NB / 4; ++j) {
+        const T xj = X[r][j];
+#pragma unroll
+        for (int q = 0; q < NB / 4; ++q)
+            if (j <= c0 + q) out[q] += xj * U[j][c0 + q];
+    }
+#pragma unroll
+    for (int q = 0; q < NB / 4; ++q) A[gr * lda + k + c0 + q] = out[q];
 }
 
 // L21 = A21 U11^-1: rows r >= k + kb, 64 rows per CTA staged in shared memory.
@@ -1259,8 +1311,10 @@ static gk_status lookahead_stream(cudaStream_t& out) {
 // too short to hide anything).
 constexpr int64_t kLookaheadMinN = 2048;
 
-// Unpivoted blocked LU.  Per panel k: the diagonal block (one CTA),
-// L21 = A21 U11^-1, U12 = L11^-1 A12, then the trailing update.  For FP32
+// Unpivoted blocked LU.  Per panel k: the diagonal block (one CTA; for FP32
+// full panels it also writes U11^-1), L21 = A21 U11^-1 (a product with that
+// inverse for FP32 full panels, else a row-parallel triangular solve),
+// U12 = L11^-1 A12, then the trailing update.  For FP32
 // systems above kLookaheadMinN the update is split: first the next panel's
 // columns, then the rest; the next diagonal block is factored on a second,
 // higher-priority stream while the rest of the update runs (which then
@@ -1276,6 +1330,9 @@ static gk_status lu_factor_nopiv(int64_t n, T* A, int64_t lda, int32_t* ipiv, vo
     if (info) GK_CUDA_TRY(cudaMemsetAsync(info, 0, sizeof(gk_info), st));
     const bool fast = sizeof(T) == 4 && (lda % 4) == 0 && ((uintptr_t)A % 16) == 0;
     const bool lookahead = fast && n > kLookaheadMinN;
+    // U11^-1 of the current panel; the inverse blocks of the solves (written
+    // after the factorization) are free until then
+    T* uinv = lu_ws_dinv<T>(work, n, 0);
     cudaStream_t side = nullptr;
     cudaEvent_t ev_ready = nullptr, ev_diag = nullptr;
     if (lookahead) {
@@ -1292,15 +1349,19 @@ static gk_status lu_factor_nopiv(int64_t n, T* A, int64_t lda, int32_t* ipiv, vo
     for (int64_t k = 0; k < n && status == GK_OK; k += NB) {
         int kb = (int)min((int64_t)NB, n - k);
         if (!diag_ready) {
-            diag_lu_kernel<T, NB><<<1, 256, 0, st>>>(A, lda, k, kb, ipiv, info);
+            diag_lu_kernel<T, NB><<<1, 256, 0, st>>>(A, lda, k, kb, ipiv, info, fast ? uinv : nullptr);
             gk_launch_counter().fetch_add(1, std::memory_order_relaxed);
             if (cudaPeekAtLastError() != cudaSuccess) { (void)cudaGetLastError(); status = GK_ERR_CUDA; break; }
         }
         diag_ready = false;
         int64_t rest = n - k - kb;
         if (rest <= 0) break;
-        trsm_right_kernel<T, NB><<<(unsigned)((rest + kTrsmRows - 1) / kTrsmRows), kTrsmRows * kTrsmLanes, 0, st>>>(
-            A, lda, n, k, kb);
+        if (fast && kb == NB) {
+            trsm_right_inv_kernel<T, NB><<<(unsigned)((rest + 63) / 64), 256, 0, st>>>(A, lda, n, k, uinv);
+        } else {
+            trsm_right_kernel<T, NB><<<(unsigned)((rest + kTrsmRows - 1) / kTrsmRows), kTrsmRows * kTrsmLanes, 0,
+                                       st>>>(A, lda, n, k, kb);
+        }
         trsm_kernel<T, NB><<<(unsigned)((rest + 127) / 128), 128, 0, st>>>(A, lda, n, k, kb);
         gk_launch_counter().fetch_add(2, std::memory_order_relaxed);
         if (cudaPeekAtLastError() != cudaSuccess) { (void)cudaGetLastError(); status = GK_ERR_CUDA; break; }
@@ -1317,7 +1378,7 @@ static gk_status lu_factor_nopiv(int64_t n, T* A, int64_t lda, int32_t* ipiv, vo
                     status = GK_ERR_CUDA;
                     break;
                 }
-                diag_lu_kernel<T, NB><<<1, 256, 0, side>>>(A, lda, c0, nkb, ipiv, info);
+                diag_lu_kernel<T, NB><<<1, 256, 0, side>>>(A, lda, c0, nkb, ipiv, info, uinv);
                 gk_launch_counter().fetch_add(1, std::memory_order_relaxed);
                 if (cudaPeekAtLastError() != cudaSuccess || cudaEventRecord(ev_diag, side) != cudaSuccess) {
                     (void)cudaGetLastError();
