@@ -22,8 +22,9 @@ GK_TIE_TOL = 1e-9
 GK_NOALLOC_MAX_N = 1024
 GK_LU_UPDATE_SIMT, GK_LU_UPDATE_TC = 0, 1
 GK_CTA_MAX_N = 4096
-GK_TUNE_EVAL_FF, GK_TUNE_EVAL_F32, GK_TUNE_BATCH_EVAL = 0, 1, 2
-TUNABLES = {"eval_ff": GK_TUNE_EVAL_FF, "eval_f32": GK_TUNE_EVAL_F32, "batch_eval": GK_TUNE_BATCH_EVAL}
+GK_TUNE_EVAL_FF, GK_TUNE_EVAL_F32, GK_TUNE_BATCH_EVAL, GK_TUNE_EVAL_FF_LIST = 0, 1, 2, 3
+TUNABLES = {"eval_ff": GK_TUNE_EVAL_FF, "eval_f32": GK_TUNE_EVAL_F32, "batch_eval": GK_TUNE_BATCH_EVAL,
+            "eval_ff_list": GK_TUNE_EVAL_FF_LIST}
 
 c_int32_p = ctypes.POINTER(ctypes.c_int32)
 c_double_p = ctypes.POINTER(ctypes.c_double)

@@ -1,7 +1,7 @@
 """Autotuner for the evaluation kernels' tile shapes.
 
-Every kernel family in ``gk_tunable`` (float-float field, FP32 field, batched
-field) has ``gk_tune_variants()`` tile shapes (grid points per thread x bytes
+Every kernel family in ``gk_tunable`` (float-float field on grids and on
+point lists, FP32 field, batched field) has ``gk_tune_variants()`` tile shapes (grid points per thread x bytes
 per shared-memory record stage).  ``tune()`` times every variant with CUDA
 events on a representative workload on the current GPU, keeps the fastest,
 and writes ``gempy_gb300/tuning/<gpu>.json``; ``apply_saved()`` loads that
@@ -95,6 +95,32 @@ def _eval_workload(prec, grid=96):
     return lambda: K.evaluate(ds, model, pts, prec, out=out)
 
 
+def _list_workload(n_points=300000, seed=0):
+    """The float-float field of the octree workload's first series at a
+    random point list (octree levels and custom grids are point lists)."""
+    from . import kernels as K
+    from . import synthetic
+    m = synthetic.folded_series(octree_levels=7)
+    ii, dd, ko = m.interpolation_input, m.data_descriptor, m.options.kernel_options
+    ss = dd.stack_structure
+    n_p, n_o = int(ss.number_of_points_per_stack[0]), int(ss.number_of_orientations_per_stack[0])
+    n_s = int(ss.number_of_surfaces_per_stack[0])
+    ds = K.DeviceSeries(ii.orientations.dip_positions[:n_o], ii.orientations.dip_gradients[:n_o],
+                        ii.orientations.nugget_effect_grad[:n_o], ii.surface_points.sp_coords[:n_p],
+                        ii.surface_points.nugget_effect_scalar[:n_p],
+                        dd.tensors_structure.number_of_points_per_surface[:n_s],
+                        range=ko.range, c_o=ko.c_o, uni_degree=ko.uni_degree)
+    w, _ = K.solve_mixed(ds, tol=1e-11)
+    model = K.prepare(ds, w)
+    og = ii.grid.octree_grid
+    ext = np.asarray(og.orthogonal_extent, dtype=np.float64)
+    rng = np.random.default_rng(seed)
+    xyz = ext[0::2] + rng.random((n_points, 3)) * (ext[1::2] - ext[0::2])
+    pts = K.Points(xyz=torch.as_tensor(xyz, device="cuda"))
+    out = {"field": torch.empty(n_points, dtype=torch.float64, device="cuda")}
+    return lambda: K.evaluate(ds, model, pts, K.GK_FF, out=out)
+
+
 def _batch_workload(n=48, grid=32):
     from . import synthetic
     from .batch import BatchRunner
@@ -102,7 +128,7 @@ def _batch_workload(n=48, grid=32):
     return br.run
 
 
-def tune(families=("eval_ff", "eval_f32", "batch_eval"), persist=True, reps=3):
+def tune(families=("eval_ff", "eval_f32", "batch_eval", "eval_ff_list"), persist=True, reps=3):
     """Time every variant of each family; install and (optionally) save the fastest."""
     from . import kernels as K
     lib = _lib.load()
@@ -115,6 +141,8 @@ def tune(families=("eval_ff", "eval_f32", "batch_eval"), persist=True, reps=3):
             fn = _eval_workload(K.GK_FF)
         elif fam == "eval_f32":
             fn = _eval_workload(K.GK_F32)
+        elif fam == "eval_ff_list":
+            fn = _list_workload()
         else:
             fn = _batch_workload()
         times = {}

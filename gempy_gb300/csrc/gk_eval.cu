@@ -904,7 +904,7 @@ static gk_status eval_impl(const gk_system* s, const void* model, const gk_point
         if (grad != nullptr || s->kernel != GK_KERNEL_CUBIC) return GK_ERR_ARG;
         P.ori = m + L.ffori;
         P.sp = m + L.ffsp;
-        const TuneVariant v = tune_variant(GK_TUNE_EVAL_FF);
+        const TuneVariant v = tune_variant(P.kind == 0 ? GK_TUNE_EVAL_FF : GK_TUNE_EVAL_FF_LIST);
         return v.ppt == 2 ? launch_eval_ff<2>(P, (const double*)(m + L.ffmeta), cs, v.stage_kb)
                           : launch_eval_ff<4>(P, (const double*)(m + L.ffmeta), cs, v.stage_kb);
     }

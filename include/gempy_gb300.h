@@ -571,7 +571,8 @@ typedef enum gk_tunable {
     GK_TUNE_EVAL_FF = 0,     /* gk_eval, GK_FF                  */
     GK_TUNE_EVAL_F32 = 1,    /* gk_eval, GK_F32 without gradient */
     GK_TUNE_BATCH_EVAL = 2,  /* gk_batch_run evaluation          */
-    GK_TUNE_COUNT = 3
+    GK_TUNE_EVAL_FF_LIST = 3, /* gk_eval, GK_FF on point lists (octree levels, custom points) */
+    GK_TUNE_COUNT = 4
 } gk_tunable;
 
 int32_t gk_tune_variants(void);

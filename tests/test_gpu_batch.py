@@ -109,7 +109,7 @@ def test_every_tile_variant_gives_the_same_field():
     zmax = float(f64.abs().max())
     alpha = kriging.point_coefficients(s, w)
     cancel = s.c_o * s.gi_res * (np.abs(alpha).sum() + np.abs(w[:3 * s.n_o]).sum() * 14 / s.range) / zmax
-    saved = {t: lib.gk_tune_get(t) for t in range(3)}
+    saved = {t: lib.gk_tune_get(t) for t in _lib.TUNABLES.values()}
     try:
         for prec, fam in ((K.GK_FF, _lib.GK_TUNE_EVAL_FF), (K.GK_F32, _lib.GK_TUNE_EVAL_F32)):
             ref = None
