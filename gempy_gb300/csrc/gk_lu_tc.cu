@@ -331,7 +331,7 @@ __global__ void __launch_bounds__(kThreads, 1) update_kernel(float* __restrict__
     if (!ok) {
         // the MMAs did not signal in time: report, wait once more (default
         // cap) for the commit still outstanding, then release tensor memory
-        if (tid == 0 && info) atomicExch(&info->status, (int)GK_ERR_TIMEOUT);
+        if (tid == 0) report(info, GK_ERR_TIMEOUT, (int)blockIdx.x);
         for (long long i = 0; i < kCopySpin && !mbar_try_wait(&mbar, (it - 1) & 1u); ++i) {
         }
     }

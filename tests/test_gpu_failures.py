@@ -172,3 +172,30 @@ def test_compute_model_reports_the_learned_fallback():
     np.testing.assert_allclose(sol.root_output.outputs[0].weights, ref.root_output.outputs[0].weights,
                                rtol=0, atol=1e-12)
     np.testing.assert_array_equal(sol.raw_arrays.custom, np.array(g["expected_ids"], float))
+
+
+def test_tensor_core_update_wait_runs_out_and_reports_timeout(wait_limit):
+    """The FP32 LU's tensor-core trailing update gives up on its MMA-completion
+    wait (cap 0): GK_ERR_TIMEOUT in the status word, the kernel still waits
+    (default cap) for its MMAs in flight and frees its tensor memory, and the
+    next factorization with the default caps is correct."""
+    from gempy_gb300 import _lib
+    from gempy_gb300 import kernels as K
+    n = 1000
+    rng = np.random.default_rng(11)
+    A = rng.normal(size=(n, n)) + 4.0 * n ** 0.5 * np.eye(n)
+    ld = K.leading_dim(n, K.GK_F32)
+    At = torch.zeros((n, ld), dtype=torch.float32, device="cuda")
+    At[:, :n] = torch.as_tensor(A, dtype=torch.float32)
+    with K.lu_update_engine(_lib.GK_LU_UPDATE_TC):
+        wait_limit(0)
+        f = K.lu_factor(At)
+        torch.cuda.synchronize()
+        inf = K.read_info(f.info)
+        assert inf["status"] == GK_ERR_TIMEOUT and inf["where"] >= 0, inf
+        wait_limit(None)
+        f = K.lu_factor(At)
+        b = rng.normal(size=n)
+        x = K.lu_solve(f, torch.as_tensor(b, dtype=torch.float32, device="cuda")).double().cpu().numpy()
+    assert K.read_info(f.info)["status"] == 0
+    assert np.abs(b - A @ x).max() / (np.abs(A).max() * np.abs(x).max() * n) < 1e-6
