@@ -135,6 +135,9 @@ SIGNATURES = [
     ("gk_lu_solve", ctypes.c_int, [ctypes.c_int, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
                                    ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
                                    ctypes.c_void_p, ctypes.c_void_p]),
+    ("gk_build_tables_bytes", ctypes.c_size_t, [ctypes.POINTER(GkSystem)]),
+    ("gk_build_tables", ctypes.c_int, [ctypes.POINTER(GkSystem), ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                       ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     ("gk_lu_update_select", ctypes.c_int, [ctypes.c_int32]),
     ("gk_lu_update_engine", ctypes.c_int32, []),
     ("gk_gemv", ctypes.c_int, [ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,

@@ -176,14 +176,27 @@ def leading_dim(n, prec):
     return (n + align - 1) // align * align
 
 
-def build(series: DeviceSeries, prec=GK_F64):
+# largest covariance-table workspace of the FP64 build (gk_build_tables)
+BUILD_TABLES_MAX_BYTES = 16 << 30
+
+
+def build(series: DeviceSeries, prec=GK_F64, tables=True):
+    """K (N x ld) and rhs.  FP64 builds use the covariance tables
+    (gk_build_tables) when their workspace is at most BUILD_TABLES_MAX_BYTES;
+    ``tables=False`` forces the direct build (gk_build)."""
     lib = _lib.load()
     N = series.N
     ld = leading_dim(N, prec)
     dt = torch.float64 if prec == GK_F64 else torch.float32
     K = torch.empty((N, ld), dtype=dt, device=series.device)
     b = torch.empty(N, dtype=dt, device=series.device)
-    check("gk_build", lib.gk_build(ctypes.byref(series.sys), prec, _ptr(K), ld, _ptr(b), _stream()))
+    wb = lib.gk_build_tables_bytes(ctypes.byref(series.sys)) if (tables and prec == GK_F64) else 0
+    if 0 < wb <= BUILD_TABLES_MAX_BYTES:
+        work = torch.empty(wb, dtype=torch.uint8, device=series.device)
+        check("gk_build_tables", lib.gk_build_tables(ctypes.byref(series.sys), _ptr(K), ld, _ptr(b), _ptr(work), wb,
+                                                     _stream()))
+    else:
+        check("gk_build", lib.gk_build(ctypes.byref(series.sys), prec, _ptr(K), ld, _ptr(b), _stream()))
     return K, b
 
 

@@ -151,6 +151,18 @@ int64_t gk_system_size(const gk_system* sys /* HOST struct */);
 gk_status gk_build(const gk_system* sys, gk_prec prec, void* K, int64_t ldk,
                    void* rhs, gk_stream stream);
 
+/* The FP64 build from covariance tables: C over every pair of surface
+ * points and C'/r (x_o - x_p) over every orientation-point pair are formed
+ * once in ``work`` (gk_build_tables_bytes), then every interface entry is
+ * assembled from them with the operations of gk_build -- the same matrix
+ * (to rounding) with about a quarter of the covariance evaluations.  The
+ * workspace is n_sp^2 + 3 n_ori n_sp doubles (16-byte aligned).  Same
+ * reference call site as gk_build. */
+size_t gk_build_tables_bytes(const gk_system* sys /* HOST struct */);
+gk_status gk_build_tables(const gk_system* sys, double* K, int64_t ldk,
+                          double* rhs, void* work, size_t work_bytes,
+                          gk_stream stream);
+
 /* ---------------- dense solve (engine ``kernel_solver``, approved JSON :136) */
 
 /* Workspace for gk_lu_factor (device bytes). */

@@ -70,6 +70,22 @@ def test_build_f64_matches_oracle(case):
     np.testing.assert_array_equal(bg.cpu().numpy(), br)
 
 
+@pytest.mark.parametrize("case", list(SERIES_CASES))
+def test_build_tables_match_direct_build(case):
+    """The table-driven FP64 build (gk_build_tables, the default) and the
+    direct build (gk_build) give the same matrix to rounding: the interface
+    entries come from the same covariances, formed once."""
+    from gempy_gb300 import kernels as K
+    s = SERIES_CASES[case]()
+    ds = _dev_series(s)
+    Kt, bt = K.build(ds, K.GK_F64, tables=True)
+    Kd, bd = K.build(ds, K.GK_F64, tables=False)
+    N = ds.N
+    a, b = Kt[:, :N].cpu().numpy(), Kd[:, :N].cpu().numpy()
+    assert np.abs(a - b).max() <= 1e-14 * np.abs(b).max()
+    np.testing.assert_array_equal(bt.cpu().numpy(), bd.cpu().numpy())
+
+
 def test_build_f32_matches_oracle():
     from gempy_gb300 import kernels as K
     s = _anticline()
