@@ -385,7 +385,9 @@ def main():
     kern = {
         "build_f64": {"ms": t_build, "bytes": N * N * 8, "achieved_GBps": N * N * 8 / (t_build * 1e-3) / 1e9,
                       "hbm_peak_GBps": pk0.get("hbm_gbs"), "flops_per_entry": F_K,
-                      "note": "DFMA-bound: ~4 FP64 kernel evaluations per interface-interface entry"},
+                      "note": "table-driven (gk_build_tables): covariances of point pairs, orientation-point pairs "
+                              "and orientation pairs formed once (FP64, DFMA-bound), entries assembled from "
+                              "them; the tables and the gathers, not the K write, set the time"},
         "lu_f32_partial_pivoting": {"ms": t_lu32, "TFLOPs": 2 / 3 * N ** 3 / (t_lu32 * 1e-3) / 1e12},
         "lu_f64_partial_pivoting": {"ms": t_lu64, "TFLOPs": 2 / 3 * N ** 3 / (t_lu64 * 1e-3) / 1e12,
                                     "note": "GB300 FP64 is ~1.2 TFLOP/s; the trailing GEMM runs at that rate"},

@@ -55,11 +55,13 @@ __global__ void __launch_bounds__(256) build_kernel(BuildParams P, T* K, int64_t
 // interface-interface entry is a four-term difference over the rest and
 // reference points of two rows, and the gradient-interface entry a difference
 // over the rest and reference points of one row, while the reference points
-// are shared by every row of a surface.  Two tables hold each distinct value
-// once -- C over every pair of surface points (n_sp x n_sp) and
-// C'/r (x_o - x_p)_u over every orientation-point pair (n_ori x n_sp x 3) --
-// and the entries are formed from them with the same operations in the same
-// order as entry_at, so K is the same matrix.
+// are shared by every row of a surface; the nine gradient-gradient entries
+// of an orientation pair share one distance and two covariances.  Three
+// tables hold each distinct value once -- C over every pair of surface points
+// (n_sp x n_sp), C'/r (x_o - x_p)_u over every orientation-point pair
+// (n_ori x n_sp x 3), and h, C'/r - C'', r^2 + 1e-5 and C'/r over every
+// orientation pair (n_ori x n_ori x 6) -- and the entries are formed from them
+// with the operations of entry_at, so K is the same matrix to rounding.
 // ---------------------------------------------------------------------------
 template <typename T>
 __global__ void __launch_bounds__(256) point_cov_kernel(BuildParams P, T* __restrict__ Pc) {
@@ -93,9 +95,33 @@ __global__ void __launch_bounds__(256) ori_point_kernel(BuildParams P, T* __rest
     for (int u = 0; u < 3; ++u) Q[3 * t + u] = k1 * h[u];
 }
 
+// per orientation pair (o, q): h = x_o - x_q, C'/r - C'', r^2 + 1e-5 and C'/r
+template <typename T>
+__global__ void __launch_bounds__(256) ori_pair_kernel(BuildParams P, T* __restrict__ G) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)P.n_ori * P.n_ori) return;
+    const int64_t o = t / P.n_ori, q = t - o * P.n_ori;
+    const Cov<T> cv = Cov<T>::make(P.kernel, P.range);
+    T x[3], y[3], h[3];
+    for (int c = 0; c < 3; ++c) {
+        x[c] = (T)P.dip_positions[3 * o + c];
+        y[c] = (T)P.dip_positions[3 * q + c];
+    }
+    const T r = dist(x, y, h);
+    const T k1 = cv.d1_r(r), k2 = cv.d2(r);
+    T* g = G + 6 * t;
+    g[0] = h[0];
+    g[1] = h[1];
+    g[2] = h[2];
+    g[3] = k1 - k2;
+    g[4] = r * r + (T)kGradEps;
+    g[5] = k1;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) build_table_kernel(BuildParams P, const T* __restrict__ Pc,
-                                                          const T* __restrict__ Q, T* K, int64_t ldk, T* rhs) {
+                                                          const T* __restrict__ Q, const T* __restrict__ G, T* K,
+                                                          int64_t ldk, T* rhs) {
     __shared__ Item rows[32], cols[32];
     const int64_t r0 = (int64_t)blockIdx.y * 32, c0 = (int64_t)blockIdx.x * 32;
     const int tid = threadIdx.y * 32 + threadIdx.x;
@@ -115,7 +141,13 @@ __global__ void __launch_bounds__(256) build_table_kernel(BuildParams P, const T
         const Item& A = rows[rl];
         const Item& B = cols[threadIdx.x];
         T v;
-        if (A.type == 1 && B.type == 1) {
+        if (A.type == 0 && B.type == 0) {
+            const T* g = G + 6 * ((int64_t)A.idx * P.n_ori + B.idx);
+            v = g[A.comp] * g[B.comp] * g[3] / g[4];
+            if (A.comp == B.comp) v -= g[5];
+            v *= c_o;
+            if (i == j) v += (T)A.nug;
+        } else if (A.type == 1 && B.type == 1) {
             const int64_t n = P.n_sp;
             v = Pc[A.rest * n + B.rest] - Pc[A.rest * n + B.ref] - Pc[A.ref * n + B.rest] + Pc[A.ref * n + B.ref];
             v *= (T)P.i_res * c_o;
@@ -143,10 +175,11 @@ __global__ void __launch_bounds__(256) build_table_kernel(BuildParams P, const T
     }
 }
 
-static size_t table_bytes(const gk_system* s, size_t& q_off) {
+static size_t table_bytes(const gk_system* s, size_t& q_off, size_t& g_off) {
     const size_t pc = (size_t)s->n_sp * s->n_sp * sizeof(double);
     q_off = (pc + 255) & ~(size_t)255;
-    return q_off + (size_t)s->n_ori * s->n_sp * 3 * sizeof(double);
+    g_off = (q_off + (size_t)s->n_ori * s->n_sp * 3 * sizeof(double) + 255) & ~(size_t)255;
+    return g_off + (size_t)s->n_ori * s->n_ori * 6 * sizeof(double);
 }
 
 }  // namespace gk
@@ -196,8 +229,8 @@ extern "C" gk_status gk_build(const gk_system* s, gk_prec prec, void* K, int64_t
 
 extern "C" size_t gk_build_tables_bytes(const gk_system* s) {
     if (check_system(s) != GK_OK) return 0;
-    size_t q_off = 0;
-    return table_bytes(s, q_off);
+    size_t q_off = 0, g_off = 0;
+    return table_bytes(s, q_off, g_off);
 }
 
 extern "C" gk_status gk_build_tables(const gk_system* s, double* K, int64_t ldk, double* rhs, void* work,
@@ -207,13 +240,19 @@ extern "C" gk_status gk_build_tables(const gk_system* s, double* K, int64_t ldk,
     const int64_t N = gk_system_size(s);
     if (K == nullptr || ldk < N) return GK_ERR_ARG;
     if (N > (int64_t)1 << 20) return GK_ERR_SIZE;
-    size_t q_off = 0;
-    const size_t need = table_bytes(s, q_off);
+    size_t q_off = 0, g_off = 0;
+    const size_t need = table_bytes(s, q_off, g_off);
     if (work == nullptr || work_bytes < need || ((uintptr_t)work % 16) != 0) return GK_ERR_SIZE;
     const BuildParams P = build_params(s);
     cudaStream_t st_ = (cudaStream_t)stream;
     double* Pc = (double*)work;
     double* Q = (double*)((char*)work + q_off);
+    double* G = (double*)((char*)work + g_off);
+    const int64_t ng = (int64_t)s->n_ori * s->n_ori;
+    if (ng > 0) {
+        ori_pair_kernel<double><<<(unsigned)((ng + 255) / 256), 256, 0, st_>>>(P, G);
+        GK_LAUNCH_CHECK();
+    }
     if (s->n_sp > 0) {
         dim3 b2(32, 8), g2((unsigned)((s->n_sp + 31) / 32), (unsigned)((s->n_sp + 31) / 32));
         point_cov_kernel<double><<<g2, b2, 0, st_>>>(P, Pc);
@@ -225,7 +264,7 @@ extern "C" gk_status gk_build_tables(const gk_system* s, double* K, int64_t ldk,
         }
     }
     dim3 block(32, 8), grid((unsigned)((N + 31) / 32), (unsigned)((N + 31) / 32));
-    build_table_kernel<double><<<grid, block, 0, st_>>>(P, Pc, Q, K, ldk, rhs);
+    build_table_kernel<double><<<grid, block, 0, st_>>>(P, Pc, Q, G, K, ldk, rhs);
     GK_LAUNCH_CHECK();
     return GK_OK;
 }

@@ -152,11 +152,12 @@ gk_status gk_build(const gk_system* sys, gk_prec prec, void* K, int64_t ldk,
                    void* rhs, gk_stream stream);
 
 /* The FP64 build from covariance tables: C over every pair of surface
- * points and C'/r (x_o - x_p) over every orientation-point pair are formed
- * once in ``work`` (gk_build_tables_bytes), then every interface entry is
- * assembled from them with the operations of gk_build -- the same matrix
- * (to rounding) with about a quarter of the covariance evaluations.  The
- * workspace is n_sp^2 + 3 n_ori n_sp doubles (16-byte aligned).  Same
+ * points, C'/r (x_o - x_p) over every orientation-point pair and the
+ * gradient-gradient terms over every orientation pair are formed once in
+ * ``work`` (gk_build_tables_bytes), then the covariance entries are
+ * assembled from them with the operations of gk_build -- the same matrix (to
+ * rounding) with a fraction of the covariance evaluations.  The workspace is
+ * n_sp^2 + 3 n_ori n_sp + 6 n_ori^2 doubles (16-byte aligned).  Same
  * reference call site as gk_build. */
 size_t gk_build_tables_bytes(const gk_system* sys /* HOST struct */);
 gk_status gk_build_tables(const gk_system* sys, double* K, int64_t ldk,
