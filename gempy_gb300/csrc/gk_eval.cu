@@ -492,6 +492,28 @@ drain:
     __syncthreads();
 }
 
+// Bounding box of a set of points over the CTA: v = {min x, y, z, max x, y,
+// z} per thread in, the CTA's box out (every thread).  sh holds 6 floats per
+// warp.
+__device__ __forceinline__ void cta_bbox(float (&v)[6], float* sh) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int c = 0; c < 6; ++c)
+        for (int o = 16; o > 0; o >>= 1) {
+            const float t = __shfl_xor_sync(0xffffffffu, v[c], o);
+            v[c] = c < 3 ? fminf(v[c], t) : fmaxf(v[c], t);
+        }
+    if (lane == 0)
+        for (int c = 0; c < 6; ++c) sh[6 * wid + c] = v[c];
+    __syncthreads();
+    for (int c = 0; c < 6; ++c) {
+        float r = sh[c];
+        for (int w = 1; w < nw; ++w) r = c < 3 ? fminf(r, sh[6 * w + c]) : fmaxf(r, sh[6 * w + c]);
+        v[c] = r;
+    }
+    __syncthreads();
+}
+
 // ---------------------------------------------------------------------------
 // float-float evaluation (cubic kernel, field only)
 // ---------------------------------------------------------------------------
@@ -500,6 +522,7 @@ __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const 
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t mbar[2];
     __shared__ int s_fail, s_abort;
+    __shared__ float s_box[6 * 8];
     const int tid = threadIdx.x;
     const int split = SPLIT ? P.split : 1;
     unsigned char* stage[2] = {smem, smem + P.stage_bytes};
@@ -570,6 +593,20 @@ __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const 
         double Z[PPT];
 #pragma unroll
         for (int p = 0; p < PPT; ++p) Z[p] = 0.0;
+        // the chunk's bounding box (high words), for the per-tile range test
+        // of the column path (col is uniform over the CTA)
+        float pbox[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+        if (PPT >= 4 && col) {   // (the 2-point variant keeps its registers for the point lists)
+#pragma unroll
+            for (int p = 0; p < PPT; ++p)
+                if (act[p])
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        pbox[c] = fminf(pbox[c], X[p].h[c]);
+                        pbox[3 + c] = fmaxf(pbox[3 + c], X[p].h[c]);
+                    }
+            cta_bbox(pbox, s_box);
+        }
 
         for (int k = 0; k < my_tiles; ++k, ++item) {
             const int t = rank + k * split;
@@ -592,9 +629,37 @@ __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const 
                 const bool ori = t < P.tiles_ori;
                 const int nr = ori ? min(P.rec_ori, P.n_ori - t * P.rec_ori)
                                    : min(P.rec_sp, P.n_sp - (t - P.tiles_ori) * P.rec_sp);
+                // every point-record pair of the tile within the range (r < 1
+                // in scaled units)?  Box distance of the high words plus the
+                // split quantum for the low words, with a margin for rounding.
+                bool in_range = false;
+                if (PPT >= 4 && col) {
+                    float rbox[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+                    for (int r = tid; r < nr; r += blockDim.x) {
+                        const float* R = rec + (ori ? 16 : 8) * r;
+                        const float rx = R[0], ry = R[2], rz = R[4];
+                        rbox[0] = fminf(rbox[0], rx);
+                        rbox[1] = fminf(rbox[1], ry);
+                        rbox[2] = fminf(rbox[2], rz);
+                        rbox[3] = fmaxf(rbox[3], rx);
+                        rbox[4] = fmaxf(rbox[4], ry);
+                        rbox[5] = fmaxf(rbox[5], rz);
+                    }
+                    cta_bbox(rbox, s_box);
+                    float far2 = 0.f;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const float m = fmaxf(pbox[3 + c] - rbox[c], rbox[3 + c] - pbox[c]) + (float)q;
+                        far2 += m * m;
+                    }
+                    in_range = far2 * 1.001f + eps2 < 0.999f;
+                }
                 bool done = !any_act;
                 if (!done && col && all_exact && all_act) {
-                    ff_tile_col<PPT>(rec, ori, nr, X, eps2, acc);
+                    if (in_range)
+                        ff_tile_col<PPT, false>(rec, ori, nr, X, eps2, acc);
+                    else
+                        ff_tile_col<PPT, true>(rec, ori, nr, X, eps2, acc);
                     done = true;
                 }
                 if (done) {

@@ -293,7 +293,9 @@ __device__ __forceinline__ void ff_tile(const float* __restrict__ rec, bool orie
 // two-sum of their high words and the low-order terms -- and, for an
 // orientation record, the x and y terms of w . h are formed once per record
 // and shared; only the z terms are per point.
-template <int NP>
+// CUT = false: the caller has shown that every pair lies within the range,
+// so the per-pair range test is compiled out.
+template <int NP, bool CUT = true>
 __device__ __forceinline__ void ff_tile_col(const float* __restrict__ rec, bool orientation, int nr,
                                             const PointFF (&X)[NP], float eps2, ffacc (&acc)[NP]) {
     for (int qr = 0; qr < nr; ++qr) {
@@ -324,7 +326,7 @@ __device__ __forceinline__ void ff_tile_col(const float* __restrict__ rec, bool 
                 float low = lxy + s2.l + b2.l;
                 low = __fmaf_rn(dl2, 2.f * dh2 + dl2, low);
                 const ff r2 = fast_two_sum(s2.h, low);
-                if (r2.h >= 1.f) continue;  // beyond the range: C'/r = 0
+                if (CUT && r2.h >= 1.f) continue;  // beyond the range: C'/r = 0
                 const ff k = ff_cubic_d1(r2, ff_sqrt_pos(r2));
                 const ff q2 = two_prod(wz.h, -dh2);
                 const float e2 = __fmaf_rn(wz.h, -dl2, __fmaf_rn(wz.l, -dh2, q2.l));
@@ -341,7 +343,7 @@ __device__ __forceinline__ void ff_tile_col(const float* __restrict__ rec, bool 
                 float low = lxy + s2.l + b2.l;
                 low = __fmaf_rn(dl2, 2.f * dh2 + dl2, low);
                 const ff r2 = fast_two_sum(s2.h, low);
-                if (r2.h >= 1.f) continue;  // beyond the range: C = 0
+                if (CUT && r2.h >= 1.f) continue;  // beyond the range: C = 0
                 ff_acc_fma(acc[p], ff_cubic_C(r2, ff_sqrt_pos(r2)), W);
             }
         }
