@@ -584,6 +584,7 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchDesc* __rest
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t mbar[2];
     __shared__ int s_fail;
+    __shared__ float s_box[6 * 8];
     const int tid = threadIdx.x;
     unsigned char* stage[2] = {smem, smem + kStage};
     const int rec_ori = kStage / 64, rec_sp = kStage / 32;
@@ -679,6 +680,20 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchDesc* __rest
             any_act = any_act || act[p];
             all_act = all_act && act[p];
         }
+        // this pass's bounding box (high words), for the per-tile range test
+        // of the column path (col is uniform over the CTA)
+        float pbox[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+        if (col) {
+#pragma unroll
+            for (int p = 0; p < kPPT; ++p)
+                if (act[p])
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        pbox[c] = fminf(pbox[c], X[p].h[c]);
+                        pbox[3 + c] = fmaxf(pbox[3 + c], X[p].h[c]);
+                    }
+            cta_bbox(pbox, s_box);
+        }
         for (int t = 0; t < nt; ++t) {
             const int sg = (int)(consumed & 1);
             const uint32_t parity = (uint32_t)((consumed >> 1) & 1);
@@ -724,9 +739,35 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchDesc* __rest
             const float* rec = reinterpret_cast<const float*>(stage[sg]);
             const bool ori = t < to;
             const int nr = ori ? min(rec_ori, d.n_ori - t * rec_ori) : min(rec_sp, d.n_sp - (t - to) * rec_sp);
+            bool in_range = false;
+            if (col) {
+                // every point-record pair of the tile within the range?
+                float rbox[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+                for (int r = tid; r < nr; r += blockDim.x) {
+                    const float* R = rec + (ori ? 16 : 8) * r;
+                    const float rx = R[0], ry = R[2], rz = R[4];
+                    rbox[0] = fminf(rbox[0], rx);
+                    rbox[1] = fminf(rbox[1], ry);
+                    rbox[2] = fminf(rbox[2], rz);
+                    rbox[3] = fmaxf(rbox[3], rx);
+                    rbox[4] = fmaxf(rbox[4], ry);
+                    rbox[5] = fmaxf(rbox[5], rz);
+                }
+                cta_bbox(rbox, s_box);
+                float far2 = 0.f;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const float m = fmaxf(pbox[3 + c] - rbox[c], rbox[3 + c] - pbox[c]) + (float)q;
+                    far2 += m * m;
+                }
+                in_range = far2 * 1.001f + eps2 < 0.999f;
+            }
             if (!any_act) {
             } else if (col && all_exact && all_act) {
-                ff_tile_col<kPPT>(rec, ori, nr, X, eps2, acc);
+                if (in_range)
+                    ff_tile_col<kPPT, false>(rec, ori, nr, X, eps2, acc);
+                else
+                    ff_tile_col<kPPT, true>(rec, ori, nr, X, eps2, acc);
             } else if (all_exact && all_act) {
                 ff_tile<kPPT, true, true>(rec, ori, nr, X, act, eps2, acc);
             } else if (all_exact) {

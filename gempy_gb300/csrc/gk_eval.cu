@@ -492,28 +492,6 @@ drain:
     __syncthreads();
 }
 
-// Bounding box of a set of points over the CTA: v = {min x, y, z, max x, y,
-// z} per thread in, the CTA's box out (every thread).  sh holds 6 floats per
-// warp.
-__device__ __forceinline__ void cta_bbox(float (&v)[6], float* sh) {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-    for (int c = 0; c < 6; ++c)
-        for (int o = 16; o > 0; o >>= 1) {
-            const float t = __shfl_xor_sync(0xffffffffu, v[c], o);
-            v[c] = c < 3 ? fminf(v[c], t) : fmaxf(v[c], t);
-        }
-    if (lane == 0)
-        for (int c = 0; c < 6; ++c) sh[6 * wid + c] = v[c];
-    __syncthreads();
-    for (int c = 0; c < 6; ++c) {
-        float r = sh[c];
-        for (int w = 1; w < nw; ++w) r = c < 3 ? fminf(r, sh[6 * w + c]) : fmaxf(r, sh[6 * w + c]);
-        v[c] = r;
-    }
-    __syncthreads();
-}
-
 // ---------------------------------------------------------------------------
 // float-float evaluation (cubic kernel, field only)
 // ---------------------------------------------------------------------------
