@@ -762,12 +762,19 @@ __global__ void __launch_bounds__(256) batch_eval_kernel(const BatchDesc* __rest
                 }
                 in_range = far2 * 1.001f + eps2 < 0.999f;
             }
+            ff wsum = {0.f, 0.f};
+            if (in_range && !ori) wsum = cta_weight_sum(rec, nr, s_box);   // uniform over the CTA
             if (!any_act) {
             } else if (col && all_exact && all_act) {
-                if (in_range)
+                if (in_range) {
+                    if (!ori) {
+#pragma unroll
+                        for (int p = 0; p < kPPT; ++p) acc[p] = {wsum.h, wsum.l};
+                    }
                     ff_tile_col<kPPT, false>(rec, ori, nr, X, eps2, acc);
-                else
+                } else {
                     ff_tile_col<kPPT, true>(rec, ori, nr, X, eps2, acc);
+                }
             } else if (all_exact && all_act) {
                 ff_tile<kPPT, true, true>(rec, ori, nr, X, act, eps2, acc);
             } else if (all_exact) {

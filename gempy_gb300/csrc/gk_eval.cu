@@ -632,12 +632,21 @@ __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const 
                     }
                     in_range = far2 * 1.001f + eps2 < 0.999f;
                 }
+                // the tile's weight sum, for the in-range surface-point path (all
+                // threads take part: in_range and ori are uniform over the CTA)
+                ff wsum = {0.f, 0.f};
+                if (in_range && !ori) wsum = cta_weight_sum(rec, nr, s_box);
                 bool done = !any_act;
                 if (!done && col && all_exact && all_act) {
-                    if (in_range)
+                    if (in_range) {
+                        if (!ori) {
+#pragma unroll
+                            for (int p = 0; p < PPT; ++p) acc[p] = {wsum.h, wsum.l};
+                        }
                         ff_tile_col<PPT, false>(rec, ori, nr, X, eps2, acc);
-                    else
+                    } else {
                         ff_tile_col<PPT, true>(rec, ori, nr, X, eps2, acc);
+                    }
                     done = true;
                 }
                 if (done) {

@@ -294,7 +294,9 @@ __device__ __forceinline__ void ff_tile(const float* __restrict__ rec, bool orie
 // orientation record, the x and y terms of w . h are formed once per record
 // and shared; only the z terms are per point.
 // CUT = false: the caller has shown that every pair lies within the range,
-// so the per-pair range test is compiled out.
+// so the per-pair range test is compiled out, and for surface-point records
+// the caller starts each accumulator at the tile's sum of weights
+// (cta_weight_sum): C = 1 + s^2 k, so only W s^2 k is accumulated per pair.
 template <int NP, bool CUT = true>
 __device__ __forceinline__ void ff_tile_col(const float* __restrict__ rec, bool orientation, int nr,
                                             const PointFF (&X)[NP], float eps2, ffacc (&acc)[NP]) {
@@ -343,8 +345,20 @@ __device__ __forceinline__ void ff_tile_col(const float* __restrict__ rec, bool 
                 float low = lxy + s2.l + b2.l;
                 low = __fmaf_rn(dl2, 2.f * dh2 + dl2, low);
                 const ff r2 = fast_two_sum(s2.h, low);
-                if (CUT && r2.h >= 1.f) continue;  // beyond the range: C = 0
-                ff_acc_fma(acc[p], ff_cubic_C(r2, ff_sqrt_pos(r2)), W);
+                if (CUT) {
+                    if (r2.h >= 1.f) continue;  // beyond the range: C = 0
+                    ff_acc_fma(acc[p], ff_cubic_C(r2, ff_sqrt_pos(r2)), W);
+                } else {
+                    // every pair in range: C = 1 + s^2 k, and the caller started the
+                    // accumulators at the tile's sum of weights, so only W s^2 k is added
+                    const ff s = ff_sqrt_pos(r2);
+                    ff k = ff_lin_dom(r2, 0.75f, -3.5f);
+                    k = ff_horner_dom(r2, k, 8.75f);
+                    k = ff_horner_dom(s, k, -7.f);
+                    const ff q = two_prod(r2.h, k.h);
+                    const float e = __fmaf_rn(r2.h, k.l, __fmaf_rn(r2.l, k.h, q.l));
+                    ff_acc_fma(acc[p], ff{q.h, e}, W);
+                }
             }
         }
         if ((qr & 7) == 7) {  // fold the low words back every 8 records
@@ -374,6 +388,28 @@ __device__ __forceinline__ void cta_bbox(float (&v)[6], float* sh) {
         v[c] = r;
     }
     __syncthreads();
+}
+
+// Sum of the weights of a tile's nr surface-point records (float-float,
+// reduced over the CTA; every thread gets the sum).  sh holds 2 floats per
+// warp.
+__device__ __forceinline__ ff cta_weight_sum(const float* __restrict__ rec, int nr, float* sh) {
+    ff s = {0.f, 0.f};
+    for (int r = threadIdx.x; r < nr; r += blockDim.x) s = ff_add(s, ff{rec[8 * r + 6], rec[8 * r + 7]});
+    for (int o = 16; o > 0; o >>= 1) {
+        const ff t = {__shfl_xor_sync(0xffffffffu, s.h, o), __shfl_xor_sync(0xffffffffu, s.l, o)};
+        s = ff_add(s, t);
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane == 0) {
+        sh[2 * wid] = s.h;
+        sh[2 * wid + 1] = s.l;
+    }
+    __syncthreads();
+    ff t = {sh[0], sh[1]};
+    for (int w = 1; w < nw; ++w) t = ff_add(t, ff{sh[2 * w], sh[2 * w + 1]});
+    __syncthreads();
+    return t;
 }
 
 __device__ __forceinline__ ff ff_from_double(double x) {
