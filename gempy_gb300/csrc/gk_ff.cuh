@@ -28,6 +28,13 @@ __device__ __forceinline__ ff fast_two_sum(float a, float b) {  // |a| >= |b| or
     return {s, e};
 }
 
+// a + b of two non-negative floats as an exact pair: Fast2Sum on the
+// ordered operands (two comparisons instead of TwoSum's three extra adds)
+__device__ __forceinline__ ff two_sum_nonneg(float a, float b) {
+    const float hi = fmaxf(a, b), lo = fminf(a, b);
+    return fast_two_sum(hi, lo);
+}
+
 __device__ __forceinline__ ff two_prod(float a, float b) {
     float p = __fmul_rn(a, b);
     float e = __fmaf_rn(a, b, -p);
@@ -307,7 +314,7 @@ __device__ __forceinline__ void ff_tile_col(const float* __restrict__ rec, bool 
         const float dh0 = X[0].h[0] - a0.x, dl0 = X[0].l[0] - a0.y;
         const float dh1 = X[0].h[1] - a0.z, dl1 = X[0].l[1] - a0.w;
         const ff b0 = two_prod(dh0, dh0), b1 = two_prod(dh1, dh1);
-        const ff sxy = two_sum(b0.h, b1.h);
+        const ff sxy = two_sum_nonneg(b0.h, b1.h);
         float lxy = sxy.l + b0.l + b1.l + eps2;
         lxy = __fmaf_rn(dl0, 2.f * dh0 + dl0, lxy);
         lxy = __fmaf_rn(dl1, 2.f * dh1 + dl1, lxy);
@@ -324,7 +331,7 @@ __device__ __forceinline__ void ff_tile_col(const float* __restrict__ rec, bool 
             for (int p = 0; p < NP; ++p) {
                 const float dh2 = X[p].h[2] - a1.x, dl2 = X[p].l[2] - a1.y;
                 const ff b2 = two_prod(dh2, dh2);
-                const ff s2 = two_sum(sxy.h, b2.h);
+                const ff s2 = two_sum_nonneg(sxy.h, b2.h);
                 float low = lxy + s2.l + b2.l;
                 low = __fmaf_rn(dl2, 2.f * dh2 + dl2, low);
                 const ff r2 = fast_two_sum(s2.h, low);
@@ -341,7 +348,7 @@ __device__ __forceinline__ void ff_tile_col(const float* __restrict__ rec, bool 
             for (int p = 0; p < NP; ++p) {
                 const float dh2 = X[p].h[2] - a1.x, dl2 = X[p].l[2] - a1.y;
                 const ff b2 = two_prod(dh2, dh2);
-                const ff s2 = two_sum(sxy.h, b2.h);
+                const ff s2 = two_sum_nonneg(sxy.h, b2.h);
                 float low = lxy + s2.l + b2.l;
                 low = __fmaf_rn(dl2, 2.f * dh2 + dl2, low);
                 const ff r2 = fast_two_sum(s2.h, low);
