@@ -37,7 +37,7 @@ sys.path.insert(0, ROOT)
 METRIC = "grid points/s + kriging solves/s: mixed/learned vs FP64 GPU at 1e-6 field error"
 # thread instructions per point-record pair of the float-float field kernel,
 # from ncu's executed-instruction count (profiles/eval_ff_precision_64.md)
-FF_OPS_PER_PAIR = 83
+FF_OPS_PER_PAIR = 80
 WORKLOAD = ("precision: 1 series, 4000 surface points on 8 folded surfaces, 1500 orientations "
             "(N=8495), cubic, linear drift, 256^3 regular grid")
 
@@ -473,7 +473,7 @@ def main():
                                     f"(max SM clock from MEASURED_PEAKS.json, {pk['_source']})",
                      "work": f"{fl_pt} algorithmic flops/point x {n_pts} points per launch",
                      "eval_ms": ev_mixed,
-                     # float-float executes ~83 thread instructions per point-record pair (ncu count of the
+                     # float-float executes ~80 thread instructions per point-record pair (ncu count of the
                      # shipped kernel at 64^3, profiles/eval_ff_precision_64.md)
                      # where the algorithmic count has 20: the pipe view
                      "fp32_pipe_ops_per_pair": FF_OPS_PER_PAIR, "algorithmic_flops_per_pair": 20,
