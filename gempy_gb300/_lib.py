@@ -183,7 +183,8 @@ SIGNATURES = [
     ("gk_octree_level_plan", ctypes.c_int, [ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
                                               ctypes.POINTER(GkOctreeLevelLayout)]),
     ("gk_octree_level", ctypes.c_int, [ctypes.c_int32, ctypes.POINTER(GkSeriesEval), ctypes.c_void_p, c_double_p,
-                                       ctypes.c_int, ctypes.c_int32, c_int32_p, ctypes.POINTER(GkOctreeLevelLayout),
+                                       ctypes.c_int, ctypes.c_int32, c_int32_p, ctypes.c_double,
+                                       ctypes.POINTER(GkOctreeLevelLayout),
                                        ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]),
     ("gk_adjoint_rhs", ctypes.c_int, [ctypes.POINTER(GkSystem), ctypes.POINTER(GkPoints), ctypes.c_void_p,
                                       ctypes.c_void_p, ctypes.c_void_p]),

@@ -7,6 +7,17 @@
 // parent order, which matches the point order of the reference's approved
 // anticline and fault-model scalar fields
 // (test/test_model_types/test_example_models_I.py:19-23, 41-68).
+//
+// The engine's second refinement test, by an error statistic
+// (``octree_error_threshold``; "marked by stats" in
+// docs/developers_notes/dev_log/log_2024-06.md:26-39), is restated as: per
+// series, the error of trilinear interpolation at the voxel centre,
+// |Z(centre) - mean of the 8 corners|, in units of the corners' standard
+// deviation; a voxel is marked when that error exceeds the level's mean error
+// by ``error_threshold`` standard deviations of the level's errors (and
+// kErrorFloor, below which it is the rounding of a field linear over the
+// voxel).  With it the combination model's approved last level
+// (test_example_models_I.py:71-88) is reproduced.
 #include <cstring>
 
 #include "gk_common.cuh"
@@ -35,14 +46,23 @@ __global__ void corners_kernel(int64_t n, const double* __restrict__ c, double h
 constexpr int kScanBlock = 256;
 constexpr int kMaxIdSets = 1 + GK_MAX_SURFACES;
 
+constexpr double kErrorFloor = 1e-6;
+constexpr int kStatThreads = 1024;
+
 // The id arrays a voxel's refinement looks at: set s holds the 8 corner ids
-// of voxel v at p[s][8 v .. 8 v + 7].
+// of voxel v at p[s][8 v .. 8 v + 7].  With n_err > 0, voxel v is also marked
+// when err[s n_vox + v] > thr[s] for some series s < n_err.
 struct IdSets {
     const int32_t* p[kMaxIdSets];
     int n;
+    int n_err;
+    int64_t n_vox;
+    const double* err;
+    const double* thr;
 };
 
-// voxel v is marked when its 8 corners differ in any id set
+// voxel v is marked when its 8 corners differ in any id set, or when its
+// interpolation error is an outlier in any series
 __device__ __forceinline__ int voxel_marked(const IdSets& ids, int64_t v) {
     int m = 0;
     for (int s = 0; s < ids.n && !m; ++s) {
@@ -50,7 +70,60 @@ __device__ __forceinline__ int voxel_marked(const IdSets& ids, int64_t v) {
         const int32_t a = c[0];
         for (int k = 1; k < 8; ++k) m |= (c[k] != a);
     }
+    for (int s = 0; s < ids.n_err && !m; ++s) m = ids.err[s * ids.n_vox + v] > ids.thr[s];
     return m;
+}
+
+// err[s n + v] = |Z_s(centre v) - mean_k Z_s(corner k of v)| / std_k Z_s(corner
+// k of v), 0 where the 8 corners are equal.  fields: n_series x np, the
+// centres' values first, then 8 corners per centre.
+__global__ void interp_error_kernel(int64_t n, int64_t np, int n_series, const double* __restrict__ fields,
+                                    double* __restrict__ err) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n * n_series) return;
+    const int s = (int)(i / n);
+    const int64_t v = i - (int64_t)s * n;
+    const double* f = fields + (int64_t)s * np;
+    const double* c = f + n + 8 * v;
+    double z[8], mean = 0.0;
+    for (int k = 0; k < 8; ++k) {
+        z[k] = c[k];
+        mean += z[k];
+    }
+    mean *= 0.125;
+    double var = 0.0;
+    for (int k = 0; k < 8; ++k) var += (z[k] - mean) * (z[k] - mean);
+    const double sd = sqrt(var * 0.125);
+    err[i] = sd > 0.0 ? fabs(f[v] - mean) / sd : 0.0;
+}
+
+// fixed-order sum over the CTA (kStatThreads threads)
+__device__ double cta_sum(double x, double* red) {
+    red[threadIdx.x] = x;
+    __syncthreads();
+    for (int off = kStatThreads / 2; off > 0; off >>= 1) {
+        if ((int)threadIdx.x < off) red[threadIdx.x] += red[threadIdx.x + off];
+        __syncthreads();
+    }
+    const double r = red[0];
+    __syncthreads();
+    return r;
+}
+
+// One CTA per series: thr[s] = max(mean + t std, kErrorFloor) of err[s n ..
+// s n + n - 1] (two passes, population std; the order of the sums is fixed,
+// so the threshold is the same on every run).
+__global__ void error_threshold_kernel(int64_t n, const double* __restrict__ err, double t,
+                                       double* __restrict__ thr) {
+    __shared__ double red[kStatThreads];
+    const double* e = err + (int64_t)blockIdx.x * n;
+    double a = 0.0;
+    for (int64_t v = threadIdx.x; v < n; v += kStatThreads) a += e[v];
+    const double mean = cta_sum(a, red) / (double)n;
+    a = 0.0;
+    for (int64_t v = threadIdx.x; v < n; v += kStatThreads) a += (e[v] - mean) * (e[v] - mean);
+    const double sd = sqrt(cta_sum(a, red) / (double)n);
+    if (threadIdx.x == 0) thr[blockIdx.x] = fmax(mean + t * sd, kErrorFloor);
 }
 
 // per-block count of marked voxels
@@ -177,7 +250,7 @@ static size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
 extern "C" gk_status gk_octree_level_plan(int32_t n_series, int64_t n, int32_t corners, int32_t refine,
                                             gk_octree_level_layout* L) {
     if (L == nullptr || n_series < 1 || n_series > GK_MAX_SURFACES || n < 0) return GK_ERR_ARG;
-    if (refine < 0 || refine > 2 || (refine == 1 && !corners)) return GK_ERR_ARG;
+    if (refine < 0 || refine > 3 || ((refine == 1 || refine == 3) && !corners)) return GK_ERR_ARG;
     memset(L, 0, sizeof(*L));
     const int64_t np = corners ? 9 * n : n;
     L->n = n;
@@ -198,6 +271,7 @@ extern "C" gk_status gk_octree_level_plan(int32_t n_series, int64_t n, int32_t c
         o += al256((size_t)8 * n * 3 * sizeof(double));
         L->count = o;  o += 256;
         L->work = o;   o += al256(gk_octree_workspace_bytes(n));
+        if (refine == 3) o += al256((size_t)n_series * n * sizeof(double)) + al256((size_t)n_series * sizeof(double));
     } else {
         L->count = L->work = o;
     }
@@ -207,9 +281,11 @@ extern "C" gk_status gk_octree_level_plan(int32_t n_series, int64_t n, int32_t c
 
 extern "C" gk_status gk_octree_level(int32_t n_series, const gk_series_eval* series, const double* centres,
                                      const double spacing[3], gk_prec prec, int32_t n_fault_sets,
-                                     const int32_t* fault_series, const gk_octree_level_layout* L, void* buf,
-                                     size_t buf_bytes, gk_info* info, gk_stream stream) {
+                                     const int32_t* fault_series, double error_threshold,
+                                     const gk_octree_level_layout* L, void* buf, size_t buf_bytes, gk_info* info,
+                                     gk_stream stream) {
     if (L == nullptr || series == nullptr || spacing == nullptr || n_series != L->n_series) return GK_ERR_ARG;
+    if (L->refine == 3 && !(error_threshold > 0.0 && error_threshold < 1e300)) return GK_ERR_ARG;
     if (n_fault_sets < 0 || n_fault_sets > GK_MAX_SURFACES || (n_fault_sets > 0 && fault_series == nullptr))
         return GK_ERR_ARG;
     gk_octree_level_layout chk;
@@ -245,13 +321,26 @@ extern "C" gk_status gk_octree_level(int32_t n_series, const gk_series_eval* ser
     if (!L->refine) return GK_OK;
     IdSets sets;
     memset(&sets, 0, sizeof(sets));
-    if (L->refine == 1) {
+    if (L->refine == 1 || L->refine == 3) {
         sets.p[sets.n++] = lith + n;   // the corners' lithology, then each fault series' block ids
         for (int f = 0; f < n_fault_sets; ++f) {
             const int s = fault_series[f];
             if (s < 0 || s >= n_series) return GK_ERR_ARG;
             sets.p[sets.n++] = ids + (int64_t)s * np + n;
         }
+    }
+    if (L->refine == 3) {
+        double* err = (double*)(b + L->work + al256(gk_octree_workspace_bytes(n)));
+        double* thr = (double*)((char*)err + al256((size_t)n_series * n * sizeof(double)));
+        const int64_t ne = n * n_series;
+        interp_error_kernel<<<(unsigned)((ne + 255) / 256), 256, 0, cs>>>(n, np, n_series, fields, err);
+        GK_LAUNCH_CHECK();
+        error_threshold_kernel<<<n_series, kStatThreads, 0, cs>>>(n, err, error_threshold, thr);
+        GK_LAUNCH_CHECK();
+        sets.n_err = n_series;
+        sets.n_vox = n;
+        sets.err = err;
+        sets.thr = thr;
     }
     return refine_voxels(n, pts, sets, L->refine == 2, spacing, (double*)(b + L->children), (int64_t*)(b + L->count),
                          b + L->work, cs);

@@ -591,6 +591,7 @@ def _compute_model(interpolation_input, options, data_descriptor, geophysics_inp
     n_levels = int(eo.number_octree_levels)
     min_level = int(eo.octree_min_level)
     levels_surface = int(getattr(eo, "number_octree_levels_surface", getattr(eo, "_number_octree_levels_surface", 0)))
+    error_threshold = float(getattr(eo, "octree_error_threshold", 1.0))
     if grid.octree_grid is not None and n_levels >= 1:
         og = grid.octree_grid
         centres = torch.as_tensor(og.values).to(device)
@@ -601,8 +602,10 @@ def _compute_model(interpolation_input, options, data_descriptor, geophysics_inp
             surface = level < levels_surface
             refine_all = level + 1 < min_level
             refine = 0 if last else (2 if refine_all else 1)
-            lvl = K.OctreeLevel(ss, centres, d, prec, corners=surface or refine == 1, refine=refine,
-                                fault_series=ev._frows)
+            if refine == 1 and error_threshold > 0 and level + 1 < levels_surface - 1:
+                refine = 3   # corner marks plus the interpolation-error statistic
+            lvl = K.OctreeLevel(ss, centres, d, prec, corners=surface or refine in (1, 3), refine=refine,
+                                fault_series=ev._frows, error_threshold=error_threshold)
             grads = [None] * len(series)
             if want_grad:
                 pts, _, V, _, _, _, _ = lvl.views(lvl.buffer)

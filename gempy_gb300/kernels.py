@@ -671,10 +671,11 @@ class OctreeLevel:
     level's points ([centres; corners] or the centres), their combination and
     -- unless it is the last level -- the children of the refined voxels, all
     in one device buffer.  ``result_bytes`` covers the level's results (points
-    to masks); the children follow."""
+    to masks); the children follow.  ``refine`` 3 adds the interpolation-
+    error test with ``error_threshold`` standard deviations."""
 
     def __init__(self, series_set: "SeriesSet", centres, spacing, prec, corners, refine, fault_series=(),
-                 info=None):
+                 info=None, error_threshold=0.0):
         lib = _lib.load()
         n = int(centres.shape[0])
         L = _lib.GkOctreeLevelLayout()
@@ -685,7 +686,8 @@ class OctreeLevel:
         fs = (ctypes.c_int32 * max(1, len(fault_series)))(*[int(f) for f in fault_series])
         sp = (ctypes.c_double * 3)(*[float(v) for v in spacing])
         check("gk_octree_level", lib.gk_octree_level(series_set.n, series_set.arr, _ptr(centres.contiguous()), sp,
-                                                     prec, len(fault_series), fs, ctypes.byref(L),
+                                                     prec, len(fault_series), fs, float(error_threshold),
+                                                     ctypes.byref(L),
                                                      self.buffer.data_ptr(), int(L.total), _ptr(info), _stream()))
         self.result_bytes = int(L.children)
 

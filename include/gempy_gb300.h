@@ -295,11 +295,12 @@ gk_status gk_solve_twolevel(int64_t n, const double* K, int64_t ldk,
  * library (8 MiB, held on every GPU that loads the library until the process
  * exits), so only systems with n <= GK_NOALLOC_MAX_N are accepted; larger n
  * returns GK_ERR_SIZE before any work is queued.  The caller still passes K,
- * b and x.  The first call made on a device looks up the array's device
- * address (cudaGetSymbolAddress); make that first call before any stream
- * capture.  The address is kept for the life of the process: after a
- * cudaDeviceReset the library must be reloaded before this entry point is
- * called again.  All calls share the one array: calls that overlap on the GPU
+ * b and x.  Like gk_solve_mixed it synchronizes its stream between Krylov
+ * steps and reads results on the host, so it cannot be captured in a CUDA
+ * graph.  The first call made on a device looks up the array's device
+ * address (cudaGetSymbolAddress), which is kept for the life of the process:
+ * after a cudaDeviceReset the library must be reloaded before this entry
+ * point is called again.  All calls share the one array: calls that overlap on the GPU
  * race, so serialize them (one stream, or explicit ordering).  Nothing here
  * calls cudaMalloc, cudaFree or an allocating library routine.  Arguments,
  * results and ``info`` are as for gk_solve_mixed (``info`` may be NULL). */
@@ -393,13 +394,18 @@ gk_status gk_octree_refine(int64_t n, const double* centres,
  * when ``corners`` -- every series at those points and their combination
  * (gk_eval_series_set), and, when ``refine`` (1: voxels whose corners differ
  * in lithology or in the block of a fault series ``fault_series[0..
- * n_fault_sets-1]``; 2: every voxel), the children of the refined voxels and
- * 8 x their count.  Every output lands in one device buffer of ``total``
+ * n_fault_sets-1]``; 2: every voxel; 3: as 1, plus the voxels whose
+ * interpolation error is an outlier -- in some series, |Z(centre) - mean of
+ * the 8 corners| / std of the 8 corners above the level's mean of that error
+ * by ``error_threshold`` (> 0) of its standard deviations, and above 1e-6:
+ * the engine's ``octree_error_threshold`` test), the children of the refined
+ * voxels and 8 x their count.  Every output lands in one device buffer of ``total``
  * bytes laid out by gk_octree_level_plan (byte offsets, 256-aligned):
  *   points   n_points x 3 FP64      fields, values  n_series x n_points FP64
  *   ids      n_series x n_points i32   block  n_points FP64
  *   lith_ids n_points i32           masks  n_series x n_points u8
- *   children 8n x 3 FP64            count  int64 (refine only), then scratch.
+ *   children 8n x 3 FP64            count  int64 (refine only), then scratch
+ *   (refine 3 also keeps the errors, n_series x n FP64, there).
  * Everything before ``children`` is the level's result; ``children[0..count)``
  * are the next level's centres.  ``centres`` may lie in the previous level's
  * buffer. */
@@ -408,7 +414,8 @@ typedef struct gk_octree_level_layout {
     int64_t n_points;   /* n, or 9n with corners                      */
     int32_t n_series;
     int32_t corners;    /* 1: points are [centres; corners]           */
-    int32_t refine;     /* 0: last level, 1: marked voxels, 2: all    */
+    int32_t refine;     /* 0: last level, 1: marked voxels, 2: all,
+                           3: marked by corners or by the error test  */
     int32_t reserved;
     uint64_t points, fields, values, ids, block, lith_ids, masks;
     uint64_t children, count, work, total;
@@ -420,6 +427,7 @@ gk_status gk_octree_level(int32_t n_series, const gk_series_eval* series,
                           const double spacing[3] /* HOST */, gk_prec prec,
                           int32_t n_fault_sets,
                           const int32_t* fault_series /* HOST */,
+                          double error_threshold,
                           const gk_octree_level_layout* layout /* HOST */,
                           void* buf, size_t buf_bytes, gk_info* info,
                           gk_stream stream);

@@ -27,10 +27,18 @@ known-answer tests:
   under the reference's comparator ``np.allclose(rtol=1e-5, atol=1e-5)``
   (``test/verify_helper.py:70-103``), octree point order included.  The
   block-level conventions (``kriging`` module docstring) were chosen with this
-  file; the fault and combination approval files judge them independently.
+  file; the fault-model approval file (``test_example_models_I.py:56-68``)
+  judges them independently;
+* pinned, field and refinement: the combination model's approval file
+  (``test_example_models_I.py:71-88``), which also fixed the form of the
+  octree's interpolation-error refinement (``octree`` module docstring);
+* pinned, counts: the combination model's marching-cubes vertex counts
+  (``test/test_modules/test_marching_cubes.py:44-47``, ``mesh`` module).
 
 Modules: ``covariance`` (kernel functions), ``kriging`` (matrix build, solve,
 evaluation), ``segmentation`` (sigmoid ids, series masks), ``octree`` (corner
-based refinement), ``pipeline`` (multi-series compute_model restatement).
+and interpolation-error refinement), ``pipeline`` (multi-series compute_model
+restatement), ``mesh`` (marching cubes), ``gravity`` (prism forward gravity,
+unpinned), ``mlp`` (the preconditioner network).
 """
 from . import covariance, kriging, segmentation, octree, pipeline  # noqa: F401

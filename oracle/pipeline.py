@@ -17,7 +17,9 @@ and at every evaluation point the fault block is evaluated first.
 Octree.  A voxel is refined when its 8 corners differ in lithology id (the
 combined block) or in the id of any fault series' block, and every voxel is
 refined while the next level is below ``octree_min_level`` (default 2).
-Levels below ``number_octree_levels_surface`` (default 4) also evaluate their
+While the next level is below ``number_octree_levels_surface - 1`` voxels are
+also refined by the interpolation-error statistic of ``octree.error_marks``
+(``octree_error_threshold`` standard deviations, default 1).  Levels below ``number_octree_levels_surface`` (default 4) also evaluate their
 voxel corners for the mesh extraction that follows, and the reference exports
 those corner values after the centres' (``exported_fields.scalar_field`` of
 ``octrees_output[l].outputs[s]``); ``compute_octree`` returns them per level.
@@ -162,10 +164,14 @@ class Level:
 
 
 def compute_octree(series_list, relations, unit_values, slope, extent, base_resolution,
-                   n_levels, min_level=2, fault_relations=None, levels_surface=None, model=None):
+                   n_levels, min_level=2, fault_relations=None, levels_surface=None, model=None,
+                   error_threshold=1.0):
     """List of (centres, Result) per level (``levels_surface`` None); with
     ``levels_surface`` set, a list of ``Level`` records whose levels below it
-    keep their corner evaluation."""
+    keep their corner evaluation.  Voxels are refined by the corner rule, and
+    while the next level is below ``levels_surface - 1`` (4 when None) also
+    by the interpolation-error statistic with ``error_threshold`` standard
+    deviations (off when <= 0)."""
     m = model or Model(series_list, relations, unit_values, slope, fault_relations)
     centres, d = octree.base_centres(extent, base_resolution)
     out = []
@@ -186,6 +192,9 @@ def compute_octree(series_list, relations, unit_values, slope, extent, base_reso
             sel = np.ones(len(centres), dtype=bool)
         else:
             sel = refinement_marks(rc)
+            ls = 4 if levels_surface is None else levels_surface
+            if error_threshold > 0 and level + 1 < ls - 1:
+                sel |= octree.error_marks(res.fields, rc.fields, error_threshold)
         centres = octree.children(centres[sel], d)
         d = d / 2.0
     return out

@@ -123,16 +123,23 @@ def test_octree_level_plan_on_the_host(lib):
     assert lib.gk_octree_level_plan(ns, n, 0, 1, ctypes.byref(L)) == _lib.GK_ERR_ARG
     assert lib.gk_octree_level_plan(0, n, 1, 1, ctypes.byref(L)) == _lib.GK_ERR_ARG
     assert lib.gk_octree_level_plan(ns, -1, 1, 1, ctypes.byref(L)) == _lib.GK_ERR_ARG
-    assert lib.gk_octree_level_plan(ns, n, 1, 3, ctypes.byref(L)) == _lib.GK_ERR_ARG
-    # a layout that the plan did not make, or a short buffer, is refused before any launch
-    assert lib.gk_octree_level_plan(ns, n, 1, 1, ctypes.byref(L)) == _lib.GK_OK
+    assert lib.gk_octree_level_plan(ns, n, 1, 4, ctypes.byref(L)) == _lib.GK_ERR_ARG
+    assert lib.gk_octree_level_plan(ns, n, 0, 3, ctypes.byref(L)) == _lib.GK_ERR_ARG
+    # the error test (refine 3) keeps n_series x n errors and the thresholds after the scan workspace
+    assert lib.gk_octree_level_plan(ns, n, 1, 3, ctypes.byref(L)) == _lib.GK_OK
+    assert L.total - L.work >= lib.gk_octree_workspace_bytes(n) + 8 * ns * n + 8 * ns
     items = (_lib.GkSeriesEval * ns)()
     sp3 = (ctypes.c_double * 3)(1.0, 1.0, 1.0)
     buf = ctypes.c_void_p(256)
-    assert lib.gk_octree_level(ns, items, buf, sp3, 0, 0, None, ctypes.byref(L), buf, L.total - 1, None,
+    for t in (0.0, -1.0, float("nan"), float("inf")):   # the error test needs a finite threshold > 0
+        assert lib.gk_octree_level(ns, items, buf, sp3, 0, 0, None, t, ctypes.byref(L), buf, L.total, None,
+                                   None) == _lib.GK_ERR_ARG
+    # a layout that the plan did not make, or a short buffer, is refused before any launch
+    assert lib.gk_octree_level_plan(ns, n, 1, 1, ctypes.byref(L)) == _lib.GK_OK
+    assert lib.gk_octree_level(ns, items, buf, sp3, 0, 0, None, 0.0, ctypes.byref(L), buf, L.total - 1, None,
                                None) == _lib.GK_ERR_SIZE
     L.masks += 256
-    assert lib.gk_octree_level(ns, items, buf, sp3, 0, 0, None, ctypes.byref(L), buf, L.total, None,
+    assert lib.gk_octree_level(ns, items, buf, sp3, 0, 0, None, 0.0, ctypes.byref(L), buf, L.total, None,
                                None) == _lib.GK_ERR_ARG
 
 

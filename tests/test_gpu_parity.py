@@ -413,16 +413,18 @@ def test_compute_model_three_series_octree_matches_oracle():
     np.testing.assert_allclose(sol.scalar_field_at_surface_points, iso_ref, rtol=1e-9, atol=0)
 
 
-def _golden_octree(name, dtype="float64"):
+def _golden_octree(name, dtype="float64", error_threshold=1.0):
     import gempy_gb300 as gg
     from oracle import inputs
     g = load_golden(name)
     ii, opts, dd, ext = engine_inputs_from_golden(g)
+    opts.evaluation_options.octree_error_threshold = error_threshold
     sol = gg.compute_model(ii, opts, dd, config=gg.EngineConfig(dtype=dtype))
     series, rels, fr = inputs.series_from_golden(g)
     oc = g["octree"]
     lv = pipeline.compute_octree(series, rels, g["unit_values"], g["sigmoid_slope"], ext, oc["base_resolution"],
-                                 oc["levels"], fault_relations=fr, levels_surface=oc.get("levels_surface", 4))
+                                 oc["levels"], fault_relations=fr, levels_surface=oc.get("levels_surface", 4),
+                                 error_threshold=error_threshold)
     return g, sol, lv, series
 
 
@@ -479,13 +481,28 @@ def test_compute_model_keep_on_device_matches_host_outputs(dtype):
             same(ch.mask_matrix, cd.mask_matrix)
 
 
-def test_compute_model_combination_model_matches_oracle():
+def test_compute_model_combination_model_pins():
     """Fault + eroding unconformity + folded strata (three series, the fault
-    offsetting both): every octree level of compute_model against the oracle,
-    including the corner values the surface levels export."""
+    offsetting both): the reference's approval file (test_example_models_I.py:
+    71-88) under its own comparator -- which needs the interpolation-error
+    refinement (4328 voxels at the last level, 4232 by the corners alone) --
+    and every octree level of compute_model against the oracle, including the
+    corner values the surface levels export."""
     g, sol, lv, series = _golden_octree("combination_model.json")
+    assert [len(o.grid_centers) for o in sol.octrees_output] == [16, 128, 776, 4328]
+    z = sol.octrees_output[-1].outputs[0].scalar_field
+    assert len(z) == 9 * len(sol.octrees_output[-1].grid_centers)
+    approved = np.array(g["octree"]["approved_scalar_field_last_level"])
+    assert np.allclose(z[:: len(z) // 50], approved, rtol=1e-5, atol=1e-5)
     _assert_levels_match(sol, lv, len(series))
-    assert len(sol.octrees_output[-1].outputs[0].scalar_field) == 9 * len(sol.octrees_output[-1].grid_centers)
+
+
+def test_compute_model_error_refinement_off_matches_oracle():
+    """octree_error_threshold <= 0 switches the interpolation-error test off:
+    the corner rule alone, on the GPU and in the oracle."""
+    g, sol, lv, series = _golden_octree("combination_model.json", error_threshold=0.0)
+    assert len(sol.octrees_output[-1].grid_centers) == 4232
+    _assert_levels_match(sol, lv, len(series))
 
 
 def test_compute_model_fault_model_mixed_matches_plain():

@@ -206,35 +206,63 @@ def test_fault_drift_offsets_horizontal_layers_exactly():
     assert set(np.unique(np.rint(F[x < 0]))) != set(np.unique(np.rint(F[x > 0])))
 
 
-def test_combination_model_export_layout_and_field():
+def test_combination_model_approval_file():
     """The combination model (examples_generator.py:244-293; four levels with
-    number_octree_levels_surface 4): its last level exports the centres'
-    values followed by the 8 corners of every centre (the first 6 of the 51
-    sampled values are level-3 cell centres, the others level-3 nodes), and
-    every approved value is a value of the oracle's fault field at such a
-    point.  (The lithology refinement of this model is not yet reproduced, so
-    the sampled positions differ; the point count is not asserted.)"""
+    number_octree_levels_surface 4) against its approval file
+    (test_example_models_I.py:71-88) with the reference's comparator: the last
+    level exports the centres' values followed by the 8 corners of every
+    centre, and its 4328 voxels include the 96 that the interpolation-error
+    statistic adds (children of four level-1 voxels whose corners agree)."""
     g, series, levels = _octree_levels("combination_model.json")
+    assert [len(l.centres) for l in levels] == [16, 128, 776, 4328]
     last = levels[-1]
-    assert last.corner_result is not None
-    assert len(last.exported_field(0)) == 9 * len(last.centres)
-    from oracle import inputs
-    ext = inputs.golden_extent(g)
-    base = np.array(g["octree"]["base_resolution"])
-    series, rels, fr = inputs.series_from_golden(g)
-    m = pipeline.Model(series, rels, g["unit_values"], g["sigmoid_slope"], fr)
-    cells = base * 2 ** (g["octree"]["levels"] - 1)
-    h = (ext[1::2] - ext[0::2]) / cells
-    axes_c = [ext[2 * i] + h[i] * (np.arange(cells[i]) + 0.5) for i in range(3)]
-    axes_n = [ext[2 * i] + h[i] * np.arange(cells[i] + 1) for i in range(3)]
-    zc = m.field(0, np.stack(np.meshgrid(*axes_c, indexing="ij"), -1).reshape(-1, 3))
-    zn = m.field(0, np.stack(np.meshgrid(*axes_n, indexing="ij"), -1).reshape(-1, 3))
+    z = last.exported_field(0)
+    assert len(z) == 9 * len(last.centres)
+    sampled = z[:: len(z) // 50]
     approved = np.array(g["octree"]["approved_scalar_field_last_level"])
-    tol = 1e-5 + 1e-5 * np.abs(approved)
-    on_centre = [np.abs(zc - v).min() <= t for v, t in zip(approved, tol)]
-    on_node = [np.abs(zn - v).min() <= t for v, t in zip(approved, tol)]
-    assert all(on_centre[:6])
-    assert all(on_node[6:])
+    assert sampled.shape == approved.shape
+    assert np.allclose(sampled, approved, rtol=1e-5, atol=1e-5)
+
+
+def test_error_statistic_adds_nothing_where_corners_suffice():
+    """Without the interpolation-error statistic the combination model's
+    sampled values no longer match (the corner rule alone gives 4232 voxels),
+    and on the one-fault model the statistic adds no voxel."""
+    from oracle import inputs
+    g = load_golden("combination_model.json")
+    series, rels, fr = inputs.series_from_golden(g)
+    oc = g["octree"]
+    lv = pipeline.compute_octree(series, rels, g["unit_values"], g["sigmoid_slope"], inputs.golden_extent(g),
+                                 oc["base_resolution"], oc["levels"], fault_relations=fr, levels_surface=4,
+                                 error_threshold=0.0)
+    assert len(lv[-1].centres) == 4232
+    z = lv[-1].exported_field(0)
+    approved = np.array(oc["approved_scalar_field_last_level"])
+    assert not np.allclose(z[:: len(z) // 50], approved, rtol=1e-5, atol=1e-5)
+    g = load_golden("fault_model.json")
+    series, rels, fr = inputs.series_from_golden(g)
+    oc = g["octree"]
+    counts = [len(l.centres) for l in pipeline.compute_octree(
+        series, rels, g["unit_values"], g["sigmoid_slope"], inputs.golden_extent(g), oc["base_resolution"],
+        oc["levels"], fault_relations=fr, levels_surface=4, error_threshold=0.0)]
+    assert counts == [8, 64, 320, 1440, 6032, 24624]
+
+
+def test_interpolation_error_is_zero_for_a_linear_field():
+    """A field linear over the voxel has zero interpolation error up to
+    rounding, which the floor keeps from marking anything."""
+    from oracle import octree
+    rng = np.random.default_rng(3)
+    c = rng.uniform(-1, 1, (500, 3))
+    d = np.array([0.1, 0.07, 0.05])
+    a = np.array([0.3, -1.2, 0.8])
+    z0 = c @ a + 0.25
+    zc = octree.corners(c, d) @ a + 0.25
+    e = octree.interpolation_error(z0, zc)
+    assert e.max() < 1e-12
+    assert not octree.error_marks([z0], [zc], 1.0).any()
+    zq = zc + 0.5 * (octree.corners(c, d)[:, 0] - np.repeat(c[:, 0], 8)) ** 2
+    assert octree.error_marks([z0], [zq], 1.0).any() or octree.interpolation_error(z0, zq).std() == 0
 
 
 def test_marching_cubes_vertex_counts_of_combination_model():
