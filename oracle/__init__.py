@@ -33,12 +33,15 @@ known-answer tests:
   (``test_example_models_I.py:71-88``), which also fixed the form of the
   octree's interpolation-error refinement (``octree`` module docstring);
 * pinned, counts: the combination model's marching-cubes vertex counts
-  (``test/test_modules/test_marching_cubes.py:44-47``, ``mesh`` module).
+  (``test/test_modules/test_marching_cubes.py:44-47``, ``mesh`` module);
+* pinned, value: the two-layer model's gravity, -1624.1714
+  (``test/test_modules/test_geophysics/test_gravity.py:89``, ``gravity``).
 
 Modules: ``covariance`` (kernel functions), ``kriging`` (matrix build, solve,
 evaluation), ``segmentation`` (sigmoid ids, series masks), ``octree`` (corner
 and interpolation-error refinement), ``pipeline`` (multi-series compute_model
-restatement), ``mesh`` (marching cubes), ``gravity`` (prism forward gravity,
-unpinned), ``mlp`` (the preconditioner network).
+restatement), ``mesh`` (marching cubes), ``gravity`` (prism forward gravity on
+centred grids, pinned by the reference's two-layer gravity value), ``mlp``
+(the preconditioner network).
 """
 from . import covariance, kriging, segmentation, octree, pipeline  # noqa: F401

@@ -9,11 +9,13 @@ engine's adapter moves the centres and radius into the transformed frame
 voxels are segmented, and ``Solutions.gravity`` is the density-weighted sum
 per device (``test/test_modules/test_geophysics/test_gravity.py:67-89``).
 The kernel construction and the tz formula live in the absent engine; this
-module restates the published design:
+module restates the published design (GemPy's centred grid, carried over from
+its version 2, as the test's own comment on the radius says):
 
 * the kernel, per axis: x and y symmetric about the device at
   ``radius * [-g[::-1], 0, g]`` with ``g = geomspace(0.01, 1, resolution // 2)``;
-  z only below it at ``-radius * (0.05 + [0, geomspace(0.01, 1, resolution)])``;
+  z only below it at ``-1.2 * radius * (0.05 + [0, geomspace(0.01, 1,
+  resolution)])`` (the vertical axis reaches 1.2 radii);
   each voxel reaches half-way to its neighbours, and the outermost voxels
   as far out as they reach in (so the voxels tile a box); voxels in ``ij``
   order (x slowest);
@@ -24,20 +26,22 @@ module restates the published design:
   voxel v of device d.
 
 ``tests/test_oracle.py`` checks the prism formula against numerical
-quadrature and the tiling against the attraction of the whole box.  The
-reference's value for its two-layer model (-1624.1714) is not reproduced by
-this kernel (it gives -1467.4): parity of gravity is unpinned.
+quadrature, the tiling against the attraction of the whole box, and the
+reference's value for its two-layer model: every kernel voxel lies in the
+basement (density 3.2), and 3.2 x sum(tz) = -1624.17138, the reference's
+-1624.1714 to its 4 decimals (``test_gravity.py:89``).
 """
 import numpy as np
 
 G_MGAL = 6.674e-3
+Z_STRETCH = 1.2     # the vertical axis of the kernel reaches 1.2 radii below the device
 
 
 def axis_nodes(resolution, radius, vertical):
     """Voxel centres along one axis and their lower/upper half-widths."""
     if vertical:
         g = np.geomspace(0.01, 1.0, int(resolution))
-        c = -radius * (0.05 + np.concatenate(([0.0], g)))
+        c = -Z_STRETCH * radius * (0.05 + np.concatenate(([0.0], g)))
         c = c[::-1]                      # increasing z
     else:
         g = np.geomspace(0.01, 1.0, int(resolution) // 2)

@@ -9,9 +9,9 @@ atan differ by an ulp or two, so tz agrees to 1e-11 of the largest |tz|.
 Gravity sums density x tz over the voxels in a fixed order on each side:
 1e-11 relative.  Lithology ids of the kernel points are compared exactly.
 
-The reference's value for this model, -1624.1714, depends on the absent
-engine's centred-grid kernel and is not reproduced (the kernel here gives
--1466.88): gravity parity is against the oracle only."""
+The reference's value for this model, -1624.1714 (test_gravity.py:89,
+``assert_almost_equal(..., decimal=4)``), is reproduced through
+compute_model on the GPU."""
 import numpy as np
 import pytest
 
@@ -84,6 +84,8 @@ def test_compute_model_gravity_matches_oracle(centers, resolution, radius):
         # the reference's kernel lies far below both surfaces: basement only
         assert (ids == 3).all()
         assert abs(sol.gravity[0] - 3.2 * ograv.tz(resolution, radius).sum()) <= 1e-11 * abs(sol.gravity[0])
+        # the reference's own check (test_gravity.py:89)
+        np.testing.assert_almost_equal(sol.gravity, np.array([-1624.1714]), decimal=4)
 
 
 def test_gravity_reduction_is_deterministic():

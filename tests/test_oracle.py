@@ -339,6 +339,20 @@ def test_prism_attraction_matches_quadrature_and_kernel_tiles_its_box():
     assert (t < 0).all()        # every voxel lies below the device
 
 
+def test_two_layer_gravity_value():
+    """The reference's gravity pin (test/test_modules/test_geophysics/
+    test_gravity.py:67-89): its kernel ([10, 10, 100], radius 16000, device at
+    the model's top) lies wholly in the basement (density 3.2, id 3 of the two
+    horizontal surfaces at z = 3.05 and 1.02), so the value is 3.2 x sum(tz);
+    the reference checks it to 4 decimals.  The vertical stretch of the kernel
+    decides it: without it the sum would be 10 % smaller."""
+    from oracle import gravity
+    c, lo, hi = gravity.kernel([10, 10, 100], 16000.0)
+    assert (c[:, 2] + hi[:, 2] + 4.0 < 1.02).all()      # every voxel below the lower surface
+    g = 3.2 * gravity.tz([10, 10, 100], 16000.0).sum()
+    np.testing.assert_almost_equal(np.array([g]), np.array([-1624.1714]), decimal=4)
+
+
 def test_centered_grid_matches_oracle_kernel():
     """The package's CenteredGrid (host set-up of the gravity grid) builds the
     oracle's kernel: same voxel centres and half-widths, device-major points."""
