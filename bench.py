@@ -37,7 +37,7 @@ sys.path.insert(0, ROOT)
 METRIC = "grid points/s + kriging solves/s: mixed/learned vs FP64 GPU at 1e-6 field error"
 # thread instructions per point-record pair of the float-float field kernel,
 # from ncu's executed-instruction count (profiles/eval_ff_precision_64.md)
-FF_OPS_PER_PAIR = 80
+FF_OPS_PER_PAIR = 76
 WORKLOAD = ("precision: 1 series, 4000 surface points on 8 folded surfaces, 1500 orientations "
             "(N=8495), cubic, linear drift, 256^3 regular grid")
 

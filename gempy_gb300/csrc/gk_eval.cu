@@ -501,6 +501,7 @@ __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const 
     __shared__ __align__(8) uint64_t mbar[2];
     __shared__ int s_fail, s_abort;
     __shared__ float s_box[6 * 8];
+    __shared__ float s_fold[10 * 8];
     const int tid = threadIdx.x;
     const int split = SPLIT ? P.split : 1;
     unsigned char* stage[2] = {smem, smem + P.stage_bytes};
@@ -632,18 +633,23 @@ __global__ void __launch_bounds__(256) eval_ff_kernel(const EvalParams P, const 
                     }
                     in_range = far2 * 1.001f + eps2 < 0.999f;
                 }
-                // the tile's weight sum, for the in-range surface-point path (all
-                // threads take part: in_range and ori are uniform over the CTA)
-                ff wsum = {0.f, 0.f};
-                if (in_range && !ori) wsum = cta_weight_sum(rec, nr, s_box);
+                // the in-range column path folds the constant and r^2 terms of
+                // the covariances into per-tile sums, which start the points'
+                // accumulators (all threads take part in the reduction: in_range
+                // and ori are uniform over the CTA)
+                ff fold[5];
+                const float o[3] = {0.5f * (pbox[0] + pbox[3]), 0.5f * (pbox[1] + pbox[4]),
+                                    0.5f * (pbox[2] + pbox[5])};
+                if (in_range) cta_fold_sums(rec, nr, ori, o, fold, s_fold);
                 bool done = !any_act;
                 if (!done && col && all_exact && all_act) {
                     if (in_range) {
-                        if (!ori) {
 #pragma unroll
-                            for (int p = 0; p < PPT; ++p) acc[p] = {wsum.h, wsum.l};
+                        for (int p = 0; p < PPT; ++p) {
+                            const ff f0 = tile_fold(fold, ori, X[p], o, eps2);
+                            acc[p] = {f0.h, f0.l};
                         }
-                        ff_tile_col<PPT, false>(rec, ori, nr, X, eps2, acc);
+                        ff_tile_col<PPT, false, true>(rec, ori, nr, X, eps2, acc);
                     } else {
                         ff_tile_col<PPT, true>(rec, ori, nr, X, eps2, acc);
                     }

@@ -126,6 +126,13 @@ __device__ __forceinline__ ff ff_lin_dom(ff x, float m, float c) {
     return {s.h, s.l + e};
 }
 
+// a * b left unnormalised (|lo| a few ulps of hi): for operands that are
+// only read through exact products
+__device__ __forceinline__ ff ff_mul_un(ff a, ff b) {
+    const ff p = two_prod(a.h, b.h);
+    return {p.h, __fmaf_rn(a.h, b.l, __fmaf_rn(a.l, b.h, p.l))};
+}
+
 __device__ __forceinline__ ff ff_cubic_C(ff s2, ff s) {
     ff c = ff_lin_dom(s2, 0.75f, -3.5f);
     c = ff_horner_dom(s2, c, 8.75f);
@@ -301,10 +308,14 @@ __device__ __forceinline__ void ff_tile(const float* __restrict__ rec, bool orie
 // orientation record, the x and y terms of w . h are formed once per record
 // and shared; only the z terms are per point.
 // CUT = false: the caller has shown that every pair lies within the range,
-// so the per-pair range test is compiled out, and for surface-point records
-// the caller starts each accumulator at the tile's sum of weights
-// (cta_weight_sum): C = 1 + s^2 k, so only W s^2 k is accumulated per pair.
-template <int NP, bool CUT = true>
+// so the per-pair range test is compiled out.  Then, without FOLD, the caller
+// starts each accumulator of a surface-point tile at the tile's sum of
+// weights (cta_weight_sum): C = 1 + s^2 k, so only W s^2 k is accumulated per
+// pair.  With FOLD, the caller starts each accumulator at the tile's terms
+// that are polynomials in x (cta_fold_sums, tile_fold): for surface-point records
+// C = 1 - 7 s^2 + s^3 m(s), and only W s^3 m is accumulated per pair; for
+// orientation records a^2 C'/r = -14 + s m(s), and only s m (w . h) is.
+template <int NP, bool CUT = true, bool FOLD = false>
 __device__ __forceinline__ void ff_tile_col(const float* __restrict__ rec, bool orientation, int nr,
                                             const PointFF (&X)[NP], float eps2, ffacc (&acc)[NP]) {
     for (int qr = 0; qr < nr; ++qr) {
@@ -335,8 +346,17 @@ __device__ __forceinline__ void ff_tile_col(const float* __restrict__ rec, bool 
                 float low = lxy + s2.l + b2.l;
                 low = __fmaf_rn(dl2, 2.f * dh2 + dl2, low);
                 const ff r2 = fast_two_sum(s2.h, low);
-                if (CUT && r2.h >= 1.f) continue;  // beyond the range: C'/r = 0
-                const ff k = ff_cubic_d1(r2, ff_sqrt_pos(r2));
+                ff k;
+                if (CUT || !FOLD) {
+                    if (CUT && r2.h >= 1.f) continue;  // beyond the range: C'/r = 0
+                    k = ff_cubic_d1(r2, ff_sqrt_pos(r2));
+                } else {
+                    // every pair in range: a^2 C'/r = -14 + s m(s), and the caller
+                    // added the tile's -14 sum_o w_o . (x_o - x), so only s m is used
+                    k = ff_lin_dom(r2, 5.25f, -17.5f);
+                    k = ff_horner_dom(r2, k, 26.25f);
+                    k = ff_mul_un(ff_sqrt_pos(r2), k);
+                }
                 const ff q2 = two_prod(wz.h, -dh2);
                 const float e2 = __fmaf_rn(wz.h, -dl2, __fmaf_rn(wz.l, -dh2, q2.l));
                 const ff sz = two_sum(sw.h, q2.h);
@@ -355,16 +375,21 @@ __device__ __forceinline__ void ff_tile_col(const float* __restrict__ rec, bool 
                 if (CUT) {
                     if (r2.h >= 1.f) continue;  // beyond the range: C = 0
                     ff_acc_fma(acc[p], ff_cubic_C(r2, ff_sqrt_pos(r2)), W);
-                } else {
+                } else if (!FOLD) {
                     // every pair in range: C = 1 + s^2 k, and the caller started the
                     // accumulators at the tile's sum of weights, so only W s^2 k is added
                     const ff s = ff_sqrt_pos(r2);
                     ff k = ff_lin_dom(r2, 0.75f, -3.5f);
                     k = ff_horner_dom(r2, k, 8.75f);
                     k = ff_horner_dom(s, k, -7.f);
-                    const ff q = two_prod(r2.h, k.h);
-                    const float e = __fmaf_rn(r2.h, k.l, __fmaf_rn(r2.l, k.h, q.l));
-                    ff_acc_fma(acc[p], ff{q.h, e}, W);
+                    ff_acc_fma(acc[p], ff_mul_un(r2, k), W);
+                } else {
+                    // every pair in range: C = 1 - 7 s^2 + s^3 m(s), and the caller
+                    // added the tile's sum of W (1 - 7 s^2) (a quadratic in x), so
+                    // only W s^3 m is added
+                    ff m = ff_lin_dom(r2, 0.75f, -3.5f);
+                    m = ff_horner_dom(r2, m, 8.75f);
+                    ff_acc_fma(acc[p], ff_mul_un(r2, ff_mul_un(ff_sqrt_pos(r2), m)), W);
                 }
             }
         }
@@ -395,6 +420,69 @@ __device__ __forceinline__ void cta_bbox(float (&v)[6], float* sh) {
         v[c] = r;
     }
     __syncthreads();
+}
+
+// The sums behind the constant and r^2 terms of an in-range tile, in
+// float-float on the FP32 pipe, reduced over the CTA in a fixed order (every
+// thread gets them), with record positions p taken relative to the centre o
+// of the CTA's points (which keeps the terms of |x - p|^2 small).  Surface-
+// point records: f = {sum W, sum W (p - o) (3), sum W |p - o|^2}; orientation
+// records: f = {sum w . (x_o - o), sum w (3), 0}.  sh holds 10 floats per warp.
+__device__ __forceinline__ void cta_fold_sums(const float* __restrict__ rec, int nr, bool orientation,
+                                              const float (&o)[3], ff (&f)[5], float* sh) {
+#pragma unroll
+    for (int c = 0; c < 5; ++c) f[c] = {0.f, 0.f};
+    for (int r = threadIdx.x; r < nr; r += blockDim.x) {
+        const float* R = rec + (orientation ? 16 : 8) * r;
+        const ff px = ff_add_f(ff{R[0], R[1]}, -o[0]), py = ff_add_f(ff{R[2], R[3]}, -o[1]),
+                 pz = ff_add_f(ff{R[4], R[5]}, -o[2]);
+        if (orientation) {
+            const ff wx = {R[6], R[7]}, wy = {R[8], R[9]}, wz = {R[10], R[11]};
+            f[0] = ff_add(f[0], ff_dot3(wx, wy, wz, px, py, pz));
+            f[1] = ff_add(f[1], wx);
+            f[2] = ff_add(f[2], wy);
+            f[3] = ff_add(f[3], wz);
+        } else {
+            const ff w = {R[6], R[7]};
+            f[0] = ff_add(f[0], w);
+            f[1] = ff_add(f[1], ff_mul(w, px));
+            f[2] = ff_add(f[2], ff_mul(w, py));
+            f[3] = ff_add(f[3], ff_mul(w, pz));
+            f[4] = ff_add(f[4], ff_mul(w, ff_dot3(px, py, pz, px, py, pz)));
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 5; ++c)
+        for (int o = 16; o > 0; o >>= 1)
+            f[c] = ff_add(f[c], ff{__shfl_xor_sync(0xffffffffu, f[c].h, o), __shfl_xor_sync(0xffffffffu, f[c].l, o)});
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane == 0)
+        for (int c = 0; c < 5; ++c) {
+            sh[10 * wid + 2 * c] = f[c].h;
+            sh[10 * wid + 2 * c + 1] = f[c].l;
+        }
+    __syncthreads();
+    for (int c = 0; c < 5; ++c) {
+        ff t = {sh[2 * c], sh[2 * c + 1]};
+        for (int w = 1; w < nw; ++w) t = ff_add(t, ff{sh[10 * w + 2 * c], sh[10 * w + 2 * c + 1]});
+        f[c] = t;
+    }
+    __syncthreads();
+}
+
+// The folded terms of an in-range tile at point x (scaled, float-float; f
+// and o from cta_fold_sums): surface points sum W (1 - 7 (|x - p|^2 + eps2)),
+// orientations -14 sum w . (x_o - x).  The start value of the point's
+// accumulator.
+__device__ __forceinline__ ff tile_fold(const ff (&f)[5], bool orientation, const PointFF& X, const float (&o)[3],
+                                        float eps2) {
+    const ff x = ff_add_f(ff{X.h[0], X.l[0]}, -o[0]), y = ff_add_f(ff{X.h[1], X.l[1]}, -o[1]),
+             z = ff_add_f(ff{X.h[2], X.l[2]}, -o[2]);
+    const ff xf = ff_dot3(x, y, z, f[1], f[2], f[3]);
+    if (orientation) return ff_mul_f(ff_add(f[0], ff{-xf.h, -xf.l}), -14.f);
+    const ff xx = ff_add_f(ff_dot3(x, y, z, x, y, z), eps2);
+    const ff r2 = ff_add(ff_add(ff_mul(f[0], xx), ff{-2.f * xf.h, -2.f * xf.l}), f[4]);
+    return ff_add(f[0], ff_mul_f(r2, -7.f));
 }
 
 // Sum of the weights of a tile's nr surface-point records (float-float,
