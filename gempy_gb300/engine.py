@@ -495,6 +495,21 @@ def _isovalues(dev_s, model):
     return iso_t
 
 
+def octree_refine_mode(level, n_levels, min_level, levels_surface, error_threshold):
+    """``refine`` of gk_octree_level for octree level ``level``: 0 on the last
+    level; 2 (every voxel) while the next level is below ``octree_min_level``;
+    3 (corner ids and the interpolation-error statistic) while the next level
+    is also below ``number_octree_levels_surface - 1`` and
+    ``octree_error_threshold`` > 0; else 1 (corner ids)."""
+    if level == n_levels - 1:
+        return 0
+    if level + 1 < min_level:
+        return 2
+    if error_threshold > 0 and level + 1 < levels_surface - 1:
+        return 3
+    return 1
+
+
 def compute_model(interpolation_input, options, data_descriptor, geophysics_input=None,
                   config: Optional[EngineConfig] = None) -> Solutions:
     if not torch.cuda.is_available():
@@ -600,10 +615,7 @@ def _compute_model(interpolation_input, options, data_descriptor, geophysics_inp
         for level in range(n_levels):
             last = level == n_levels - 1
             surface = level < levels_surface
-            refine_all = level + 1 < min_level
-            refine = 0 if last else (2 if refine_all else 1)
-            if refine == 1 and error_threshold > 0 and level + 1 < levels_surface - 1:
-                refine = 3   # corner marks plus the interpolation-error statistic
+            refine = octree_refine_mode(level, n_levels, min_level, levels_surface, error_threshold)
             lvl = K.OctreeLevel(ss, centres, d, prec, corners=surface or refine in (1, 3), refine=refine,
                                 fault_series=ev._frows, error_threshold=error_threshold)
             grads = [None] * len(series)

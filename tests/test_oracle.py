@@ -364,3 +364,32 @@ def test_centered_grid_matches_oracle_kernel():
     np.testing.assert_array_equal(cg.left_voxel_edges, lo)
     np.testing.assert_array_equal(cg.right_voxel_edges, hi)
     np.testing.assert_array_equal(cg.values, gravity.points(cg.centers, [10, 10, 100], [16000.0, 8000.0, 16000.0]))
+
+
+def test_engine_refine_modes_follow_the_oracle(monkeypatch):
+    """The engine's choice of refinement per octree level (gk_octree_level's
+    ``refine``: 0 last, 2 all, 3 corners + error statistic, 1 corners) is the
+    oracle's: the levels where the oracle applies its error statistic are
+    exactly those where the engine asks for mode 3."""
+    from gempy_gb300.engine import octree_refine_mode
+    from oracle import inputs, octree
+    g = load_golden("anticline_corners.json")
+    series, rels, fr = inputs.series_from_golden(g)
+    ext = inputs.golden_extent(g)
+    for n_levels, min_level, ls, t in [(4, 2, 4, 1.0), (4, 2, 4, 0.0), (4, 1, 4, 1.0), (4, 2, 5, 1.0),
+                                       (3, 2, 2, 1.0), (4, 3, 6, 2.0)]:
+        called = []
+        real = octree.error_marks
+
+        def spy(centre_fields, corner_fields, n_std):
+            called.append(len(np.asarray(centre_fields[0])))
+            return real(centre_fields, corner_fields, n_std)
+        monkeypatch.setattr(octree, "error_marks", spy)
+        lv = pipeline.compute_octree(series, rels, g["unit_values"], g["sigmoid_slope"], ext, [2, 2, 2], n_levels,
+                                     min_level=min_level, fault_relations=fr, levels_surface=ls, error_threshold=t)
+        monkeypatch.setattr(octree, "error_marks", real)
+        sizes = [len(l.centres) for l in lv]
+        modes = [octree_refine_mode(L, n_levels, min_level, ls, t) for L in range(len(lv))]
+        assert modes[-1] == 0
+        assert [sizes[L] for L, m in enumerate(modes) if m == 3] == called
+        assert all(m == 2 for L, m in enumerate(modes) if L + 1 < min_level and L < n_levels - 1)
