@@ -24,6 +24,7 @@ There is no CPU path: without the CUDA library this raises.
 import dataclasses
 import os
 import time
+import warnings
 from dataclasses import dataclass
 from typing import List, Optional
 
@@ -607,6 +608,9 @@ def _compute_model(interpolation_input, options, data_descriptor, geophysics_inp
     min_level = int(eo.octree_min_level)
     levels_surface = int(getattr(eo, "number_octree_levels_surface", getattr(eo, "_number_octree_levels_surface", 0)))
     error_threshold = float(getattr(eo, "octree_error_threshold", 1.0))
+    if float(getattr(eo, "octree_curvature_threshold", -1.0)) >= 0 and grid.octree_grid is not None:
+        warnings.warn("octree_curvature_threshold is not supported: the octree refines by corner ids and "
+                      "the interpolation-error statistic only", RuntimeWarning, stacklevel=3)
     if grid.octree_grid is not None and n_levels >= 1:
         og = grid.octree_grid
         centres = torch.as_tensor(og.values).to(device)
