@@ -393,3 +393,16 @@ def test_engine_refine_modes_follow_the_oracle(monkeypatch):
         assert modes[-1] == 0
         assert [sizes[L] for L, m in enumerate(modes) if m == 3] == called
         assert all(m == 2 for L, m in enumerate(modes) if L + 1 < min_level and L < n_levels - 1)
+
+
+def test_field_pool_matches_serial_evaluation():
+    """The CPU baseline's worker pool (oracle/parallel.py) returns the serial
+    evaluation's field bit for bit, in point order."""
+    from oracle.parallel import FieldPool
+    g = load_golden("anticline_corners.json")
+    s = oracle_series_from_golden(g)
+    w = kriging.solve(*kriging.build_system(s))
+    x = np.random.default_rng(5).uniform(-0.3, 0.3, (5000, 3))
+    with FieldPool(s, 2) as pool:
+        z = pool.evaluate(x, w)
+    np.testing.assert_array_equal(z, kriging.evaluate(s, w, x))
