@@ -490,7 +490,7 @@ def main():
         line["batch"] = batch_section(n_real=args.batch_realisations)
         line["octree"] = octree_section()
         line["learned"] = learned_section(args.learned_points, args.learned_config)
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:   # host cores are shared by all ranks at N > 1
         line["cpu_baseline"] = cpu_baseline(m)
     if rank == 0:
         print(json.dumps(line), flush=True)
