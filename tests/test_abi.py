@@ -39,6 +39,8 @@ def test_library_exports_every_declared_symbol(lib):
     out = subprocess.run(["nm", "-D", "--defined-only", _lib.LIB_PATH], capture_output=True, text=True).stdout
     exported = set(re.findall(r"\bT (gk_[a-z0-9_]+)", out))
     assert set(header_functions()) <= exported
+    # and nothing is exported under the library's prefix that the header does not declare
+    assert exported <= set(header_functions())
 
 
 def test_version_and_size_queries_without_gpu(lib):
